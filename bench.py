@@ -1,0 +1,296 @@
+"""Benchmark: batched Helmholtz apply of a 16-orbital batch (k=9, prec 1e-6, absolute), nodes/s.
+
+One step = one level-synchronous batched apply of all 16 orbitals (each with its own
+mu_i = sqrt(-2 eps_i) operator and uneven tree) in norm-tiered mixed precision, inputs
+resident in device memory.  Beside it: the plain FP64 GPU apply of the same batch, the
+relative L2 error of every mixed output against the FP64 output, the end-to-end rate
+through the C ABI with host buffers (upload + apply + download), and the CPU oracle
+(OpenMP FP64) on a bounded sample of the same workload.
+
+Synthetic inputs stand in for an SCF state: phi_i = p_i(r - R_i) exp(-a_i |r - R_i|^2) with
+p_i a random cubic (20 N(0,1) coefficients), a_i log-uniform in [0.3, 20], R_i uniform in
+[-2, 2]^3, normalized; eps_i uniform in [-2, -0.1]; numpy default_rng(20261203).
+
+`--impl reference` times the CPU oracle alone (the reference's own CPU path, MRCPP, is not
+available to build) on the same metric.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+SEED = 20261203
+NORB, ORDER, PREC = 16, 9, 1e-6
+METRIC = "Helmholtz-apply nodes/s: batched mixed vs plain FP64 GPU at 1e-6 rel. error"
+
+
+def cubic_monomials():
+    return [(a, b, c) for a in range(4) for b in range(4) for c in range(4) if a + b + c <= 3]
+
+
+def orbital_terms(rng):
+    mons = cubic_monomials()
+    out = []
+    for _ in range(NORB):
+        alpha = float(np.exp(rng.uniform(np.log(0.3), np.log(20.0))))
+        R = rng.uniform(-2.0, 2.0, 3)
+        coefs = rng.standard_normal(len(mons))
+        out.append([(float(c), alpha, tuple(R), m) for c, m in zip(coefs, mons)])
+    eps = rng.uniform(-2.0, -0.1, NORB)
+    return out, np.sqrt(-2.0 * eps)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.samples, self.proc = [], None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", "0"], stdout=subprocess.PIPE, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(self.samples[0][1]) if self.samples[0][1].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_sample(terms, mus, max_iter):
+    """Oracle (OpenMP FP64) Helmholtz apply of orbital 0, first max_iter refinement levels."""
+    from oracle import pyoracle as po
+    po.build()
+    threads = os.cpu_count() or 1
+    po.set_threads(threads)
+    mra = po.MRA(ORDER)
+    phi = po.project_gauss(PREC, po.Tree(mra), terms[0], abs_prec=True)
+    phi.rescale(1.0 / phi.norm())
+    op = po.helmholtz(mra, float(mus[0]), PREC)
+    out = po.Tree(mra)
+    t0 = time.perf_counter()
+    st = po.apply(PREC, out, op, phi, max_iter=max_iter, abs_prec=True)
+    dt = time.perf_counter() - t0
+    return {"value": st["out_nodes"] / dt, "unit": "nodes/s", "cores": threads, "kind": "port",
+            "sample": "orbital 0 of the batch, levels 0..%d of the adaptive apply (%d output nodes, %.1f s)"
+                      % (max_iter, st["out_nodes"], dt)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    rng = np.random.default_rng(SEED)
+    terms, mus = orbital_terms(rng)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(terms, mus, args.cpu_levels)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s = cpu_sample(terms, mus, args.cpu_levels)
+        vals.append(s["value"])
+    wall = time.perf_counter() - t0
+    v = float(np.mean(vals))
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": "nodes/s", "n_gpus": args.gpus,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / max(args.steps, 1),
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic",
+                      "config": {"workload": "helmholtz-batch16-k9-prec1e-6", "orbitals": NORB, "order": ORDER,
+                                 "prec": PREC, "sample": s["sample"]},
+                      "cpu_baseline": {"value": v, "unit": "nodes/s", "cores": s["cores"], "kind": "port",
+                                       "sample": s["sample"]},
+                      "e2e": {"value": v, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def run(args):
+    import torch
+
+    import mrchem_gb300 as mw
+    from mrchem_gb300 import build as mwbuild
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    mwbuild.build()
+    mw.load_library()
+
+    rng = np.random.default_rng(SEED)
+    terms, mus = orbital_terms(rng)
+    mra = mw.MultiResolutionAnalysis(ORDER, device=local)
+    phis = []
+    for t in terms:
+        f = mw.project(PREC, mw.FunctionTree(mra), t, abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        phis.append(f)
+    t0 = time.perf_counter()
+    ops = [mw.HelmholtzOperator(mra, float(m), PREC) for m in mus]
+    op_build_s = time.perf_counter() - t0
+    in_nodes = [p.nnodes for p in phis]
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def step(precision, outs):
+        for o in outs:
+            o.clear()
+        return mw.apply_batch([PREC] * NORB, outs, ops, phis, abs_prec=True, precision=precision)
+
+    outs = [mw.FunctionTree(mra) for _ in range(NORB)]
+    # plain FP64 reference result (also the error reference)
+    barrier()
+    t0 = time.perf_counter()
+    st64 = step("fp64", outs)
+    barrier()
+    fp64_s = time.perf_counter() - t0
+    ref = [o.download()[1] for o in outs]
+
+    for _ in range(args.warmup):
+        step("mixed", outs)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    with ClockSampler() as clk:
+        barrier()
+        start.record()
+        for _ in range(args.steps):
+            stats.append(step("mixed", outs))
+        end.record()
+        barrier()
+    ms = start.elapsed_time(end) / args.steps
+    nodes = stats[-1]["out_nodes"]
+    errs = []
+    for o, r in zip(outs, ref):
+        c = o.download()[1]
+        errs.append(float(np.linalg.norm(c - r) / np.linalg.norm(r)) if c.shape == r.shape else float("inf"))
+    local_v = nodes / (ms / 1e3)
+    t_max = ms
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = nodes * world / (t_max / 1e3)
+
+    # end-to-end through the C ABI: host input buffers -> device, apply, device -> host output
+    host_inputs = [p.download() for p in phis]
+    e2e_phis = [mw.FunctionTree(mra) for _ in range(NORB)]
+    h2d = sum(k.nbytes + c.nbytes for k, c, _ in host_inputs)
+    barrier()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(args.e2e_steps):
+        for f, (k, c, _) in zip(e2e_phis, host_inputs):
+            f.upload(k, c)
+        for o in outs:
+            o.clear()
+        mw.apply_batch([PREC] * NORB, outs, ops, e2e_phis, abs_prec=True, precision="mixed")
+        d2h = 0
+        for o in outs:
+            k, c, lf = o.download()
+            d2h += k.nbytes + c.nbytes + lf.nbytes
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    e2e_v = nodes * world / e2e_s
+
+    st = stats[-1]
+    kern_s = st["kernel_ms"] / 1e3
+    peaks = measured_peaks()
+    fp64_tf = args.fp64_peak_tflops
+    achieved = st["flops"] / kern_s / 1e12 if kern_s > 0 else 0.0
+    roofline = {"bound": "fp64-pipe", "achieved": achieved, "peak": fp64_tf, "unit": "TFLOP/s",
+                "frac": achieved / fp64_tf if fp64_tf else None, "traffic": None,
+                "kernel": "apply_kernel (FP64 + FP32 tiers)",
+                "note": "algorithmic 6K^4 flops per surviving component pair over the CUDA-event time of the "
+                        "contraction launches; FP64 peak probed on this GPU"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "config": {"workload": "helmholtz-batch16-k9-prec1e-6", "orbitals": NORB, "order": ORDER, "prec": PREC,
+                   "basis": "interpolating", "box": "[-32,32]^3", "input_nodes": in_nodes,
+                   "output_nodes": nodes, "l2": "inputs larger than L2 (%.1f GB of FP64 blocks)"
+                   % (sum(in_nodes) * 8 * (ORDER + 1) ** 3 * 8 / 1e9),
+                   "operator_terms": [o.nterms for o in ops], "operator_build_s": op_build_s},
+        "fp64": {"value": st64["out_nodes"] * world / fp64_s, "unit": "nodes/s", "seconds": fp64_s,
+                 "items": st64["items"]},
+        "speedup_mixed_vs_fp64": (st64["out_nodes"] / fp64_s) / (nodes / (ms / 1e3)),
+        "rel_l2_vs_fp64_max": max(errs),
+        "items": {"total": st["items"], "fp64": st["items_fp64"], "fp32": st["items_fp32"]},
+        "kernel_ms_per_step": st["kernel_ms"], "host_ms_per_step": st["host_ms"],
+        "gpu_launches": int(st["launches"]),
+        "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": roofline,
+        "clocks": clk.summary(),
+    }
+    line["speedup_mixed_vs_fp64"] = (nodes / (ms / 1e3)) / (st64["out_nodes"] / fp64_s)
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(terms, mus, args.cpu_levels)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-levels", type=int, default=4)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fp64-peak-tflops", type=float, default=1.25)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run(args)
+
+
+if __name__ == "__main__":
+    main()

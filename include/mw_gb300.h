@@ -1,0 +1,146 @@
+/*
+ * mw_gb300.h -- C ABI of the GB300-native multiwavelet apply engine.
+ *
+ * Drop-in boundary for the mrcpp:: calls MRChem makes on its hot path
+ * (MRCPP commit 0e5b32003eed8e1abb22a44ba4e1a2ce9fd9ddb1, fetched by
+ * external/upstream/fetch_mrcpp.cmake:39-42).  Plain pointers and sizes only.
+ * Every entry returns an int status (MW_OK = 0); mw_last_error() gives the
+ * message of the last failure on a context.  Calls on one context are
+ * serialised on that context's CUDA stream; trees and operators belong to
+ * the context that created them.
+ *
+ * Conventions:
+ *   node key   int[4] = (n, lx, ly, lz): the box [2^-n l, 2^-n (l+1)]^3
+ *   block      8 * K^3 doubles (K = order + 1): component c = cx|cy<<1|cz<<2
+ *              (bit set = wavelet in that dimension), inner index
+ *              ix + K*iy + K*K*iz.  Component 0 holds the node's scaling
+ *              coefficients, components 1..7 its wavelet coefficients.
+ *   tree       complete octree: every node has 0 or 8 children; host arrays
+ *              are in canonical order (by scale, then Morton order with z
+ *              most significant).
+ */
+#ifndef MW_GB300_H
+#define MW_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MW_OK 0
+#define MW_ERR_ARG 1
+#define MW_ERR_OOM 2
+#define MW_ERR_CUDA 3
+#define MW_ERR_TIMEOUT 4
+#define MW_ERR_STATE 5
+
+#define MW_BASIS_LEGENDRE 0
+#define MW_BASIS_INTERPOLATING 1
+
+/* precision modes of mw_apply / mw_apply_batch */
+#define MW_PREC_FP64 0   /* every contraction in FP64 */
+#define MW_PREC_MIXED 1  /* norm-tiered FP64 / FP32 / BF16 tensor-core contractions */
+
+typedef struct mw_ctx_s *mw_ctx;
+typedef struct mw_tree_s *mw_tree;
+typedef struct mw_op_s *mw_op;
+
+/* coef * (x-X)^px (y-Y)^py (z-Z)^pz * exp(-alpha |r-R|^2) */
+typedef struct {
+    double coef;
+    double alpha;
+    double pos[3];
+    int pw[3];
+    int pad;
+} mw_gterm;
+
+typedef struct {
+    long long out_nodes;     /* output nodes computed */
+    long long items;         /* (output node, input node, term) contractions */
+    long long items_fp64;    /* ... of which in FP64 */
+    long long items_fp32;    /* ... in FP32 */
+    long long items_bf16;    /* ... in BF16 tensor-core */
+    long long generated;     /* generated input nodes */
+    long long levels;        /* refinement iterations */
+    long long launches;      /* kernels launched */
+    double flops;            /* algorithmic: 6 K^4 per surviving component pair */
+    double flops_issued;     /* as executed by the kernels */
+    double bytes;            /* algorithmic coefficient + operator bytes */
+    double kernel_ms;        /* CUDA-event time of the contraction kernels */
+    double host_ms;          /* wall time of the call */
+} mw_stats;
+
+/* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */
+int mw_ctx_create(int device, int root_scale, const int corner[3], const int boxes[3], int order, int basis,
+                  int max_depth, mw_ctx *out);
+int mw_ctx_destroy(mw_ctx ctx);
+const char *mw_last_error(mw_ctx ctx);
+int mw_ctx_basis(mw_ctx ctx, double *qx, double *qw, double *filter, double *c2v, double *v2c);
+int mw_ctx_last_stats(mw_ctx ctx, mw_stats *st);
+int mw_ctx_synchronize(mw_ctx ctx);
+
+/* ---- trees (replaces FunctionTree<3>, src/qmfunctions/Orbital.h:51) ---- */
+int mw_tree_create(mw_ctx ctx, mw_tree *out);
+int mw_tree_destroy(mw_tree t);
+int mw_tree_nnodes(mw_tree t, int *n);
+int mw_tree_nleaves(mw_tree t, int *n);
+int mw_tree_depth(mw_tree t, int *d);
+int mw_tree_upload(mw_tree t, int nnodes, const int *keys, const double *coefs);
+int mw_tree_download(mw_tree t, int *keys, double *coefs, unsigned char *is_leaf);
+int mw_tree_squared_norm(mw_tree t, double *out);
+int mw_tree_integrate(mw_tree t, double *out);
+int mw_tree_rescale(mw_tree t, double c);
+int mw_tree_eval(mw_tree t, int npts, const double *xyz, double *out);
+/* FunctionTree::clear / mrcpp::clear: back to the root nodes, zero coefficients */
+int mw_tree_clear(mw_tree t);
+
+/* mrcpp::project(prec, tree, GaussExp<3>) (src/qmfunctions/...; density_utils.cpp) */
+int mw_project_gauss(double prec, mw_tree out, int nterms, const mw_gterm *terms, int abs_prec);
+/* hydrogen-like orbital n, l (<= 1), m (x,y,z for l = 1), src/analyticfunctions/HydrogenFunction.cpp:35-198 */
+int mw_project_hydrogen(double prec, mw_tree out, int n, int l, int m, double Z, const double origin[3], int abs_prec);
+
+/* grids: mrcpp::copy_grid / build_grid / copy_func (src/qmfunctions/density_utils.cpp:72,85,87) */
+int mw_copy_grid(mw_tree out, mw_tree inp);
+int mw_build_grid(mw_tree out, int n, const mw_tree *trees);
+int mw_copy_func(mw_tree out, mw_tree inp);
+/* FunctionTree::crop(prec) (src/qmfunctions/density_utils.cpp:147) */
+int mw_crop(mw_tree t, double prec, int abs_prec);
+/* mrcpp::dot (src/qmfunctions/orbital_utils.cpp:79-82) */
+int mw_dot(mw_tree a, mw_tree b, double *out);
+
+/* ---- operators (src/driver.cpp:1131,1283; src/scf_solver/HelmholtzVector.cpp:144) ---- */
+int mw_op_create_poisson(mw_ctx ctx, double prec, mw_op *out);
+int mw_op_create_helmholtz(mw_ctx ctx, double mu, double prec, mw_op *out);
+int mw_op_destroy(mw_op op);
+int mw_op_nterms(mw_op op, int *n);
+int mw_op_terms(mw_op op, double *coefs, double *exps);
+int mw_op_band(mw_op op, int term, int scale, int *band);
+int mw_op_block(mw_op op, int term, int scale, int l, double *blk, double *norms4);
+
+/* ---- the hot path ---- */
+/* mrcpp::apply(prec, out, oper, inp[, precTrees], maxIter, absPrec)
+ * (CoulombPotential.cpp:131,156; HelmholtzVector.cpp:149,154; ExchangePotential.cpp:200,204).
+ * out must be empty (root nodes only); nprec = 0 for the plain call. */
+int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const mw_tree *prec_trees, int max_iter,
+             int abs_prec, int precision_mode);
+/* n independent applies (own operator, input, output, prec) in lockstep, one launch per level
+ * (HelmholtzVector::operator(), src/scf_solver/HelmholtzVector.cpp:70-91) */
+int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, int max_iter, int abs_prec,
+                   int precision_mode);
+/* apply on a fixed output grid (the output's current grid, no refinement) */
+int mw_apply_fixed(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec, int precision_mode);
+/* transpose apply: out = O^T inp on the fixed grid of out (adjoint of mw_apply_fixed) */
+int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec);
+
+/* mrcpp::multiply(prec, out, coef, a, b, maxIter, absPrec, useMaxNorms)
+ * (QMPotential.cpp:147; ExchangePotential.cpp:175,213,223); out's current grid is the start grid */
+int mw_multiply(double prec, mw_tree out, double coef, mw_tree a, mw_tree b, int max_iter, int abs_prec,
+                int use_max_norms);
+/* mrcpp::square(prec, out, inp) (src/qmfunctions/density_utils.cpp:73) */
+int mw_square(double prec, mw_tree out, mw_tree inp, int max_iter, int abs_prec);
+/* mrcpp::add(prec, out, FunctionTreeVector, maxIter) on the union grid (density_utils.cpp:85-86) */
+int mw_add(double prec, mw_tree out, int n, const double *coefs, const mw_tree *trees, int max_iter);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,454 @@
+"""GB300-native multiwavelet apply engine: Python mirror of the mrcpp:: call surface.
+
+The compute path is libmwgb300.so (CUDA sm_103a kernels + host C++ driver),
+loaded from the package's _lib/ directory through its C ABI
+(include/mw_gb300.h).  There is no host fallback: if the library is missing or
+no CUDA device is usable, the calls raise.
+
+Names and argument meaning follow the MRCPP calls MRChem makes on this path:
+    mrcpp::MultiResolutionAnalysis<3>      src/mrenv.cpp:105-122
+    mrcpp::PoissonOperator(MRA, prec)       src/driver.cpp:1131,1283
+    mrcpp::HelmholtzOperator(MRA, mu, prec) src/scf_solver/HelmholtzVector.cpp:144
+    mrcpp::apply(prec, out, oper, inp[, precTrees], maxIter, absPrec)
+                                            src/qmoperators/two_electron/CoulombPotential.cpp:131
+    mrcpp::multiply / square / add          src/qmoperators/QMPotential.cpp:147,
+                                            src/qmfunctions/density_utils.cpp:73,86
+    mrcpp::build_grid / copy_grid / copy_func / clear
+                                            src/qmfunctions/density_utils.cpp:72,85,87
+"""
+import ctypes as C
+import os
+import weakref
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmwgb300.so")
+
+MW_OK = 0
+PREC_FP64 = 0
+PREC_MIXED = 1
+_PREC = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
+
+
+class MWError(RuntimeError):
+    """Raised when an engine call returns a non-zero status."""
+
+    def __init__(self, code, msg):
+        super().__init__("mw error %d: %s" % (code, msg))
+        self.code = code
+
+
+class GTerm(C.Structure):
+    _fields_ = [("coef", C.c_double), ("alpha", C.c_double), ("pos", C.c_double * 3),
+                ("pw", C.c_int * 3), ("pad", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("out_nodes", C.c_longlong), ("items", C.c_longlong), ("items_fp64", C.c_longlong),
+                ("items_fp32", C.c_longlong), ("items_bf16", C.c_longlong), ("generated", C.c_longlong),
+                ("levels", C.c_longlong), ("launches", C.c_longlong), ("flops", C.c_double),
+                ("flops_issued", C.c_double), ("bytes", C.c_double), ("kernel_ms", C.c_double),
+                ("host_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+EXPORTS = [
+    "mw_ctx_create", "mw_ctx_destroy", "mw_last_error", "mw_ctx_basis", "mw_ctx_last_stats", "mw_ctx_synchronize",
+    "mw_tree_create", "mw_tree_destroy", "mw_tree_nnodes", "mw_tree_nleaves", "mw_tree_depth", "mw_tree_upload",
+    "mw_tree_download", "mw_tree_squared_norm", "mw_tree_integrate", "mw_tree_rescale", "mw_tree_eval",
+    "mw_tree_clear", "mw_project_gauss", "mw_project_hydrogen", "mw_copy_grid", "mw_build_grid", "mw_copy_func",
+    "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
+    "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
+    "mw_multiply", "mw_square", "mw_add",
+]
+
+
+def load_library(path=None):
+    """Loads libmwgb300.so (build it first with mrchem_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError("libmwgb300.so not built: run `python -m mrchem_gb300.build` (or __graft_entry__.build())")
+    L = C.CDLL(path)
+    P, I, D = C.c_void_p, C.c_int, C.c_double
+    ip, dp, pp = C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_void_p)
+    sig = {
+        "mw_ctx_create": [I, I, ip, ip, I, I, I, pp],
+        "mw_ctx_destroy": [P],
+        "mw_ctx_basis": [P, dp, dp, dp, dp, dp],
+        "mw_ctx_last_stats": [P, C.POINTER(Stats)],
+        "mw_ctx_synchronize": [P],
+        "mw_tree_create": [P, pp],
+        "mw_tree_destroy": [P],
+        "mw_tree_nnodes": [P, ip],
+        "mw_tree_nleaves": [P, ip],
+        "mw_tree_depth": [P, ip],
+        "mw_tree_upload": [P, I, ip, dp],
+        "mw_tree_download": [P, ip, dp, C.POINTER(C.c_ubyte)],
+        "mw_tree_squared_norm": [P, dp],
+        "mw_tree_integrate": [P, dp],
+        "mw_tree_rescale": [P, D],
+        "mw_tree_eval": [P, I, dp, dp],
+        "mw_tree_clear": [P],
+        "mw_project_gauss": [D, P, I, C.POINTER(GTerm), I],
+        "mw_project_hydrogen": [D, P, I, I, I, D, dp, I],
+        "mw_copy_grid": [P, P],
+        "mw_build_grid": [P, I, pp],
+        "mw_copy_func": [P, P],
+        "mw_crop": [P, D, I],
+        "mw_dot": [P, P, dp],
+        "mw_op_create_poisson": [P, D, pp],
+        "mw_op_create_helmholtz": [P, D, D, pp],
+        "mw_op_destroy": [P],
+        "mw_op_nterms": [P, ip],
+        "mw_op_terms": [P, dp, dp],
+        "mw_op_band": [P, I, I, ip],
+        "mw_op_block": [P, I, I, I, dp, dp],
+        "mw_apply": [D, P, P, P, I, pp, I, I, I],
+        "mw_apply_batch": [I, dp, pp, pp, pp, I, I, I],
+        "mw_apply_fixed": [D, P, P, P, I, I],
+        "mw_apply_adjoint": [D, P, P, P, I],
+        "mw_multiply": [D, P, D, P, P, I, I, I],
+        "mw_square": [D, P, P, I, I],
+        "mw_add": [D, P, I, dp, pp, I],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.mw_last_error.argtypes = [P]
+    L.mw_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _check(rc, ctx=None):
+    if rc != MW_OK:
+        msg = _lib.mw_last_error(ctx).decode() if _lib is not None else ""
+        raise MWError(rc, msg)
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class MultiResolutionAnalysis:
+    """World box [corner, corner + boxes] * 2^-root_scale with a scaling basis of the given order.
+
+    Mirrors mrcpp::MultiResolutionAnalysis<3>(BoundingBox<3>(root_scale, corner, boxes), Basis(order), max_depth)
+    (src/mrenv.cpp:105-122); the reference test fixture is order 5 interpolating on [-32,32]^3
+    (tests/unit_tests.cpp:66-84).
+    """
+
+    def __init__(self, order, root_scale=-5, corner=(-1, -1, -1), boxes=(2, 2, 2), basis="interpolating",
+                 max_depth=25, device=0):
+        L = load_library()
+        self.order, self.K = order, order + 1
+        self.root_scale, self.corner, self.boxes = root_scale, tuple(corner), tuple(boxes)
+        self.basis, self.max_depth = basis, max_depth
+        c = np.ascontiguousarray(corner, dtype=np.int32)
+        b = np.ascontiguousarray(boxes, dtype=np.int32)
+        h = C.c_void_p()
+        _check(L.mw_ctx_create(device, root_scale, _ip(c), _ip(b), order, 1 if basis == "interpolating" else 0,
+                               max_depth, C.byref(h)))
+        self.ptr = h.value
+        self._owned = weakref.WeakSet()  # trees and operators, released before the context
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            for obj in list(self._owned):
+                obj.close()
+            _lib.mw_ctx_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def basis_data(self):
+        K = self.K
+        qx, qw, W = np.zeros(K), np.zeros(K), np.zeros((2 * K, 2 * K))
+        c2v, v2c = np.zeros((K, K)), np.zeros((K, K))
+        _check(_lib.mw_ctx_basis(self.ptr, _dp(qx), _dp(qw), _dp(W), _dp(c2v), _dp(v2c)), self.ptr)
+        return dict(qx=qx, qw=qw, W=W, c2v=c2v, v2c=v2c)
+
+    def last_stats(self):
+        st = Stats()
+        _check(_lib.mw_ctx_last_stats(self.ptr, C.byref(st)), self.ptr)
+        return st.as_dict()
+
+    def synchronize(self):
+        _check(_lib.mw_ctx_synchronize(self.ptr), self.ptr)
+
+
+class FunctionTree:
+    """Device-resident adaptive function tree (mrcpp::FunctionTree<3>)."""
+
+    def __init__(self, mra):
+        self.mra = mra
+        h = C.c_void_p()
+        _check(_lib.mw_tree_create(mra.ptr, C.byref(h)), mra.ptr)
+        self.ptr = h.value
+        mra._owned.add(self)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            _lib.mw_tree_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _int(self, fn):
+        v = C.c_int()
+        _check(fn(self.ptr, C.byref(v)), self.mra.ptr)
+        return v.value
+
+    @property
+    def nnodes(self):
+        return self._int(_lib.mw_tree_nnodes)
+
+    def getNNodes(self):
+        return self.nnodes
+
+    @property
+    def nleaves(self):
+        return self._int(_lib.mw_tree_nleaves)
+
+    @property
+    def depth(self):
+        return self._int(_lib.mw_tree_depth)
+
+    def squared_norm(self):
+        v = C.c_double()
+        _check(_lib.mw_tree_squared_norm(self.ptr, C.byref(v)), self.mra.ptr)
+        return v.value
+
+    def norm(self):
+        return float(np.sqrt(self.squared_norm()))
+
+    def integrate(self):
+        v = C.c_double()
+        _check(_lib.mw_tree_integrate(self.ptr, C.byref(v)), self.mra.ptr)
+        return v.value
+
+    def rescale(self, c):
+        _check(_lib.mw_tree_rescale(self.ptr, float(c)), self.mra.ptr)
+
+    def evalf(self, points):
+        pts = np.ascontiguousarray(np.atleast_2d(points), dtype=np.float64)
+        out = np.zeros(pts.shape[0])
+        _check(_lib.mw_tree_eval(self.ptr, pts.shape[0], _dp(pts), _dp(out)), self.mra.ptr)
+        return out
+
+    def clear(self):
+        _check(_lib.mw_tree_clear(self.ptr), self.mra.ptr)
+
+    def crop(self, prec, abs_prec=False):
+        _check(_lib.mw_crop(self.ptr, prec, int(abs_prec)), self.mra.ptr)
+
+    def download(self):
+        """(keys[n,4] int32, coefs[n, 8K^3] float64, is_leaf[n] uint8) in canonical order."""
+        n = self.nnodes
+        keys = np.zeros((n, 4), dtype=np.int32)
+        coefs = np.zeros((n, 8 * self.mra.K ** 3))
+        leaf = np.zeros(n, dtype=np.uint8)
+        _check(_lib.mw_tree_download(self.ptr, _ip(keys), _dp(coefs), leaf.ctypes.data_as(C.POINTER(C.c_ubyte))),
+               self.mra.ptr)
+        return keys, coefs, leaf
+
+    def upload(self, keys, coefs):
+        keys = np.ascontiguousarray(keys, dtype=np.int32)
+        coefs = np.ascontiguousarray(coefs, dtype=np.float64)
+        _check(_lib.mw_tree_upload(self.ptr, keys.shape[0], _ip(keys), _dp(coefs)), self.mra.ptr)
+        return self
+
+
+def _gterms(terms):
+    arr = (GTerm * len(terms))()
+    for i, (c, a, pos, pw) in enumerate(terms):
+        arr[i].coef, arr[i].alpha = c, a
+        for d in range(3):
+            arr[i].pos[d] = pos[d]
+            arr[i].pw[d] = pw[d]
+    return arr
+
+
+def project(prec, tree, terms, abs_prec=False):
+    """mrcpp::project of a Gaussian expansion: terms = [(coef, alpha, (X,Y,Z), (px,py,pz)), ...]."""
+    arr = _gterms(terms)
+    _check(_lib.mw_project_gauss(prec, tree.ptr, len(terms), arr, int(abs_prec)), tree.mra.ptr)
+    return tree
+
+
+def project_hydrogen(prec, tree, n, l, m, Z=1.0, origin=(0.0, 0.0, 0.0), abs_prec=False):
+    """Projects the hydrogen-like orbital (n, l, m) of src/analyticfunctions/HydrogenFunction.cpp."""
+    o = np.ascontiguousarray(origin, dtype=np.float64)
+    _check(_lib.mw_project_hydrogen(prec, tree.ptr, n, l, m, Z, _dp(o), int(abs_prec)), tree.mra.ptr)
+    return tree
+
+
+class ConvolutionOperator:
+    def __init__(self, mra, ptr):
+        self.mra, self.ptr = mra, ptr
+        mra._owned.add(self)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            _lib.mw_op_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def nterms(self):
+        v = C.c_int()
+        _check(_lib.mw_op_nterms(self.ptr, C.byref(v)), self.mra.ptr)
+        return v.value
+
+    def terms(self):
+        T = self.nterms
+        c, a = np.zeros(T), np.zeros(T)
+        _check(_lib.mw_op_terms(self.ptr, _dp(c), _dp(a)), self.mra.ptr)
+        return c, a
+
+    def band(self, term, scale):
+        v = C.c_int()
+        _check(_lib.mw_op_band(self.ptr, term, scale, C.byref(v)), self.mra.ptr)
+        return v.value
+
+    def block(self, term, scale, l):
+        K = self.mra.K
+        b, nr = np.zeros((2 * K, 2 * K)), np.zeros(4)
+        _check(_lib.mw_op_block(self.ptr, term, scale, l, _dp(b), _dp(nr)), self.mra.ptr)
+        return b, nr
+
+
+class PoissonOperator(ConvolutionOperator):
+    """Separated Gaussian-sum expansion of 1/r (mrcpp::PoissonOperator(MRA, prec))."""
+
+    def __init__(self, mra, prec):
+        h = C.c_void_p()
+        _check(_lib.mw_op_create_poisson(mra.ptr, prec, C.byref(h)), mra.ptr)
+        super().__init__(mra, h.value)
+
+
+class HelmholtzOperator(ConvolutionOperator):
+    """Separated Gaussian-sum expansion of exp(-mu r)/r (mrcpp::HelmholtzOperator(MRA, mu, prec))."""
+
+    def __init__(self, mra, mu, prec):
+        h = C.c_void_p()
+        _check(_lib.mw_op_create_helmholtz(mra.ptr, mu, prec, C.byref(h)), mra.ptr)
+        super().__init__(mra, h.value)
+
+
+def _ptrs(trees):
+    return (C.c_void_p * max(1, len(trees)))(*[t.ptr for t in trees])
+
+
+def apply(prec, out, oper, inp, prec_trees=(), max_iter=-1, abs_prec=False, precision="fp64"):
+    """mrcpp::apply(prec, out, oper, inp[, precTrees], maxIter, absPrec); returns the call's statistics."""
+    _check(_lib.mw_apply(prec, out.ptr, oper.ptr, inp.ptr, len(prec_trees), _ptrs(prec_trees), max_iter,
+                         int(abs_prec), _PREC[precision]), out.mra.ptr)
+    return out.mra.last_stats()
+
+
+def apply_batch(precs, outs, opers, inps, max_iter=-1, abs_prec=False, precision="fp64"):
+    """Independent applies (own operator, input, output) run level-synchronously in shared launches."""
+    n = len(outs)
+    p = np.ascontiguousarray(precs if np.ndim(precs) else [precs] * n, dtype=np.float64)
+    _check(_lib.mw_apply_batch(n, _dp(p), _ptrs(outs), _ptrs(opers), _ptrs(inps), max_iter, int(abs_prec),
+                               _PREC[precision]), outs[0].mra.ptr)
+    return outs[0].mra.last_stats()
+
+
+def apply_fixed(prec, out, oper, inp, abs_prec=False, precision="fp64"):
+    """apply on out's current grid (no refinement)."""
+    _check(_lib.mw_apply_fixed(prec, out.ptr, oper.ptr, inp.ptr, int(abs_prec), _PREC[precision]), out.mra.ptr)
+    return out.mra.last_stats()
+
+
+def multiply(prec, out, coef, a, b, max_iter=-1, abs_prec=False, use_max_norms=False):
+    """mrcpp::multiply(prec, out, coef, a, b, maxIter, absPrec, useMaxNorms); out's grid is the start grid."""
+    _check(_lib.mw_multiply(prec, out.ptr, coef, a.ptr, b.ptr, max_iter, int(abs_prec), int(use_max_norms)),
+           out.mra.ptr)
+    return out.mra.last_stats()
+
+
+def square(prec, out, inp, max_iter=-1, abs_prec=False):
+    """mrcpp::square(prec, out, inp)."""
+    _check(_lib.mw_square(prec, out.ptr, inp.ptr, max_iter, int(abs_prec)), out.mra.ptr)
+    return out.mra.last_stats()
+
+
+def add(prec, out, vec, max_iter=-1):
+    """mrcpp::add(prec, out, FunctionTreeVector, maxIter); vec = [(coef, tree), ...], union grid."""
+    coefs = np.ascontiguousarray([c for c, _ in vec], dtype=np.float64)
+    trees = [t for _, t in vec]
+    _check(_lib.mw_add(prec, out.ptr, len(trees), _dp(coefs), _ptrs(trees), max_iter), out.mra.ptr)
+    return out.mra.last_stats()
+
+
+def build_grid(out, trees):
+    """mrcpp::build_grid(out, vec): extend out's grid by the union of the trees' grids."""
+    if isinstance(trees, FunctionTree):
+        trees = [trees]
+    trees = [t[1] if isinstance(t, tuple) else t for t in trees]
+    _check(_lib.mw_build_grid(out.ptr, len(trees), _ptrs(trees)), out.mra.ptr)
+
+
+def copy_grid(out, inp):
+    """mrcpp::copy_grid(out, inp)."""
+    _check(_lib.mw_copy_grid(out.ptr, inp.ptr), out.mra.ptr)
+
+
+def copy_func(out, inp):
+    """mrcpp::copy_func(out, inp): inp's coefficients on out's grid."""
+    _check(_lib.mw_copy_func(out.ptr, inp.ptr), out.mra.ptr)
+
+
+def clear(trees, dealloc=False):
+    """mrcpp::clear(vec, dealloc)."""
+    for t in trees:
+        t = t[1] if isinstance(t, tuple) else t
+        if dealloc:
+            t.close()
+        else:
+            t.clear()
+
+
+def dot(a, b):
+    """mrcpp::dot(a, b) = <a|b>."""
+    v = C.c_double()
+    _check(_lib.mw_dot(a.ptr, b.ptr, C.byref(v)), a.mra.ptr)
+    return v.value
+
+
+def cuda_available():
+    """True when the engine can create a context on device 0."""
+    try:
+        load_library()
+        MultiResolutionAnalysis(order=5, max_depth=4).close()
+        return True
+    except (MWError, ImportError, OSError):
+        return False

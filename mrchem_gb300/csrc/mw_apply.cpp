@@ -1,0 +1,627 @@
+// mw_apply.cpp -- host drivers of the hot path: adaptive NS-form apply
+// (single, batched, fixed grid), tree multiply and add.
+//
+// mrcpp::apply(prec, out, oper, inp[, precTrees], maxIter, absPrec) is called at
+// src/qmoperators/two_electron/CoulombPotential.cpp:131,156,
+// src/scf_solver/HelmholtzVector.cpp:149,154 and
+// src/qmoperators/two_electron/ExchangePotential.cpp:200,204.  The algorithm
+// (published method: Frediani et al., Mol. Phys. 111 (2013) 1143):
+//   - the output grid grows from the root nodes one scale per iteration; the
+//     split decision and the screening are host logic on FP64 norms;
+//   - an item (output node o, input node i, term t) contributes
+//     c_t (A_z (x) A_y (x) A_x) in_i to o for every component pair except the
+//     scaling-scaling pair below the root scale; it is skipped when
+//         b = sum_{(ft,gt)} |in_ft| prod_d |A_d^{g_d f_d}|_F  <  0.01 thr(o);
+//   - o is split when |wavelet part| * w(o) > thr(o) = prec R 2^{-(n+1)/2};
+//   - afterwards the scales are summed top-down and the tree is compressed.
+// The contractions run on the GPU in deterministic per-node order; with
+// MW_PREC_MIXED the items are split into FP64 / FP32 tiers by their bound b.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "mw_internal.h"
+
+namespace mwg {
+
+namespace {
+
+constexpr double TIER_FP64 = 1e5;  // b above TIER_FP64 * screening threshold -> FP64
+constexpr double BOUND_PRUNE = 8.0 * 2.8285;  // (sum_f |in_f|) / |block| <= sqrt(8); 8 output components
+
+double split_thr(double prec, double R, int n) { return prec * R * std::pow(2.0, -0.5 * (n + 1)); }
+
+inline double item_bound(const double *nx, const double *ny, const double *nz, const double *cn, bool root) {
+    double b = 0.0;
+    for (int ft = 0; ft < 8; ft++) {
+        if (cn[ft] == 0.0) continue;
+        int fx = ft & 1, fy = (ft >> 1) & 1, fz = (ft >> 2) & 1;
+        double s = 0.0;
+        for (int gt = 0; gt < 8; gt++) {
+            if (!root && ft == 0 && gt == 0) continue;
+            int gx = gt & 1, gy = (gt >> 1) & 1, gz = (gt >> 2) & 1;
+            s += nx[2 * gx + fx] * ny[2 * gy + fy] * nz[2 * gz + fz];
+        }
+        b += cn[ft] * s;
+    }
+    return b;
+}
+
+// component pairs with a non-zero contraction (the algorithmic work unit, 6 K^4 flops each)
+inline int item_pairs(const double *nx, const double *ny, const double *nz, const double *cn, bool root) {
+    int p = 0;
+    for (int ft = 0; ft < 8; ft++) {
+        if (cn[ft] == 0.0) continue;
+        int fx = ft & 1, fy = (ft >> 1) & 1, fz = (ft >> 2) & 1;
+        for (int gt = 0; gt < 8; gt++) {
+            if (!root && ft == 0 && gt == 0) continue;
+            int gx = gt & 1, gy = (gt >> 1) & 1, gz = (gt >> 2) & 1;
+            if (nx[2 * gx + fx] != 0.0 && ny[2 * gy + fy] != 0.0 && nz[2 * gz + fz] != 0.0) p++;
+        }
+    }
+    return p;
+}
+
+inline double block_norm8(const double *cn) {
+    double s = 0.0;
+    for (int c = 0; c < 8; c++) s += cn[c] * cn[c];
+    return std::sqrt(s);
+}
+
+inline double wavelet_norm8(const double *cn) {
+    double s = 0.0;
+    for (int c = 1; c < 8; c++) s += cn[c] * cn[c];
+    return std::sqrt(s);
+}
+
+double prec_weight(const std::vector<Tree *> &pt, int n, const int *l) {
+    double w = 0.0;
+    for (const Tree *t : pt) {
+        int idx = t->find(n, l), an = n;
+        if (idx < 0) idx = find_ancestor(*t, n, l, &an);
+        if (idx < 0) continue;
+        w += block_norm8(&t->cn[8 * (size_t)idx]) * std::pow(2.0, 1.5 * an);
+    }
+    return w;
+}
+
+struct Cand {
+    int t, lx, ly, lz;
+    int src;  // input node index, or generated slot
+    int gen;  // 1: src is a generated slot (ancestor index before generation)
+};
+
+struct JobState {
+    ApplyJob *job = nullptr;
+    double R = 1.0, fmax = 0.0;
+    std::vector<int> work;
+    std::vector<double> wgt;
+    int iter = 0;
+    GenSet gens;
+    double *gbase = nullptr;
+    float *gbase32 = nullptr;
+    std::vector<double> gcn;
+    std::vector<std::vector<Cand>> cand;
+};
+
+struct LookupCache {
+    int L = -1, side = 0;
+    std::vector<int> idx;      // -3 unknown, -2 outside, >= 0 node, <= -4 generated with ancestor -(v+4)
+    std::vector<double> anorm;
+    void reset(int Lm) {
+        L = Lm;
+        side = 2 * Lm + 1;
+        idx.assign((size_t)side * side * side, -3);
+        anorm.assign((size_t)side * side * side, 0.0);
+    }
+};
+
+// phase A for one output node: candidate items with bounds from real norms or ancestor norms
+void enumerate_node(JobState &js, int w, int s, bool root, double thr, LookupCache &cache) {
+    const Tree &inp = *js.job->inp;
+    const Oper &op = *js.job->op;
+    const Basis &b = inp.ctx->basis;
+    const NodeInfo &o = js.job->out->nodes[js.work[w]];
+    std::vector<Cand> &out = js.cand[w];
+    out.clear();
+    const double fm = BOUND_PRUNE * js.fmax;
+    int Lm = 0;
+    for (int t = 0; t < op.T; t++) Lm = std::max(Lm, op.band[t * op.S + s]);
+    cache.reset(Lm);
+    for (int t = 0; t < op.T; t++) {
+        int L = op.band[t * op.S + s];
+        if (L < 0) continue;
+        double A = op.amax[t * op.S + s], X = op.xmax[t * op.S + s];
+        if (!root && fm * 3.0 * X * A * A < thr) continue;
+        for (int lz = -L; lz <= L; lz++) {
+            const double *nz = op.norm(t, s, lz);
+            double az = std::max(std::max(nz[0], nz[1]), std::max(nz[2], nz[3]));
+            double xz = std::max(nz[1], std::max(nz[2], nz[3]));
+            if (!root && fm * (xz * A * A + 2.0 * az * X * A) < thr) continue;
+            for (int ly = -L; ly <= L; ly++) {
+                const double *ny = op.norm(t, s, ly);
+                double ay = std::max(std::max(ny[0], ny[1]), std::max(ny[2], ny[3]));
+                double xy = std::max(ny[1], std::max(ny[2], ny[3]));
+                if (!root && fm * (xz * ay * A + az * xy * A + az * ay * X) < thr) continue;
+                for (int lx = -L; lx <= L; lx++) {
+                    size_t ci = ((size_t)(lz + Lm) * cache.side + (ly + Lm)) * cache.side + (lx + Lm);
+                    int &ce = cache.idx[ci];
+                    if (ce == -3) {
+                        int p[3] = {o.l[0] - lx, o.l[1] - ly, o.l[2] - lz};
+                        if (!b.in_world(o.n, p)) {
+                            ce = -2;
+                        } else {
+                            int i = inp.find(o.n, p);
+                            if (i >= 0) {
+                                ce = i;
+                            } else {
+                                int a = find_ancestor(inp, o.n, p, nullptr);
+                                ce = -(a + 4);
+                                cache.anorm[ci] = block_norm8(&inp.cn[8 * (size_t)a]);
+                            }
+                        }
+                    }
+                    if (ce == -2) continue;
+                    const double *nx = op.norm(t, s, lx);
+                    double cnb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    const double *cn;
+                    if (ce >= 0) {
+                        cn = &inp.cn[8 * (size_t)ce];
+                    } else {
+                        cnb[0] = cache.anorm[ci];
+                        cn = cnb;
+                    }
+                    double bd = item_bound(nx, ny, nz, cn, root);
+                    if (!root && bd < thr) continue;
+                    out.push_back(Cand{t, lx, ly, lz, ce >= 0 ? ce : -(ce + 4), ce >= 0 ? 0 : 1});
+                }
+            }
+        }
+    }
+}
+
+struct LevelItems {
+    // per tier: node list, begin offsets, item SoA
+    std::vector<double *> out;
+    std::vector<long long> begin;
+    std::vector<const void *> in, ax, ay, az;
+    std::vector<double> coef;
+    void clear() {
+        out.clear();
+        begin.assign(1, 0);
+        in.clear();
+        ax.clear();
+        ay.clear();
+        az.clear();
+        coef.clear();
+    }
+};
+
+void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int fp32, mw_stats &st) {
+    int nn = (int)li.out.size();
+    if (nn == 0) return;
+    Packer pk;
+    pk.add(li.out.data(), li.out.size() * sizeof(double *));
+    pk.add(li.begin.data(), li.begin.size() * sizeof(long long));
+    pk.add(li.in.data(), li.in.size() * sizeof(void *));
+    pk.add(li.ax.data(), li.ax.size() * sizeof(void *));
+    pk.add(li.ay.data(), li.ay.size() * sizeof(void *));
+    pk.add(li.az.data(), li.az.size() * sizeof(void *));
+    pk.add(li.coef.data(), li.coef.size() * sizeof(double));
+    pk.ship(ctx, ctx.arena);
+    int *counter = (int *)ctx.arena.alloc(sizeof(int));
+    ApplyLaunch L;
+    L.nnodes = nn;
+    L.root = root ? 1 : 0;
+    L.set = set ? 1 : 0;
+    L.out = (double *const *)pk.ptr(0);
+    L.begin = (const long long *)pk.ptr(1);
+    L.in = (const void *const *)pk.ptr(2);
+    L.ax = (const void *const *)pk.ptr(3);
+    L.ay = (const void *const *)pk.ptr(4);
+    L.az = (const void *const *)pk.ptr(5);
+    L.coef = (const double *)pk.ptr(6);
+    L.counter = counter;
+    k_apply(ctx.dbasis, L, fp32, ctx.nsm, ctx.stream);
+    st.launches++;
+}
+
+}  // namespace
+
+void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st) {
+    if (jobs.empty()) return;
+    Ctx &ctx = *jobs[0].out->ctx;
+    const Basis &b = ctx.basis;
+    const int K = b.K, bs = b.bs, bsz = 4 * K * K;
+    const double K4 = (double)K * K * K * K;
+    const bool mixed = precision_mode == MW_PREC_MIXED;
+    auto t_start = std::chrono::steady_clock::now();
+    Arena &arena = ctx.arena;
+    arena.reset();
+    cudaEvent_t ev0, ev1;
+    MWG_CUDA(cudaEventCreate(&ev0));
+    MWG_CUDA(cudaEventCreate(&ev1));
+    float kernel_ms = 0.0f;
+
+    std::vector<JobState> js(jobs.size());
+    int max_levels = 0;
+    for (size_t j = 0; j < jobs.size(); j++) {
+        ApplyJob &job = jobs[j];
+        JobState &s = js[j];
+        s.job = &job;
+        if (job.inp->ctx != &ctx || job.out->ctx != &ctx || job.op->ctx != &ctx)
+            throw Error(MW_ERR_ARG, "apply: trees and operator must belong to one context");
+        for (int i = 0; i < job.inp->nn(); i++) s.fmax = std::max(s.fmax, block_norm8(&job.inp->cn[8 * (size_t)i]));
+        if (!fixed_grid) {
+            if (job.out->nn() != job.out->nroots) throw Error(MW_ERR_STATE, "apply: output tree must be empty");
+            tree_zero(*job.out, 0, job.out->nn());
+        }
+        if (mixed) {
+            Tree &in = *job.inp;
+            if (in.cap32 < (size_t)in.nn()) {
+                if (in.d_coefs32) cudaFree(in.d_coefs32);
+                MWG_CUDA(cudaMalloc(&in.d_coefs32, sizeof(float) * (size_t)bs * in.cap));
+                in.cap32 = in.cap;
+            }
+            k_to_fp32(in.d_coefs, in.d_coefs32, (size_t)bs * in.nn(), ctx.stream);
+            st.launches++;
+        }
+        for (int i = 0; i < job.out->nroots; i++) s.work.push_back(i);
+        if (fixed_grid) max_levels = std::max(max_levels, job.out->max_scale() - b.n0 + 1);
+        s.R = 1.0;
+    }
+    // fixed grid: per level, the output's nodes at that scale
+    auto fixed_level_nodes = [&](JobState &s, int n) {
+        s.work.clear();
+        for (int i = 0; i < s.job->out->nn(); i++)
+            if (s.job->out->nodes[i].n == n) s.work.push_back(i);
+    };
+
+    LevelItems li64, li32;
+    int level = 0;
+    while (true) {
+        const int n = b.n0 + level, sidx = level;
+        if (fixed_grid) {
+            if (level >= max_levels) break;
+            for (auto &s : js) fixed_level_nodes(s, n);
+        }
+        bool any = false;
+        for (auto &s : js) any |= !s.work.empty();
+        if (!any) break;
+        const bool root = (level == 0);
+        // thresholds and precision-steering weights
+        for (auto &s : js) {
+            s.wgt.assign(s.work.size(), 1.0);
+            if (!s.job->prec_trees.empty())
+                for (size_t w = 0; w < s.work.size(); w++)
+                    s.wgt[w] = prec_weight(s.job->prec_trees, n, s.job->out->nodes[s.work[w]].l);
+            s.cand.assign(s.work.size(), {});
+        }
+        // phase A: candidate enumeration (host, all jobs' nodes in parallel)
+        std::vector<std::pair<int, int>> flat;
+        for (size_t j = 0; j < js.size(); j++)
+            for (size_t w = 0; w < js[j].work.size(); w++) flat.push_back({(int)j, (int)w});
+#pragma omp parallel
+        {
+            LookupCache cache;
+#pragma omp for schedule(dynamic, 4)
+            for (long q = 0; q < (long)flat.size(); q++) {
+                JobState &s = js[flat[q].first];
+                int w = flat[q].second;
+                if (!root && s.wgt[w] <= 0.0) {
+                    s.cand[w].clear();
+                    continue;
+                }
+                double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / s.wgt[w];
+                enumerate_node(s, w, sidx, root, thr, cache);
+            }
+        }
+        // phase B: generated input nodes
+        for (auto &s : js) {
+            s.gens.clear();
+            for (size_t w = 0; w < s.work.size(); w++) {
+                const NodeInfo &o = s.job->out->nodes[s.work[w]];
+                for (Cand &c : s.cand[w]) {
+                    if (!c.gen) continue;
+                    int p[3] = {o.l[0] - c.lx, o.l[1] - c.ly, o.l[2] - c.lz};
+                    c.src = s.gens.request(*s.job->inp, n, p, c.src);
+                }
+            }
+            s.gbase = s.gens.generate(*s.job->inp, arena, s.gcn, &st);
+            s.gbase32 = nullptr;
+            if (mixed && s.gbase) {
+                s.gbase32 = (float *)arena.alloc(sizeof(float) * (size_t)bs * s.gens.keys.size());
+                k_to_fp32(s.gbase, s.gbase32, (size_t)bs * s.gens.keys.size(), ctx.stream);
+                st.launches++;
+            }
+        }
+        // phase C: exact screening, tiers, item lists in node order
+        li64.clear();
+        li32.clear();
+        long long pairs_tot = 0, n64 = 0, n32 = 0;
+        for (auto &s : js) {
+            const Tree &inp = *s.job->inp;
+            const Oper &op = *s.job->op;
+            for (size_t w = 0; w < s.work.size(); w++) {
+                int oi = s.work[w];
+                double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / std::max(s.wgt[w], 1e-300);
+                double *ob = s.job->out->block(oi);
+                li64.out.push_back(ob);
+                size_t n32_before = li32.in.size();
+                for (const Cand &c : s.cand[w]) {
+                    const double *cn = c.gen ? &s.gcn[8 * (size_t)c.src] : &inp.cn[8 * (size_t)c.src];
+                    const double *nx = op.norm(c.t, sidx, c.lx), *ny = op.norm(c.t, sidx, c.ly),
+                                 *nz = op.norm(c.t, sidx, c.lz);
+                    double bd = item_bound(nx, ny, nz, cn, root);
+                    if (!root && bd < thr) continue;
+                    pairs_tot += item_pairs(nx, ny, nz, cn, root);
+                    long bxi = op.block_index(c.t, sidx, c.lx), byi = op.block_index(c.t, sidx, c.ly),
+                         bzi = op.block_index(c.t, sidx, c.lz);
+                    bool near = std::max(std::abs(c.lx), std::max(std::abs(c.ly), std::abs(c.lz))) <= 1;
+                    bool use64 = !mixed || root || near || bd > TIER_FP64 * thr;
+                    if (use64) {
+                        li64.in.push_back(c.gen ? (const void *)(s.gbase + (size_t)c.src * bs)
+                                                : (const void *)inp.block(c.src));
+                        li64.ax.push_back(op.d_blocks + (size_t)bxi * bsz);
+                        li64.ay.push_back(op.d_blocks + (size_t)byi * bsz);
+                        li64.az.push_back(op.d_blocks + (size_t)bzi * bsz);
+                        li64.coef.push_back(op.c[c.t]);
+                        n64++;
+                    } else {
+                        li32.in.push_back(c.gen ? (const void *)(s.gbase32 + (size_t)c.src * bs)
+                                                : (const void *)(inp.d_coefs32 + (size_t)c.src * bs));
+                        li32.ax.push_back(op.d_blocks32 + (size_t)bxi * bsz);
+                        li32.ay.push_back(op.d_blocks32 + (size_t)byi * bsz);
+                        li32.az.push_back(op.d_blocks32 + (size_t)bzi * bsz);
+                        li32.coef.push_back(op.c[c.t]);
+                        n32++;
+                    }
+                }
+                li64.begin.push_back((long long)li64.in.size());
+                if (li32.in.size() > n32_before) {
+                    li32.out.push_back(ob);
+                    li32.begin.push_back((long long)li32.in.size());
+                }
+            }
+        }
+        st.items += n64 + n32;
+        st.items_fp64 += n64;
+        st.items_fp32 += n32;
+        st.flops += 6.0 * K4 * (double)pairs_tot;
+        st.flops_issued += 96.0 * K4 * (double)(n64 + n32);
+        st.bytes += 8.0 * bs * (double)(n64 + n32) * 0.0;  // coefficient bytes are counted per node below
+        MWG_CUDA(cudaEventRecord(ev0, ctx.stream));
+        launch_tier(ctx, li64, root, true, 0, st);
+        launch_tier(ctx, li32, root, false, 1, st);
+        MWG_CUDA(cudaEventRecord(ev1, ctx.stream));
+        // norms of the level's output nodes
+        std::vector<double *> bl, cnp;
+        for (auto &s : js)
+            for (int oi : s.work) {
+                bl.push_back(s.job->out->block(oi));
+                cnp.push_back(s.job->out->d_cn + (size_t)8 * oi);
+            }
+        {
+            Packer pk;
+            pk.add(bl.data(), bl.size() * sizeof(double *));
+            pk.add(cnp.data(), cnp.size() * sizeof(double *));
+            pk.ship(ctx, arena);
+            k_norms(ctx.dbasis, (double *const *)pk.ptr(0), (double *const *)pk.ptr(1), (int)bl.size(), ctx.stream);
+            st.launches++;
+        }
+        for (auto &s : js) {
+            Tree &out = *s.job->out;
+            MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
+                                     ctx.stream));
+        }
+        ctx.sync();
+        float ms = 0.0f;
+        MWG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        kernel_ms += ms;
+        // refinement
+        for (auto &s : js) {
+            Tree &out = *s.job->out;
+            st.out_nodes += (long long)s.work.size();
+            st.bytes += 8.0 * bs * (double)s.work.size();
+            if (root && !s.job->abs_prec) {
+                double r2 = 0.0;
+                for (int oi : s.work) r2 += std::pow(block_norm8(&out.cn[8 * (size_t)oi]), 2);
+                s.R = r2 > 0.0 ? std::sqrt(r2) : 1.0;
+            }
+            std::vector<int> next;
+            if (!fixed_grid && (s.job->max_iter < 0 || s.iter < s.job->max_iter) && n < b.max_scale()) {
+                double thr = split_thr(s.job->prec, s.R, n);
+                for (size_t w = 0; w < s.work.size(); w++) {
+                    int oi = s.work[w];
+                    if (wavelet_norm8(&out.cn[8 * (size_t)oi]) * s.wgt[w] > thr) {
+                        int c0 = out.split(oi);
+                        for (int c = 0; c < 8; c++) next.push_back(c0 + c);
+                    }
+                }
+                tree_zero(out, out.nn() - (int)next.size(), (int)next.size());
+            }
+            s.work.swap(next);
+            s.iter++;
+        }
+        st.levels++;
+        arena.reset();
+        level++;
+    }
+    // input bytes: every distinct input block read once per apply (FP64 or FP32 shadow) + operator blocks
+    for (auto &s : js) st.bytes += 8.0 * bs * (double)s.job->inp->nn();
+
+    // post-processing: top-down sum over scales, then bottom-up compression
+    int maxn = b.n0;
+    for (auto &s : js) maxn = std::max(maxn, s.job->out->max_scale());
+    for (int n = b.n0; n < maxn; n++) {
+        std::vector<PairTask> tasks;
+        for (auto &s : js) {
+            Tree &out = *s.job->out;
+            for (int i = 0; i < out.nn(); i++)
+                if (out.nodes[i].n == n && out.nodes[i].child0 >= 0)
+                    tasks.push_back({out.block(i), out.block(out.nodes[i].child0)});
+        }
+        if (tasks.empty()) continue;
+        Packer pk;
+        pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
+        pk.ship(ctx, arena);
+        k_topdown(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
+        st.launches++;
+    }
+    for (int n = maxn - 1; n >= b.n0; n--) {
+        std::vector<PairTask> tasks;
+        std::vector<double *> cnp;
+        for (auto &s : js) {
+            Tree &out = *s.job->out;
+            for (int i = 0; i < out.nn(); i++)
+                if (out.nodes[i].n == n && out.nodes[i].child0 >= 0) {
+                    tasks.push_back({out.block(i), out.block(out.nodes[i].child0)});
+                    cnp.push_back(out.d_cn + (size_t)8 * i);
+                }
+        }
+        if (tasks.empty()) continue;
+        Packer pk;
+        pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
+        pk.add(cnp.data(), cnp.size() * sizeof(double *));
+        pk.ship(ctx, arena);
+        k_compress(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(), ctx.stream);
+        st.launches++;
+    }
+    // leaf norms after the top-down pass
+    {
+        std::vector<double *> bl, cnp;
+        for (auto &s : js) {
+            Tree &out = *s.job->out;
+            for (int i = 0; i < out.nn(); i++)
+                if (out.nodes[i].child0 < 0) {
+                    bl.push_back(out.block(i));
+                    cnp.push_back(out.d_cn + (size_t)8 * i);
+                }
+        }
+        Packer pk;
+        pk.add(bl.data(), bl.size() * sizeof(double *));
+        pk.add(cnp.data(), cnp.size() * sizeof(double *));
+        pk.ship(ctx, arena);
+        k_norms(ctx.dbasis, (double *const *)pk.ptr(0), (double *const *)pk.ptr(1), (int)bl.size(), ctx.stream);
+        st.launches++;
+    }
+    for (auto &s : js) {
+        Tree &out = *s.job->out;
+        MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
+                                 ctx.stream));
+    }
+    ctx.sync();
+    arena.reset();
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    st.kernel_ms += kernel_ms;
+    st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+}
+
+// ------------------------------------------------------------------ multiply
+void multiply(double prec, Tree &out, double coef, Tree &a, Tree &b, int max_iter, bool abs_prec, bool use_max_norms,
+              mw_stats &st) {
+    Ctx &ctx = *out.ctx;
+    const Basis &bs_ = ctx.basis;
+    int bs = bs_.bs;
+    Arena &arena = ctx.arena;
+    auto t_start = std::chrono::steady_clock::now();
+    // unresolved detail below each node: tail^2 = sum over children (|w|^2 + tail^2)
+    auto tails = [&](const Tree &t) {
+        std::vector<double> tl(t.nn(), 0.0);
+        std::vector<int> order(t.nn());
+        for (int i = 0; i < t.nn(); i++) order[i] = i;
+        std::sort(order.begin(), order.end(), [&](int x, int y) { return t.nodes[x].n > t.nodes[y].n; });
+        for (int i : order) {
+            if (t.nodes[i].child0 < 0) continue;
+            double s = 0.0;
+            for (int c = 0; c < 8; c++) {
+                int ci = t.nodes[i].child0 + c;
+                double w = wavelet_norm8(&t.cn[8 * (size_t)ci]);
+                s += w * w + tl[ci] * tl[ci];
+            }
+            tl[i] = std::sqrt(s);
+        }
+        return tl;
+    };
+    std::vector<double> ta, tb;
+    if (use_max_norms) {
+        ta = tails(a);
+        tb = tails(b);
+    }
+    std::vector<int> work;
+    for (int i = 0; i < out.nn(); i++)
+        if (out.nodes[i].child0 < 0) work.push_back(i);
+    int iter = 0;
+    while (!work.empty()) {
+        arena.reset();
+        GenSet ga, gb;
+        for (int oi : work) {
+            const NodeInfo &o = out.nodes[oi];
+            if (a.find(o.n, o.l) < 0) ga.request(a, o.n, o.l, find_ancestor(a, o.n, o.l, nullptr));
+            if (b.find(o.n, o.l) < 0) gb.request(b, o.n, o.l, find_ancestor(b, o.n, o.l, nullptr));
+        }
+        std::vector<double> gca, gcb;
+        double *baseA = ga.generate(a, arena, gca, &st), *baseB = gb.generate(b, arena, gcb, &st);
+        std::vector<MulTask> tasks(work.size());
+        std::vector<double> crit(work.size(), 0.0);
+        for (size_t w = 0; w < work.size(); w++) {
+            const NodeInfo &o = out.nodes[work[w]];
+            int ia = a.find(o.n, o.l), ib = b.find(o.n, o.l);
+            tasks[w].a = block_at(a, ga, baseA, o.n, o.l);
+            tasks[w].b = block_at(b, gb, baseB, o.n, o.l);
+            tasks[w].out = out.block(work[w]);
+            tasks[w].cn = out.d_cn + (size_t)8 * work[w];
+            tasks[w].scale = coef * std::pow(2.0, 1.5 * (o.n + 1));
+            if (use_max_norms) {
+                const double *cna = ia >= 0 ? &a.cn[8 * (size_t)ia] : &gca[8 * (size_t)ga.slot.at(Key{o.n, {o.l[0], o.l[1], o.l[2]}})];
+                const double *cnb = ib >= 0 ? &b.cn[8 * (size_t)ib] : &gcb[8 * (size_t)gb.slot.at(Key{o.n, {o.l[0], o.l[1], o.l[2]}})];
+                double mna = block_norm8(cna) * std::pow(2.0, 1.5 * o.n), mnb = block_norm8(cnb) * std::pow(2.0, 1.5 * o.n);
+                crit[w] = (ia >= 0 ? ta[ia] : 0.0) * mnb + (ib >= 0 ? tb[ib] : 0.0) * mna;
+            }
+        }
+        Packer pk;
+        pk.add(tasks.data(), tasks.size() * sizeof(MulTask));
+        pk.ship(ctx, arena);
+        k_multiply(ctx.dbasis, (const MulTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
+        st.launches++;
+        st.out_nodes += (long long)work.size();
+        MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
+                                 ctx.stream));
+        ctx.sync();
+        double R = abs_prec ? 1.0 : std::sqrt(out.sqnorm_leaves());
+        std::vector<int> next;
+        if (max_iter < 0 || iter < max_iter) {
+            for (size_t w = 0; w < work.size(); w++) {
+                int oi = work[w];
+                int n = out.nodes[oi].n;
+                if (n >= bs_.max_scale()) continue;
+                double thr = split_thr(prec, R, n);
+                if (wavelet_norm8(&out.cn[8 * (size_t)oi]) > thr || crit[w] > thr) {
+                    int c0 = out.split(oi);
+                    for (int c = 0; c < 8; c++) next.push_back(c0 + c);
+                }
+            }
+            if (!next.empty()) tree_zero(out, out.nn() - (int)next.size(), (int)next.size());
+        }
+        work.swap(next);
+        iter++;
+    }
+    tree_compress(out, arena, &st);
+    arena.reset();
+    st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+}
+
+void add(Tree &out, const std::vector<const Tree *> &trees, const std::vector<double> &coefs, mw_stats &st) {
+    Ctx &ctx = *out.ctx;
+    auto t_start = std::chrono::steady_clock::now();
+    build_grid(out, trees);
+    ctx.arena.reset();
+    combine_on_grid(out, trees, coefs, ctx.arena, &st);
+    ctx.arena.reset();
+    st.out_nodes += out.nn();
+    st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+}
+
+}  // namespace mwg

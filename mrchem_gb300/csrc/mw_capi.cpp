@@ -1,0 +1,457 @@
+// mw_capi.cpp -- extern "C" entry points (include/mw_gb300.h).
+// Every entry catches errors and returns a status; the message is kept on the
+// context for mw_last_error().  Nothing here falls back to host arithmetic:
+// without a usable CUDA device the calls fail with MW_ERR_CUDA.
+#include <cmath>
+#include <cstring>
+
+#include "mw_internal.h"
+
+struct mw_ctx_s {
+    mwg::Ctx ctx;
+};
+struct mw_tree_s {
+    mwg::Tree tree;
+};
+struct mw_op_s {
+    mwg::Oper op;
+};
+
+namespace {
+
+thread_local std::string g_noctx_err;
+
+template <typename F>
+int guard(mwg::Ctx *ctx, F &&f) {
+    try {
+        if (ctx) MWG_CUDA(cudaSetDevice(ctx->device));
+        f();
+        return MW_OK;
+    } catch (const mwg::Error &e) {
+        (ctx ? ctx->err : g_noctx_err) = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        (ctx ? ctx->err : g_noctx_err) = "host allocation failed";
+        return MW_ERR_OOM;
+    } catch (const std::exception &e) {
+        (ctx ? ctx->err : g_noctx_err) = e.what();
+        return MW_ERR_STATE;
+    }
+}
+
+mwg::Ctx *ctx_of(mw_tree t) { return t ? t->tree.ctx : nullptr; }
+
+void check_same(const mwg::Tree &a, const mwg::Tree &b) {
+    if (a.ctx != b.ctx) throw mwg::Error(MW_ERR_ARG, "trees belong to different contexts");
+}
+
+}  // namespace
+
+extern "C" {
+
+int mw_ctx_create(int device, int root_scale, const int corner[3], const int boxes[3], int order, int basis,
+                  int max_depth, mw_ctx *out) {
+    if (!out || !corner || !boxes) return MW_ERR_ARG;
+    *out = nullptr;
+    if (order + 1 < 4 || order + 1 > mwg::KMAX) {
+        g_noctx_err = "order must be in [3, 9] (K = order + 1 <= 10 on the GPU)";
+        return MW_ERR_ARG;
+    }
+    if (max_depth < 1 || max_depth > 30 || (basis != MW_BASIS_LEGENDRE && basis != MW_BASIS_INTERPOLATING)) {
+        g_noctx_err = "invalid max_depth or basis";
+        return MW_ERR_ARG;
+    }
+    for (int d = 0; d < 3; d++)
+        if (boxes[d] < 1) {
+            g_noctx_err = "boxes must be >= 1";
+            return MW_ERR_ARG;
+        }
+    mw_ctx c = new mw_ctx_s;
+    int rc = guard(nullptr, [&] {
+        int ndev = 0;
+        MWG_CUDA(cudaGetDeviceCount(&ndev));
+        if (device < 0 || device >= ndev) throw mwg::Error(MW_ERR_ARG, "no such CUDA device");
+        c->ctx.device = device;
+        MWG_CUDA(cudaSetDevice(device));
+        MWG_CUDA(cudaStreamCreateWithFlags(&c->ctx.stream, cudaStreamNonBlocking));
+        MWG_CUDA(cudaDeviceGetAttribute(&c->ctx.nsm, cudaDevAttrMultiProcessorCount, device));
+        mwg::Basis &b = c->ctx.basis;
+        b.init(root_scale, corner, boxes, order, basis, max_depth);
+        int K = b.K, K2 = 2 * K;
+        size_t nd = 4 * K2 * K2 + 2 * K * K + 3 * K + K * K;
+        std::vector<double> h(nd);
+        double *p = h.data();
+        std::memcpy(p, b.W.data(), sizeof(double) * K2 * K2);
+        std::memcpy(p + K2 * K2, b.WT.data(), sizeof(double) * K2 * K2);
+        std::memcpy(p + 2 * K2 * K2, b.c2v.data(), sizeof(double) * K * K);
+        std::memcpy(p + 2 * K2 * K2 + K * K, b.v2c.data(), sizeof(double) * K * K);
+        std::memcpy(p + 2 * K2 * K2 + 2 * K * K, b.qx.data(), sizeof(double) * K);
+        std::memcpy(p + 2 * K2 * K2 + 2 * K * K + K, b.qw.data(), sizeof(double) * K);
+        std::memcpy(p + 2 * K2 * K2 + 2 * K * K + 2 * K, b.legq.data(), sizeof(double) * K * K);
+        MWG_CUDA(cudaMalloc(&c->ctx.d_basis, sizeof(double) * nd));
+        MWG_CUDA(cudaMemcpy(c->ctx.d_basis, h.data(), sizeof(double) * nd, cudaMemcpyHostToDevice));
+        double *d = c->ctx.d_basis;
+        c->ctx.dbasis = mwg::DevBasis{K, basis, d, d + K2 * K2, d + 2 * K2 * K2, d + 2 * K2 * K2 + K * K,
+                                      d + 2 * K2 * K2 + 2 * K * K, d + 2 * K2 * K2 + 2 * K * K + K,
+                                      d + 2 * K2 * K2 + 2 * K * K + 2 * K};
+    });
+    if (rc != MW_OK) {
+        if (c->ctx.stream) cudaStreamDestroy(c->ctx.stream);
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return MW_OK;
+}
+
+int mw_ctx_destroy(mw_ctx c) {
+    if (!c) return MW_ERR_ARG;
+    cudaSetDevice(c->ctx.device);
+    cudaStreamSynchronize(c->ctx.stream);
+    c->ctx.arena.release();
+    if (c->ctx.h_pinned) cudaFreeHost(c->ctx.h_pinned);
+    if (c->ctx.d_basis) cudaFree(c->ctx.d_basis);
+    cudaStreamDestroy(c->ctx.stream);
+    delete c;
+    return MW_OK;
+}
+
+const char *mw_last_error(mw_ctx c) { return c ? c->ctx.err.c_str() : g_noctx_err.c_str(); }
+
+int mw_ctx_basis(mw_ctx c, double *qx, double *qw, double *filter, double *c2v, double *v2c) {
+    if (!c) return MW_ERR_ARG;
+    const mwg::Basis &b = c->ctx.basis;
+    int K = b.K;
+    if (qx) std::memcpy(qx, b.qx.data(), sizeof(double) * K);
+    if (qw) std::memcpy(qw, b.qw.data(), sizeof(double) * K);
+    if (filter) std::memcpy(filter, b.W.data(), sizeof(double) * 4 * K * K);
+    if (c2v) std::memcpy(c2v, b.c2v.data(), sizeof(double) * K * K);
+    if (v2c) std::memcpy(v2c, b.v2c.data(), sizeof(double) * K * K);
+    return MW_OK;
+}
+
+int mw_ctx_last_stats(mw_ctx c, mw_stats *st) {
+    if (!c || !st) return MW_ERR_ARG;
+    *st = c->ctx.last;
+    return MW_OK;
+}
+
+int mw_ctx_synchronize(mw_ctx c) {
+    if (!c) return MW_ERR_ARG;
+    return guard(&c->ctx, [&] { c->ctx.sync(); });
+}
+
+// ---------------------------------------------------------------- trees
+int mw_tree_create(mw_ctx c, mw_tree *out) {
+    if (!c || !out) return MW_ERR_ARG;
+    *out = nullptr;
+    mw_tree t = new mw_tree_s;
+    t->tree.ctx = &c->ctx;
+    int rc = guard(&c->ctx, [&] { mwg::tree_clear(t->tree); c->ctx.sync(); });
+    if (rc != MW_OK) {
+        t->tree.free_device();
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return MW_OK;
+}
+
+int mw_tree_destroy(mw_tree t) {
+    if (!t) return MW_ERR_ARG;
+    cudaSetDevice(t->tree.ctx->device);
+    cudaStreamSynchronize(t->tree.ctx->stream);
+    t->tree.free_device();
+    delete t;
+    return MW_OK;
+}
+
+int mw_tree_nnodes(mw_tree t, int *n) {
+    if (!t || !n) return MW_ERR_ARG;
+    *n = t->tree.nn();
+    return MW_OK;
+}
+
+int mw_tree_nleaves(mw_tree t, int *n) {
+    if (!t || !n) return MW_ERR_ARG;
+    int c = 0;
+    for (auto &nd : t->tree.nodes) c += nd.child0 < 0;
+    *n = c;
+    return MW_OK;
+}
+
+int mw_tree_depth(mw_tree t, int *d) {
+    if (!t || !d) return MW_ERR_ARG;
+    *d = t->tree.max_scale() - t->tree.ctx->basis.n0 + 1;
+    return MW_OK;
+}
+
+int mw_tree_upload(mw_tree t, int nnodes, const int *keys, const double *coefs) {
+    if (!t || nnodes < 1 || !keys || !coefs) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { mwg::tree_upload(t->tree, nnodes, keys, coefs, t->tree.ctx->arena); });
+}
+
+int mw_tree_download(mw_tree t, int *keys, double *coefs, unsigned char *is_leaf) {
+    if (!t) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { mwg::tree_download(t->tree, keys, coefs, is_leaf); });
+}
+
+int mw_tree_squared_norm(mw_tree t, double *out) {
+    if (!t || !out) return MW_ERR_ARG;
+    *out = t->tree.sqnorm_leaves();
+    return MW_OK;
+}
+
+int mw_tree_integrate(mw_tree t, double *out) {
+    if (!t || !out) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { *out = mwg::integrate(t->tree); });
+}
+
+int mw_tree_rescale(mw_tree t, double c) {
+    if (!t) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { mwg::rescale(t->tree, c); });
+}
+
+int mw_tree_eval(mw_tree t, int npts, const double *xyz, double *out) {
+    if (!t || npts < 0 || (npts > 0 && (!xyz || !out))) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { mwg::eval_points(t->tree, npts, xyz, out, t->tree.ctx->arena); });
+}
+
+int mw_tree_clear(mw_tree t) {
+    if (!t) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { mwg::tree_clear(t->tree); t->tree.ctx->sync(); });
+}
+
+int mw_project_gauss(double prec, mw_tree out, int nterms, const mw_gterm *terms, int abs_prec) {
+    if (!out || nterms < 1 || !terms || !(prec > 0.0)) return MW_ERR_ARG;
+    return guard(ctx_of(out), [&] {
+        for (int i = 0; i < nterms; i++)
+            if (!(terms[i].alpha > 0.0) || terms[i].pw[0] < 0 || terms[i].pw[1] < 0 || terms[i].pw[2] < 0)
+                throw mwg::Error(MW_ERR_ARG, "gaussian term needs alpha > 0 and non-negative powers");
+        mwg::project_gauss(prec, out->tree, nterms, terms, abs_prec != 0, out->tree.ctx->arena);
+    });
+}
+
+int mw_project_hydrogen(double prec, mw_tree out, int n, int l, int m, double Z, const double origin[3], int abs_prec) {
+    if (!out || !(prec > 0.0) || !(Z > 0.0)) return MW_ERR_ARG;
+    return guard(ctx_of(out),
+                 [&] { mwg::project_hydrogen(prec, out->tree, n, l, m, Z, origin, abs_prec != 0, out->tree.ctx->arena); });
+}
+
+int mw_copy_grid(mw_tree out, mw_tree inp) {
+    if (!out || !inp) return MW_ERR_ARG;
+    return guard(ctx_of(out), [&] {
+        check_same(out->tree, inp->tree);
+        mwg::copy_grid(out->tree, inp->tree);
+        out->tree.ctx->sync();
+    });
+}
+
+int mw_build_grid(mw_tree out, int n, const mw_tree *trees) {
+    if (!out || n < 0 || (n > 0 && !trees)) return MW_ERR_ARG;
+    return guard(ctx_of(out), [&] {
+        std::vector<const mwg::Tree *> v;
+        for (int i = 0; i < n; i++) {
+            if (!trees[i]) throw mwg::Error(MW_ERR_ARG, "null tree");
+            check_same(out->tree, trees[i]->tree);
+            v.push_back(&trees[i]->tree);
+        }
+        mwg::build_grid(out->tree, v);
+        out->tree.ctx->sync();
+    });
+}
+
+int mw_copy_func(mw_tree out, mw_tree inp) {
+    if (!out || !inp) return MW_ERR_ARG;
+    return guard(ctx_of(out), [&] {
+        check_same(out->tree, inp->tree);
+        mwg::copy_func(out->tree, inp->tree, out->tree.ctx->arena);
+    });
+}
+
+int mw_crop(mw_tree t, double prec, int abs_prec) {
+    if (!t || !(prec > 0.0)) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { mwg::crop(t->tree, prec, abs_prec != 0, t->tree.ctx->arena); });
+}
+
+int mw_dot(mw_tree a, mw_tree b, double *out) {
+    if (!a || !b || !out) return MW_ERR_ARG;
+    return guard(ctx_of(a), [&] {
+        check_same(a->tree, b->tree);
+        *out = mwg::dot(a->tree, b->tree, a->tree.ctx->arena);
+    });
+}
+
+// ---------------------------------------------------------------- operators
+static int op_create(mw_ctx c, int kind, double mu, double prec, mw_op *out) {
+    if (!c || !out || !(prec > 0.0) || prec >= 1.0) return MW_ERR_ARG;
+    if (kind == 1 && !(mu > 0.0)) {
+        c->ctx.err = "Helmholtz operator needs mu > 0";
+        return MW_ERR_ARG;
+    }
+    *out = nullptr;
+    mw_op o = new mw_op_s;
+    o->op.ctx = &c->ctx;
+    o->op.kind = kind;
+    o->op.mu = mu;
+    o->op.prec = prec;
+    int rc = guard(&c->ctx, [&] { o->op.build(c->ctx.basis); });
+    if (rc != MW_OK) {
+        delete o;
+        return rc;
+    }
+    *out = o;
+    return MW_OK;
+}
+
+int mw_op_create_poisson(mw_ctx c, double prec, mw_op *out) { return op_create(c, 0, 0.0, prec, out); }
+
+int mw_op_create_helmholtz(mw_ctx c, double mu, double prec, mw_op *out) { return op_create(c, 1, mu, prec, out); }
+
+int mw_op_destroy(mw_op o) {
+    if (!o) return MW_ERR_ARG;
+    cudaSetDevice(o->op.ctx->device);
+    cudaStreamSynchronize(o->op.ctx->stream);
+    if (o->op.d_blocks) cudaFree(o->op.d_blocks);
+    if (o->op.d_blocks32) cudaFree(o->op.d_blocks32);
+    if (o->op.d_blocks16) cudaFree(o->op.d_blocks16);
+    delete o;
+    return MW_OK;
+}
+
+int mw_op_nterms(mw_op o, int *n) {
+    if (!o || !n) return MW_ERR_ARG;
+    *n = o->op.T;
+    return MW_OK;
+}
+
+int mw_op_terms(mw_op o, double *coefs, double *exps) {
+    if (!o) return MW_ERR_ARG;
+    for (int t = 0; t < o->op.T; t++) {
+        if (coefs) coefs[t] = o->op.c[t];
+        if (exps) exps[t] = o->op.a[t];
+    }
+    return MW_OK;
+}
+
+int mw_op_band(mw_op o, int term, int scale, int *band) {
+    if (!o || !band) return MW_ERR_ARG;
+    int s = scale - o->op.ctx->basis.n0;
+    if (term < 0 || term >= o->op.T || s < 0 || s >= o->op.S) return MW_ERR_ARG;
+    *band = o->op.band[term * o->op.S + s];
+    return MW_OK;
+}
+
+int mw_op_block(mw_op o, int term, int scale, int l, double *blk, double *norms4) {
+    if (!o) return MW_ERR_ARG;
+    int s = scale - o->op.ctx->basis.n0;
+    if (term < 0 || term >= o->op.T || s < 0 || s >= o->op.S) return MW_ERR_ARG;
+    int L = o->op.band[term * o->op.S + s];
+    if (L < 0 || l < -L || l > L) return MW_ERR_ARG;
+    mwg::Ctx *ctx = o->op.ctx;
+    return guard(ctx, [&] {
+        int K = ctx->basis.K, bsz = 4 * K * K;
+        long bi = o->op.block_index(term, s, l);
+        if (blk)
+            MWG_CUDA(cudaMemcpy(blk, o->op.d_blocks + (size_t)bi * bsz, sizeof(double) * bsz, cudaMemcpyDeviceToHost));
+        if (norms4) std::memcpy(norms4, o->op.norm(term, s, l), sizeof(double) * 4);
+    });
+}
+
+// ---------------------------------------------------------------- hot path
+int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const mw_tree *prec_trees, int max_iter,
+             int abs_prec, int precision_mode) {
+    if (!out || !op || !inp || !(prec > 0.0) || nprec < 0 || (nprec > 0 && !prec_trees)) return MW_ERR_ARG;
+    if (precision_mode != MW_PREC_FP64 && precision_mode != MW_PREC_MIXED) return MW_ERR_ARG;
+    if (out == inp) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(out);
+    return guard(ctx, [&] {
+        std::vector<mwg::ApplyJob> jobs(1);
+        jobs[0] = mwg::ApplyJob{&out->tree, &op->op, &inp->tree, prec, abs_prec != 0, max_iter, {}};
+        for (int i = 0; i < nprec; i++) {
+            if (!prec_trees[i]) throw mwg::Error(MW_ERR_ARG, "null precision tree");
+            jobs[0].prec_trees.push_back(&prec_trees[i]->tree);
+        }
+        mw_stats st{};
+        mwg::apply_batch(jobs, precision_mode, false, st);
+        ctx->last = st;
+    });
+}
+
+int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, int max_iter, int abs_prec,
+                   int precision_mode) {
+    if (n < 1 || !precs || !outs || !ops || !inps) return MW_ERR_ARG;
+    if (precision_mode != MW_PREC_FP64 && precision_mode != MW_PREC_MIXED) return MW_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (!outs[i] || !ops[i] || !inps[i] || !(precs[i] > 0.0) || outs[i] == inps[i]) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(outs[0]);
+    return guard(ctx, [&] {
+        std::vector<mwg::ApplyJob> jobs(n);
+        for (int i = 0; i < n; i++)
+            jobs[i] = mwg::ApplyJob{&outs[i]->tree, &ops[i]->op, &inps[i]->tree, precs[i], abs_prec != 0, max_iter, {}};
+        mw_stats st{};
+        mwg::apply_batch(jobs, precision_mode, false, st);
+        ctx->last = st;
+    });
+}
+
+int mw_apply_fixed(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec, int precision_mode) {
+    if (!out || !op || !inp || !(prec > 0.0) || out == inp) return MW_ERR_ARG;
+    if (precision_mode != MW_PREC_FP64 && precision_mode != MW_PREC_MIXED) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(out);
+    return guard(ctx, [&] {
+        std::vector<mwg::ApplyJob> jobs(1);
+        jobs[0] = mwg::ApplyJob{&out->tree, &op->op, &inp->tree, prec, abs_prec != 0, 0, {}};
+        mw_stats st{};
+        mwg::apply_batch(jobs, precision_mode, true, st);
+        ctx->last = st;
+    });
+}
+
+int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec) {
+    (void)prec;
+    (void)abs_prec;
+    if (!out || !op || !inp) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(out);
+    ctx->err = "mw_apply_adjoint: not available in this build";
+    return MW_ERR_STATE;
+}
+
+int mw_multiply(double prec, mw_tree out, double coef, mw_tree a, mw_tree b, int max_iter, int abs_prec,
+                int use_max_norms) {
+    if (!out || !a || !b || !(prec > 0.0)) return MW_ERR_ARG;
+    if (out == a || out == b) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(out);
+    return guard(ctx, [&] {
+        check_same(out->tree, a->tree);
+        check_same(out->tree, b->tree);
+        mw_stats st{};
+        mwg::multiply(prec, out->tree, coef, a->tree, b->tree, max_iter, abs_prec != 0, use_max_norms != 0, st);
+        ctx->last = st;
+    });
+}
+
+int mw_square(double prec, mw_tree out, mw_tree inp, int max_iter, int abs_prec) {
+    return mw_multiply(prec, out, 1.0, inp, inp, max_iter, abs_prec, 0);
+}
+
+int mw_add(double prec, mw_tree out, int n, const double *coefs, const mw_tree *trees, int max_iter) {
+    (void)prec;
+    (void)max_iter;
+    if (!out || n < 1 || !coefs || !trees) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(out);
+    return guard(ctx, [&] {
+        std::vector<const mwg::Tree *> v;
+        std::vector<double> c(coefs, coefs + n);
+        for (int i = 0; i < n; i++) {
+            if (!trees[i] || trees[i] == out) throw mwg::Error(MW_ERR_ARG, "add: null tree or output among inputs");
+            check_same(out->tree, trees[i]->tree);
+            v.push_back(&trees[i]->tree);
+        }
+        mw_stats st{};
+        mwg::add(out->tree, v, c, st);
+        ctx->last = st;
+    });
+}
+
+}  // extern "C"

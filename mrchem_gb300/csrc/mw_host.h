@@ -1,0 +1,250 @@
+// mw_host.h -- host-side structures of the GB300 multiwavelet engine.
+//
+// Trees live on the device as SoA arrays (one FP64 block of 8*K^3
+// coefficients per node, 8 component norms per node); the host keeps the
+// integer structure (keys, parent/child links, Morton-sortable) and a copy of
+// the component norms, which is all the refinement and screening decisions
+// need.  Children of a node are always 8 consecutive nodes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/mw_gb300.h"
+
+namespace mwg {
+
+constexpr int KMAX = 10;          // largest K = order + 1 with a GPU kernel
+constexpr double SCREEN_FAC = 0.01;
+constexpr double ZERO_EXP = 45.0;
+constexpr double NS_CLEAN = 1e-13;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define MWG_CUDA(call)                                                                                     \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+            throw ::mwg::Error(e_ == cudaErrorMemoryAllocation ? MW_ERR_OOM : MW_ERR_CUDA,                 \
+                               std::string(#call) + ": " + cudaGetErrorString(e_));                        \
+    } while (0)
+
+struct Key {
+    int n, l[3];
+    bool operator==(const Key &o) const { return n == o.n && l[0] == o.l[0] && l[1] == o.l[1] && l[2] == o.l[2]; }
+};
+
+struct KeyHash {
+    size_t operator()(const Key &k) const {
+        uint64_t h = (uint64_t)(uint32_t)k.n * 0x9E3779B97F4A7C15ULL;
+        h ^= (uint64_t)(uint32_t)k.l[0] * 0xC2B2AE3D27D4EB4FULL;
+        h = (h << 21) | (h >> 43);
+        h ^= (uint64_t)(uint32_t)k.l[1] * 0x165667B19E3779F9ULL;
+        h = (h << 21) | (h >> 43);
+        h ^= (uint64_t)(uint32_t)k.l[2] * 0xD6E8FEB86659FD93ULL;
+        h ^= h >> 31;
+        h *= 0xBF58476D1CE4E5B9ULL;
+        h ^= h >> 29;
+        return (size_t)h;
+    }
+};
+
+inline int floordiv2(int l) { return (l - (l & 1)) / 2; }
+
+// ---------------------------------------------------------------- basis
+struct Basis {
+    int n0, corner[3], boxes[3], k, K, type, max_depth, bs;
+    std::vector<double> qx, qw, legq, c2v, v2c, integ, W, WT;
+    void init(int root_scale, const int *corner, const int *boxes, int order, int type, int max_depth);
+    void eval(double x, double *out) const;  // all K scaling functions at x in [0,1]
+    bool in_world(int n, const int *l) const;
+    int max_scale() const { return n0 + max_depth - 1; }
+};
+
+void gauss_legendre(int n, double *x, double *w);
+void legendre_shifted(int n, double x, double *p);
+
+// ---------------------------------------------------------------- device basis data
+struct DevBasis {
+    int K, type;
+    const double *W, *WT, *c2v, *v2c, *qx, *qw, *legq;  // device
+};
+
+// ---------------------------------------------------------------- context
+struct Ctx;
+
+struct NodeInfo {
+    int n, l[3];
+    int parent, child0;
+};
+
+struct Tree {
+    Ctx *ctx = nullptr;
+    std::vector<NodeInfo> nodes;
+    std::unordered_map<Key, int, KeyHash> map;
+    std::vector<double> cn;       // 8 component norms per node (host copy)
+    double *d_coefs = nullptr;    // cap * bs
+    double *d_cn = nullptr;       // cap * 8
+    float *d_coefs32 = nullptr;   // FP32 shadow (mixed-precision applies), cap32 blocks
+    size_t cap = 0, cap32 = 0;
+    int nroots = 0;
+
+    int find(int n, const int *l) const {
+        auto it = map.find(Key{n, {l[0], l[1], l[2]}});
+        return it == map.end() ? -1 : it->second;
+    }
+    int nn() const { return (int)nodes.size(); }
+    double *block(int i) const;
+    void reserve(size_t n);
+    int add(int n, const int *l, int parent);
+    int split(int i);
+    void reset_roots();
+    void download_norms(int first, int count);
+    double sqnorm_leaves() const;
+    int max_scale() const;
+    void free_device();
+};
+
+struct Oper {
+    Ctx *ctx = nullptr;
+    int kind = 0;  // 0 poisson, 1 helmholtz
+    double mu = 0, prec = 0, eps = 0, rmin = 0, rmax = 0;
+    int T = 0, S = 0;
+    std::vector<double> c, a;
+    std::vector<int> band;       // [T*S]
+    std::vector<long> off;       // [T*S] block index of l = -band
+    std::vector<double> norms;   // 4 per block, [g][f]
+    std::vector<double> amax, xmax;  // per (t,s)
+    long nblocks = 0;
+    double *d_blocks = nullptr;  // (2K)^2 per block, FP64
+    float *d_blocks32 = nullptr; // FP32 copy
+    uint16_t *d_blocks16 = nullptr; // BF16 copy (bit patterns)
+    const double *norm(int t, int s, int l) const { return &norms[(size_t)(off[t * S + s] + l + band[t * S + s]) * 4]; }
+    long block_index(int t, int s, int l) const { return off[t * S + s] + l + band[t * S + s]; }
+    void build(const Basis &b);
+};
+
+// Device bump allocator for per-call scratch (task lists, items, generated
+// blocks).  reset() keeps one chunk large enough for the previous peak.
+struct Arena {
+    struct Chunk {
+        void *ptr = nullptr;
+        size_t size = 0, used = 0;
+    };
+    std::vector<Chunk> chunks;
+    size_t total = 0;
+    void *alloc(size_t bytes);
+    void reset();
+    void release();
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Basis basis;
+    DevBasis dbasis{};
+    double *d_basis = nullptr;
+    std::string err;
+    mw_stats last{};
+    int nsm = 0;
+    Arena arena;
+    void *h_pinned = nullptr;
+    size_t pinned_bytes = 0;
+    void *pinned(size_t bytes);
+    void sync();
+};
+
+// Packs host arrays into the context's pinned buffer and ships them to the
+// device with a single copy; ptr(i) is the device address of array i.
+struct Packer {
+    std::vector<size_t> offs, size;
+    std::vector<const void *> srcs;
+    char *dev = nullptr;
+    void *add(const void *src, size_t bytes);
+    void ship(Ctx &ctx, Arena &arena);
+    void *ptr(size_t i) const { return dev + offs[i]; }
+};
+
+// ---------------------------------------------------------------- kernel interface (mw_kernels.cu)
+struct GenTask {
+    const double *anc;  // ancestor block
+    double *out;        // generated block
+    double *cn;         // 8 norms of the generated block
+    uint64_t path;      // 3 bits per step, first step in the lowest bits
+    int steps;
+    int pad;
+};
+
+struct ProjFunc {
+    int kind;  // 0 gaussian sum, 1 hydrogen
+    int nterms;
+    const mw_gterm *terms;  // device
+    int hn, hl, hm;
+    double Z, origin[3], hnorm;
+};
+
+struct ProjTask {
+    int n, l[3];
+    double *out;
+    double *cn;
+    int zero;
+    int pad;
+};
+
+struct ApplyLaunch {
+    int nnodes;
+    int root;                     // 1: include the (0,0) component pair
+    int set;                      // 1: write the block, 0: add to it
+    double *const *out;           // per node: output block
+    const long long *begin;       // per node + 1: item range
+    const void *const *in;        // per item: input block (double or float)
+    const void *const *ax;        // per item: operator blocks (double or float)
+    const void *const *ay;
+    const void *const *az;
+    const double *coef;           // per item
+    int *counter;                 // dynamic node counter (persistent grid)
+};
+
+struct PairTask {  // parent -> children (8 consecutive blocks)
+    double *parent;
+    double *child0;
+};
+
+struct MulTask {
+    const double *a, *b;
+    double *out;
+    double *cn;
+    double scale;  // coef * 2^{3(n+1)/2}
+};
+
+struct AddTask {
+    double *out;
+    double *cn;
+    int first, count;  // into the (src, coef) arrays
+};
+
+void k_project(const DevBasis &b, const ProjFunc &f, const ProjTask *tasks, int n, cudaStream_t s);
+void k_generate(const DevBasis &b, const GenTask *tasks, int n, cudaStream_t s);
+void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s);
+void k_norms(const DevBasis &b, double *const *blocks, double *const *cn, int n, cudaStream_t s);
+void k_topdown(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s);
+void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s);
+void k_multiply(const DevBasis &b, const MulTask *tasks, int n, cudaStream_t s);
+void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
+           cudaStream_t s);
+void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);
+void k_dot(const double *const *a, const double *const *b, const int *start, int n, int bs, double *partial,
+           cudaStream_t s);
+void k_scale(double *x, size_t n, double c, cudaStream_t s);
+void k_eval(const DevBasis &b, const double *const *blocks, const int *keys, const double *pts, int npts,
+            double *out, cudaStream_t s);
+
+}  // namespace mwg

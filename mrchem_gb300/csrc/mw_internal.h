@@ -1,0 +1,61 @@
+// mw_internal.h -- driver-level declarations shared by the host translation units.
+#pragma once
+
+#include "mw_host.h"
+
+namespace mwg {
+
+// generated (reconstructed) blocks of one source tree at requested positions
+struct GenSet {
+    std::unordered_map<Key, int, KeyHash> slot;
+    std::vector<Key> keys;
+    std::vector<int> anc;
+    std::vector<GenTask> tasks;
+    void clear();
+    int request(const Tree &src, int n, const int *l, int ancestor);
+    double *generate(const Tree &src, Arena &arena, std::vector<double> &cn_out, mw_stats *st);
+};
+
+int find_ancestor(const Tree &t, int n, const int *l, int *an_out);
+const double *block_at(const Tree &src, const GenSet &gs, const double *gbase, int n, const int *l);
+bool key_less(const Basis &b, const NodeInfo &x, const NodeInfo &y);
+std::vector<int> canonical_order(const Tree &t);
+
+void tree_zero(Tree &t, int first, int count);
+void tree_clear(Tree &t);
+void tree_compress(Tree &t, Arena &arena, mw_stats *st);
+void tree_norms_all(Tree &t, Arena &arena);
+void tree_upload(Tree &t, int nnodes, const int *keys, const double *coefs, Arena &arena);
+void tree_download(Tree &t, int *keys, double *coefs, unsigned char *leaf);
+
+void project_gauss(double prec, Tree &t, int nterms, const mw_gterm *terms, bool abs_prec, Arena &arena);
+void project_hydrogen(double prec, Tree &t, int n, int l, int m, double Z, const double *origin, bool abs_prec,
+                      Arena &arena);
+
+void copy_grid(Tree &out, const Tree &inp);
+void build_grid(Tree &out, const std::vector<const Tree *> &trees);
+void combine_on_grid(Tree &out, const std::vector<const Tree *> &trees, const std::vector<double> &coefs, Arena &arena,
+                     mw_stats *st);
+void copy_func(Tree &out, const Tree &inp, Arena &arena);
+void crop(Tree &t, double prec, bool abs_prec, Arena &arena);
+double dot(const Tree &a, const Tree &b, Arena &arena);
+double integrate(const Tree &t);
+void rescale(Tree &t, double c);
+void eval_points(const Tree &t, int npts, const double *xyz, double *out, Arena &arena);
+
+struct ApplyJob {
+    Tree *out;
+    Oper *op;
+    Tree *inp;
+    double prec;
+    bool abs_prec;
+    int max_iter;
+    std::vector<Tree *> prec_trees;
+};
+
+void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st);
+void multiply(double prec, Tree &out, double coef, Tree &a, Tree &b, int max_iter, bool abs_prec, bool use_max_norms,
+              mw_stats &st);
+void add(Tree &out, const std::vector<const Tree *> &trees, const std::vector<double> &coefs, mw_stats &st);
+
+}  // namespace mwg

@@ -1,0 +1,642 @@
+// mw_kernels.cu -- sm_103a kernels of the multiwavelet engine.
+//
+// Layouts: a node block is 8*K^3 doubles, component-major (component
+// c = cx|cy<<1|cz<<2, inner index ix + K*iy + K*K*iz).  Inside a CTA a block
+// is staged as the (2K)^3 "cube" cube[Z][Y][X] with X = cx*K + ix, so a
+// multiwavelet transform or a non-standard-form operator application is three
+// 2K x 2K matrix passes, one per dimension.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mw_host.h"
+
+namespace mwg {
+
+namespace {
+
+__device__ __forceinline__ int cube_of_block(int gi, int K) {
+    int K3 = K * K * K;
+    int c = gi / K3, r = gi - c * K3;
+    int iz = r / (K * K), iy = (r / K) % K, ix = r % K;
+    int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
+    int N2 = 2 * K;
+    return (Z * N2 + Y) * N2 + X;
+}
+
+// cube <- (M (x) M (x) M) cube, M 2K x 2K row-major; tmp is a second cube buffer
+__device__ void cube_transform(double *cube, double *tmp, const double *M, int K) {
+    int N2 = 2 * K, C = N2 * N2 * N2;
+    for (int i = threadIdx.x; i < C; i += blockDim.x) {
+        int X = i % N2, YZ = i / N2;
+        const double *src = cube + YZ * N2;
+        double s = 0.0;
+        for (int k = 0; k < N2; k++) s += M[X * N2 + k] * src[k];
+        tmp[i] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < C; i += blockDim.x) {
+        int X = i % N2, Y = (i / N2) % N2, Z = i / (N2 * N2);
+        double s = 0.0;
+        for (int k = 0; k < N2; k++) s += M[Y * N2 + k] * tmp[(Z * N2 + k) * N2 + X];
+        cube[i] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < C; i += blockDim.x) {
+        int XY = i % (N2 * N2), Z = i / (N2 * N2);
+        double s = 0.0;
+        for (int k = 0; k < N2; k++) s += M[Z * N2 + k] * cube[k * N2 * N2 + XY];
+        tmp[i] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < C; i += blockDim.x) cube[i] = tmp[i];
+    __syncthreads();
+}
+
+// per-dimension K x K map on each half of every dimension (children-wise map)
+__device__ void cube_map_halves(double *cube, double *tmp, const double *A, int K) {
+    int N2 = 2 * K, C = N2 * N2 * N2;
+    for (int i = threadIdx.x; i < C; i += blockDim.x) {
+        int X = i % N2, YZ = i / N2, hx = (X / K) * K, x = X % K;
+        double s = 0.0;
+        for (int k = 0; k < K; k++) s += A[x * K + k] * cube[YZ * N2 + hx + k];
+        tmp[i] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < C; i += blockDim.x) {
+        int X = i % N2, Y = (i / N2) % N2, Z = i / (N2 * N2), hy = (Y / K) * K, y = Y % K;
+        double s = 0.0;
+        for (int k = 0; k < K; k++) s += A[y * K + k] * tmp[(Z * N2 + hy + k) * N2 + X];
+        cube[i] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < C; i += blockDim.x) {
+        int XY = i % (N2 * N2), Z = i / (N2 * N2), hz = (Z / K) * K, z = Z % K;
+        double s = 0.0;
+        for (int k = 0; k < K; k++) s += A[z * K + k] * cube[(hz + k) * N2 * N2 + XY];
+        tmp[i] = s;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < C; i += blockDim.x) cube[i] = tmp[i];
+    __syncthreads();
+}
+
+__device__ void load_block(double *cube, const double *g, int K) {
+    int n = 8 * K * K * K;
+    for (int gi = threadIdx.x; gi < n; gi += blockDim.x) cube[cube_of_block(gi, K)] = g[gi];
+    __syncthreads();
+}
+
+__device__ void store_block(double *g, const double *cube, int K) {
+    int n = 8 * K * K * K;
+    for (int gi = threadIdx.x; gi < n; gi += blockDim.x) g[gi] = cube[cube_of_block(gi, K)];
+}
+
+// 8 component norms of a block in global memory; deterministic fixed-order reduction
+__device__ void block_norms(const double *g, double *cn, int K, double *red) {
+    int K3 = K * K * K;
+    int nt = blockDim.x;
+    for (int c = 0; c < 8; c++) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < K3; i += nt) {
+            double v = g[c * K3 + i];
+            s += v * v;
+        }
+        red[c * nt + threadIdx.x] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double s = 0.0;
+        for (int i = 0; i < nt; i++) s += red[threadIdx.x * nt + i];
+        cn[threadIdx.x] = sqrt(s);
+    }
+    __syncthreads();
+}
+
+__device__ void basis_eval(const DevBasis &b, double x, double *out) {
+    int K = b.K;
+    double p[KMAX];
+    double t = 2.0 * x - 1.0;
+    p[0] = 1.0;
+    if (K > 1) p[1] = t;
+    for (int j = 1; j + 1 < K; j++) p[j + 1] = ((2.0 * j + 1.0) * t * p[j] - j * p[j - 1]) / (j + 1.0);
+    for (int j = 0; j < K; j++) p[j] *= sqrt(2.0 * j + 1.0);
+    if (b.type == MW_BASIS_LEGENDRE) {
+        for (int j = 0; j < K; j++) out[j] = p[j];
+        return;
+    }
+    for (int j = 0; j < K; j++) {
+        double s = 0.0;
+        for (int i = 0; i < K; i++) s += b.legq[j * K + i] * p[i];
+        out[j] = sqrt(b.qw[j]) * s;
+    }
+}
+
+// ----------------------------------------------------------------- projection
+__device__ double laguerre(int k, int a, double x) {
+    if (k == 0) return 1.0;
+    double l0 = 1.0, l1 = 1.0 + a - x;
+    for (int j = 1; j < k; j++) {
+        double l2 = ((2.0 * j + 1.0 + a - x) * l1 - (j + a) * l0) / (j + 1.0);
+        l0 = l1;
+        l1 = l2;
+    }
+    return l1;
+}
+
+__device__ double func_eval(const ProjFunc &f, double x, double y, double z) {
+    if (f.kind == 0) {
+        double v = 0.0;
+        for (int t = 0; t < f.nterms; t++) {
+            const mw_gterm &g = f.terms[t];
+            double dx = x - g.pos[0], dy = y - g.pos[1], dz = z - g.pos[2];
+            double e = g.alpha * (dx * dx + dy * dy + dz * dz);
+            if (e > 700.0) continue;
+            double p = g.coef;
+            for (int i = 0; i < g.pw[0]; i++) p *= dx;
+            for (int i = 0; i < g.pw[1]; i++) p *= dy;
+            for (int i = 0; i < g.pw[2]; i++) p *= dz;
+            v += p * exp(-e);
+        }
+        return v;
+    }
+    double q[3] = {x - f.origin[0], y - f.origin[1], z - f.origin[2]};
+    double rr = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+    double rho = 2.0 * f.Z * rr / f.hn;
+    double rad = f.hnorm * pow(rho, (double)f.hl) * laguerre(f.hn - f.hl - 1, 2 * f.hl + 1, rho) * exp(-0.5 * rho);
+    double ang = 0.5 / sqrt(3.14159265358979323846);
+    if (f.hl == 1) ang *= sqrt(3.0) * (rr > 0.0 ? q[f.hm] / rr : 0.0);
+    return rad * ang;
+}
+
+__global__ void project_kernel(DevBasis b, ProjFunc f, const ProjTask *tasks, int n) {
+    extern __shared__ double sm[];
+    int K = b.K, N2 = 2 * K, C = N2 * N2 * N2;
+    double *cube = sm, *tmp = sm + C, *red = sm + 2 * C;
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        ProjTask task = tasks[t];
+        if (task.zero) {
+            for (int i = threadIdx.x; i < C; i += blockDim.x) task.out[i] = 0.0;
+            if (threadIdx.x < 8) task.cn[threadIdx.x] = 0.0;
+            __syncthreads();
+            continue;
+        }
+        double h = ldexp(1.0, -(task.n + 1));
+        for (int i = threadIdx.x; i < C; i += blockDim.x) {
+            int X = i % N2, Y = (i / N2) % N2, Z = i / (N2 * N2);
+            double x = h * (2 * task.l[0] + X / K + b.qx[X % K]);
+            double y = h * (2 * task.l[1] + Y / K + b.qx[Y % K]);
+            double z = h * (2 * task.l[2] + Z / K + b.qx[Z % K]);
+            cube[i] = func_eval(f, x, y, z);
+        }
+        __syncthreads();
+        cube_map_halves(cube, tmp, b.v2c, K);
+        double sc = pow(2.0, -1.5 * (task.n + 1));
+        for (int i = threadIdx.x; i < C; i += blockDim.x) cube[i] *= sc;
+        __syncthreads();
+        cube_transform(cube, tmp, b.W, K);
+        store_block(task.out, cube, K);
+        __syncthreads();
+        block_norms(task.out, task.cn, K, red);
+    }
+}
+
+// ----------------------------------------------------------------- generated nodes
+__global__ void generate_kernel(DevBasis b, const GenTask *tasks, int n) {
+    extern __shared__ double sm[];
+    int K = b.K, N2 = 2 * K, C = N2 * N2 * N2, K3 = K * K * K;
+    double *cube = sm, *tmp = sm + C, *red = sm + 2 * C;
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        GenTask task = tasks[t];
+        load_block(cube, task.anc, K);
+        for (int s = 0; s < task.steps; s++) {
+            int c = (int)((task.path >> (3 * s)) & 7);
+            int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
+            // child c's scaling part: rows b*K.. of W^T in each dimension
+            for (int i = threadIdx.x; i < N2 * N2 * K; i += blockDim.x) {
+                int x = i % K, YZ = i / K;
+                double acc = 0.0;
+                for (int k = 0; k < N2; k++) acc += b.WT[(bx * K + x) * N2 + k] * cube[YZ * N2 + k];
+                tmp[YZ * K + x] = acc;  // tmp[Z][Y][x]
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < N2 * K * K; i += blockDim.x) {
+                int x = i % K, y = (i / K) % K, Z = i / (K * K);
+                double acc = 0.0;
+                for (int k = 0; k < N2; k++) acc += b.WT[(by * K + y) * N2 + k] * tmp[(Z * N2 + k) * K + x];
+                cube[i] = acc;  // cube[Z][y][x] (compact)
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                int xy = i % (K * K), z = i / (K * K);
+                double acc = 0.0;
+                for (int k = 0; k < N2; k++) acc += b.WT[(bz * K + z) * N2 + k] * cube[k * K * K + xy];
+                tmp[i] = acc;  // s[z][y][x]
+            }
+            __syncthreads();
+            for (int i = threadIdx.x; i < C; i += blockDim.x) {
+                int X = i % N2, Y = (i / N2) % N2, Z = i / (N2 * N2);
+                cube[i] = (X < K && Y < K && Z < K) ? tmp[(Z * K + Y) * K + X] : 0.0;
+            }
+            __syncthreads();
+        }
+        store_block(task.out, cube, K);
+        __syncthreads();
+        block_norms(task.out, task.cn, K, red);
+    }
+}
+
+// ----------------------------------------------------------------- NS-form apply
+// One CTA per output node (persistent grid, dynamic node counter).  Thread
+// (Yp, Xp) owns the output column cube[:, Yp, Xp] in registers.  Per item:
+//   x pass  t1[Z][Y][X'] = sum_X Ax[X'][X] in[Z][Y][X]            (shared)
+//   y pass  t2[Z]        = sum_Y Ay[Y'][Y] t1[Z][Y][X']           (registers)
+//   z pass  acc[Z']     += c sum_Z Az[Z'][Z] t2[Z]
+// Below the root scale the all-scaling path (f = 000 -> g = 000) is left out
+// exactly: u holds the wavelet-in-x part of t1 on the scaling octant, and
+// t2x the y pass that avoids the scaling-scaling path, used by g = 000.
+template <typename T, int K>
+__global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32) apply_kernel(ApplyLaunch L) {
+    constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *s_in = reinterpret_cast<T *>(smem_raw);
+    T *s_t1 = s_in + C;
+    T *s_u = s_t1 + C;
+    T *s_A = s_u + K3;
+    __shared__ int s_node;
+    const int tid = threadIdx.x;
+    const bool active = tid < NC;
+    const int Yp = tid / N2, Xp = tid % N2;
+    const bool excl = !L.root && active && (Yp < K) && (Xp < K);
+
+    while (true) {
+        if (tid == 0) s_node = atomicAdd(L.counter, 1);
+        __syncthreads();
+        const int w = s_node;
+        if (w >= L.nnodes) break;
+        T acc[N2];
+#pragma unroll
+        for (int z = 0; z < N2; z++) acc[z] = T(0);
+        const long long b0 = L.begin[w], b1 = L.begin[w + 1];
+        for (long long j = b0; j < b1; j++) {
+            __syncthreads();
+            const T *gin = reinterpret_cast<const T *>(L.in[j]);
+            for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
+                int c = gi / K3, r = gi - c * K3;
+                int iz = r / (K * K), iy = (r / K) % K, ix = r % K;
+                int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
+                s_in[(Z * N2 + Y) * N2 + X] = gin[gi];
+            }
+            const T *ax = reinterpret_cast<const T *>(L.ax[j]);
+            const T *ay = reinterpret_cast<const T *>(L.ay[j]);
+            const T *az = reinterpret_cast<const T *>(L.az[j]);
+            for (int i = tid; i < NC; i += blockDim.x) {
+                s_A[i] = ax[i];
+                s_A[NC + i] = ay[i];
+                s_A[2 * NC + i] = az[i];
+            }
+            const T cf = T(L.coef[j]);
+            __syncthreads();
+            if (active) {
+                const T *arow = s_A + Xp * N2;
+                T a[N2];
+#pragma unroll
+                for (int X = 0; X < N2; X++) a[X] = arow[X];
+#pragma unroll 2
+                for (int Z = 0; Z < N2; Z++) {
+                    const T *src = s_in + (Z * N2 + Yp) * N2;
+                    T s0 = T(0), s1 = T(0);
+#pragma unroll
+                    for (int X = 0; X < K; X++) s0 += a[X] * src[X];
+#pragma unroll
+                    for (int X = K; X < N2; X++) s1 += a[X] * src[X];
+                    s_t1[(Z * N2 + Yp) * N2 + Xp] = s0 + s1;
+                    if (excl && Z < K) s_u[(Z * K + Yp) * K + Xp] = s1;
+                }
+            }
+            __syncthreads();
+            if (active) {
+                const T *arow = s_A + NC + Yp * N2;
+                T t2[N2], t2x[K];
+#pragma unroll
+                for (int Z = 0; Z < N2; Z++) {
+                    T s0 = T(0), s1 = T(0);
+#pragma unroll
+                    for (int Y = 0; Y < K; Y++) s0 += arow[Y] * s_t1[(Z * N2 + Y) * N2 + Xp];
+#pragma unroll
+                    for (int Y = K; Y < N2; Y++) s1 += arow[Y] * s_t1[(Z * N2 + Y) * N2 + Xp];
+                    t2[Z] = s0 + s1;
+                    if (Z < K) {
+                        T su = T(0);
+                        if (excl) {
+#pragma unroll
+                            for (int Y = 0; Y < K; Y++) su += arow[Y] * s_u[(Z * K + Y) * K + Xp];
+                        }
+                        t2x[Z] = su + s1;
+                    }
+                }
+                const T *azm = s_A + 2 * NC;
+#pragma unroll
+                for (int Zp = 0; Zp < N2; Zp++) {
+                    T s = T(0);
+#pragma unroll
+                    for (int Z = 0; Z < N2; Z++) {
+                        T v = t2[Z];
+                        if (Zp < K && Z < K) v = excl ? t2x[Z < K ? Z : 0] : v;
+                        s += azm[Zp * N2 + Z] * v;
+                    }
+                    acc[Zp] += cf * s;
+                }
+            }
+        }
+        if (active) {
+            double *out = L.out[w];
+#pragma unroll
+            for (int Zp = 0; Zp < N2; Zp++) {
+                int c = (Xp >= K ? 1 : 0) | (Yp >= K ? 2 : 0) | (Zp >= K ? 4 : 0);
+                int gi = c * K3 + (Zp % K) * K * K + (Yp % K) * K + (Xp % K);
+                if (L.set)
+                    out[gi] = double(acc[Zp]);
+                else
+                    out[gi] += double(acc[Zp]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T, int K>
+void launch_apply_t(const ApplyLaunch &L, int nsm, cudaStream_t s) {
+    constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K;
+    const int threads = ((NC + 31) / 32) * 32;
+    const size_t smem = sizeof(T) * (2 * C + K3 + 3 * NC);
+    auto fn = apply_kernel<T, K>;
+    MWG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    MWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    if (per_sm < 1) per_sm = 1;
+    int grid = nsm * per_sm;
+    if (grid > L.nnodes) grid = L.nnodes;
+    if (grid < 1) return;
+    fn<<<grid, threads, smem, s>>>(L);
+    MWG_CUDA(cudaGetLastError());
+}
+
+template <typename T>
+void launch_apply_k(int K, const ApplyLaunch &L, int nsm, cudaStream_t s) {
+    switch (K) {
+        case 4: launch_apply_t<T, 4>(L, nsm, s); break;
+        case 5: launch_apply_t<T, 5>(L, nsm, s); break;
+        case 6: launch_apply_t<T, 6>(L, nsm, s); break;
+        case 7: launch_apply_t<T, 7>(L, nsm, s); break;
+        case 8: launch_apply_t<T, 8>(L, nsm, s); break;
+        case 9: launch_apply_t<T, 9>(L, nsm, s); break;
+        case 10: launch_apply_t<T, 10>(L, nsm, s); break;
+        default: throw Error(MW_ERR_ARG, "no apply kernel for this order");
+    }
+}
+
+// ----------------------------------------------------------------- post-processing
+__global__ void norms_kernel(DevBasis b, double *const *blocks, double *const *cn, int n) {
+    extern __shared__ double sm[];
+    for (int t = blockIdx.x; t < n; t += gridDim.x) block_norms(blocks[t], cn[t], b.K, sm);
+}
+
+__global__ void topdown_kernel(DevBasis b, const PairTask *tasks, int n) {
+    extern __shared__ double sm[];
+    int K = b.K, N2 = 2 * K, C = N2 * N2 * N2, K3 = K * K * K;
+    double *cube = sm, *tmp = sm + C;
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        PairTask task = tasks[t];
+        load_block(cube, task.parent, K);
+        cube_transform(cube, tmp, b.WT, K);
+        // children's scaling parts += reconstruction; child c occupies octant c of the cube
+        for (int gi = threadIdx.x; gi < 8 * K3; gi += blockDim.x) {
+            int c = gi / K3, r = gi - c * K3;
+            double *child = task.child0 + (size_t)c * 8 * K3;
+            child[r] += cube[cube_of_block(gi, K)];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void compress_kernel(DevBasis b, const PairTask *tasks, double *const *cn, int n) {
+    extern __shared__ double sm[];
+    int K = b.K, N2 = 2 * K, C = N2 * N2 * N2, K3 = K * K * K;
+    double *cube = sm, *tmp = sm + C, *red = sm + 2 * C;
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        PairTask task = tasks[t];
+        for (int gi = threadIdx.x; gi < 8 * K3; gi += blockDim.x) {
+            int c = gi / K3, r = gi - c * K3;
+            cube[cube_of_block(gi, K)] = task.child0[(size_t)c * 8 * K3 + r];
+        }
+        __syncthreads();
+        cube_transform(cube, tmp, b.W, K);
+        store_block(task.parent, cube, K);
+        __syncthreads();
+        block_norms(task.parent, cn[t], K, red);
+    }
+}
+
+__global__ void multiply_kernel(DevBasis b, const MulTask *tasks, int n) {
+    extern __shared__ double sm[];
+    int K = b.K, N2 = 2 * K, C = N2 * N2 * N2;
+    double *ca = sm, *cb = sm + C, *tmp = sm + 2 * C, *red = sm + 3 * C;
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        MulTask task = tasks[t];
+        load_block(ca, task.a, K);
+        load_block(cb, task.b, K);
+        cube_transform(ca, tmp, b.WT, K);
+        cube_map_halves(ca, tmp, b.c2v, K);
+        cube_transform(cb, tmp, b.WT, K);
+        cube_map_halves(cb, tmp, b.c2v, K);
+        for (int i = threadIdx.x; i < C; i += blockDim.x) ca[i] = ca[i] * cb[i] * task.scale;
+        __syncthreads();
+        cube_map_halves(ca, tmp, b.v2c, K);
+        cube_transform(ca, tmp, b.W, K);
+        store_block(task.out, ca, K);
+        __syncthreads();
+        block_norms(task.out, task.cn, K, red);
+    }
+}
+
+__global__ void add_kernel(DevBasis b, const AddTask *tasks, const double *const *src, const double *coefs, int n,
+                           int bs) {
+    extern __shared__ double sm[];
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        AddTask task = tasks[t];
+        for (int i = threadIdx.x; i < bs; i += blockDim.x) {
+            double s = 0.0;
+            for (int k = 0; k < task.count; k++) s += coefs[task.first + k] * src[task.first + k][i];
+            task.out[i] = s;
+        }
+        __syncthreads();
+        block_norms(task.out, task.cn, b.K, sm);
+    }
+}
+
+__global__ void to_fp32_kernel(const double *in, float *out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+__global__ void scale_kernel(double *x, size_t n, double c) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        x[i] *= c;
+}
+
+__global__ void dot_kernel(const double *const *a, const double *const *bb, const int *start, int n, int bs,
+                           double *partial) {
+    extern __shared__ double sm[];
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        const double *x = a[t], *y = bb[t];
+        double s = 0.0;
+        for (int i = start[t] + threadIdx.x; i < bs; i += blockDim.x) s += x[i] * y[i];
+        sm[threadIdx.x] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int i = 0; i < (int)blockDim.x; i++) tot += sm[i];
+            partial[t] = tot;
+        }
+        __syncthreads();
+    }
+}
+
+// point evaluation: one CTA per point; blocks[p] is the leaf containing point p, keys[4p] its key
+__global__ void eval_kernel(DevBasis b, const double *const *blocks, const int *keys, const double *pts, int npts,
+                            double *out) {
+    extern __shared__ double sm[];
+    int K = b.K, N2 = 2 * K, C = N2 * N2 * N2, K3 = K * K * K;
+    double *cube = sm, *tmp = sm + C, *red = sm + 2 * C;
+    for (int p = blockIdx.x; p < npts; p += gridDim.x) {
+        int n = keys[4 * p];
+        load_block(cube, blocks[p], K);
+        cube_transform(cube, tmp, b.WT, K);
+        double h = ldexp(1.0, -(n + 1));
+        int c = 0;
+        double y[3];
+        for (int d = 0; d < 3; d++) {
+            double r = pts[3 * p + d];
+            int cl = (int)floor(r / h);
+            int lo = 2 * keys[4 * p + 1 + d];
+            if (cl < lo) cl = lo;
+            if (cl > lo + 1) cl = lo + 1;
+            c |= (cl - lo) << d;
+            y[d] = r / h - cl;
+        }
+        double ph[3][KMAX];
+        for (int d = 0; d < 3; d++) basis_eval(b, y[d], ph[d]);
+        double s = 0.0;
+        for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+            int ix = i % K, iy = (i / K) % K, iz = i / (K * K);
+            s += cube[cube_of_block(c * K3 + i, K)] * ph[0][ix] * ph[1][iy] * ph[2][iz];
+        }
+        red[threadIdx.x] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int i = 0; i < (int)blockDim.x; i++) tot += red[i];
+            out[p] = tot * pow(2.0, 1.5 * (n + 1));
+        }
+        __syncthreads();
+    }
+}
+
+int grid_for(int n) { return n < 4096 ? (n > 0 ? n : 1) : 4096; }
+
+size_t cube_bytes(int K) { return sizeof(double) * 8 * K * K * K; }
+
+}  // namespace
+
+void k_project(const DevBasis &b, const ProjFunc &f, const ProjTask *tasks, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    size_t smem = 2 * cube_bytes(b.K) + 8 * 256 * sizeof(double);
+    MWG_CUDA(cudaFuncSetAttribute(project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    project_kernel<<<grid_for(n), 256, smem, s>>>(b, f, tasks, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_generate(const DevBasis &b, const GenTask *tasks, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    size_t smem = 2 * cube_bytes(b.K) + 8 * 256 * sizeof(double);
+    MWG_CUDA(cudaFuncSetAttribute(generate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    generate_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s) {
+    if (L.nnodes <= 0) return;
+    MWG_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(int), s));
+    if (fp32)
+        launch_apply_k<float>(b.K, L, nsm, s);
+    else
+        launch_apply_k<double>(b.K, L, nsm, s);
+}
+
+void k_norms(const DevBasis &b, double *const *blocks, double *const *cn, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    norms_kernel<<<grid_for(n), 256, 8 * 256 * sizeof(double), s>>>(b, blocks, cn, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_topdown(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    size_t smem = 2 * cube_bytes(b.K);
+    MWG_CUDA(cudaFuncSetAttribute(topdown_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    topdown_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    size_t smem = 2 * cube_bytes(b.K) + 8 * 256 * sizeof(double);
+    MWG_CUDA(cudaFuncSetAttribute(compress_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    compress_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, cn, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_multiply(const DevBasis &b, const MulTask *tasks, int n, cudaStream_t s) {
+    if (n <= 0) return;
+    size_t smem = 3 * cube_bytes(b.K) + 8 * 256 * sizeof(double);
+    MWG_CUDA(cudaFuncSetAttribute(multiply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    multiply_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
+           cudaStream_t s) {
+    if (n <= 0) return;
+    add_kernel<<<grid_for(n), 256, 8 * 256 * sizeof(double), s>>>(b, tasks, src, coefs, n, bs);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s) {
+    if (n == 0) return;
+    to_fp32_kernel<<<4096, 256, 0, s>>>(in, out, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_scale(double *x, size_t n, double c, cudaStream_t s) {
+    if (n == 0) return;
+    scale_kernel<<<4096, 256, 0, s>>>(x, n, c);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_dot(const double *const *a, const double *const *b, const int *start, int n, int bs, double *partial,
+           cudaStream_t s) {
+    if (n <= 0) return;
+    dot_kernel<<<grid_for(n), 256, 256 * sizeof(double), s>>>(a, b, start, n, bs, partial);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_eval(const DevBasis &b, const double *const *blocks, const int *keys, const double *pts, int npts,
+            double *out, cudaStream_t s) {
+    if (npts <= 0) return;
+    size_t smem = 2 * cube_bytes(b.K) + 256 * sizeof(double);
+    MWG_CUDA(cudaFuncSetAttribute(eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    eval_kernel<<<grid_for(npts), 256, smem, s>>>(b, blocks, keys, pts, npts, out);
+    MWG_CUDA(cudaGetLastError());
+}
+
+}  // namespace mwg
