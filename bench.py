@@ -29,7 +29,8 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 SEED = 20261203
-NORB, ORDER, PREC = 16, 9, 1e-6
+ORDER, PREC = 9, 1e-6
+NORB = 16
 METRIC = "Helmholtz-apply nodes/s: batched mixed vs plain FP64 GPU at 1e-6 rel. error"
 
 
@@ -98,7 +99,7 @@ def measured_peaks():
 
 
 def cpu_sample(terms, mus, max_iter):
-    """Oracle (OpenMP FP64) Helmholtz apply of orbital 0, first max_iter refinement levels."""
+    """Oracle (OpenMP FP64) Helmholtz apply of orbital 0 (max_iter = -1: the complete adaptive apply)."""
     from oracle import pyoracle as po
     po.build()
     threads = os.cpu_count() or 1
@@ -112,8 +113,8 @@ def cpu_sample(terms, mus, max_iter):
     st = po.apply(PREC, out, op, phi, max_iter=max_iter, abs_prec=True)
     dt = time.perf_counter() - t0
     return {"value": st["out_nodes"] / dt, "unit": "nodes/s", "cores": threads, "kind": "port",
-            "sample": "orbital 0 of the batch, levels 0..%d of the adaptive apply (%d output nodes, %.1f s)"
-                      % (max_iter, st["out_nodes"], dt)}
+            "sample": "orbital 0 of the batch, %s adaptive apply (%d output nodes, %.1f s)"
+                      % ("complete" if max_iter < 0 else "levels 0..%d of the" % max_iter, st["out_nodes"], dt)}
 
 
 def run_reference(args):
@@ -182,13 +183,25 @@ def run(args):
         return mw.apply_batch([PREC] * NORB, outs, ops, phis, abs_prec=True, precision=precision)
 
     outs = [mw.FunctionTree(mra) for _ in range(NORB)]
-    # plain FP64 reference result (also the error reference)
-    barrier()
-    t0 = time.perf_counter()
-    st64 = step("fp64", outs)
-    barrier()
-    fp64_s = time.perf_counter() - t0
+
+    def timed(precision, steps):
+        """CUDA-event time per step of `steps` batched applies (after one untimed step)."""
+        step(precision, outs)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        e0.record()
+        for _ in range(steps):
+            st_ = step(precision, outs)
+        e1.record()
+        barrier()
+        return e0.elapsed_time(e1) / steps, st_
+
+    # plain FP64 GPU apply of the same batch: the baseline of the metric and the error reference
+    fp64_ms, st64 = timed("fp64", args.fp64_steps)
+    fp64_s = fp64_ms / 1e3
     ref = [o.download()[1] for o in outs]
+    near_ms, st_near = timed("mixed-near64", 1)
+    near_err = max(float(np.linalg.norm(o.download()[1] - r) / np.linalg.norm(r)) for o, r in zip(outs, ref))
 
     for _ in range(args.warmup):
         step("mixed", outs)
@@ -237,15 +250,18 @@ def run(args):
     e2e_v = nodes * world / e2e_s
 
     st = stats[-1]
-    kern_s = st["kernel_ms"] / 1e3
-    peaks = measured_peaks()
-    fp64_tf = args.fp64_peak_tflops
-    achieved = st["flops"] / kern_s / 1e12 if kern_s > 0 else 0.0
-    roofline = {"bound": "fp64-pipe", "achieved": achieved, "peak": fp64_tf, "unit": "TFLOP/s",
-                "frac": achieved / fp64_tf if fp64_tf else None, "traffic": None,
-                "kernel": "apply_kernel (FP64 + FP32 tiers)",
-                "note": "algorithmic 6K^4 flops per surviving component pair over the CUDA-event time of the "
-                        "contraction launches; FP64 peak probed on this GPU"}
+    fp64_tf = mra.probe_fma_peak(True)
+    fp32_tf = mra.probe_fma_peak(False)
+
+    def roof(flops, ms, peak, kernel):
+        ach = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
+        return {"bound": "fp64-pipe" if "double" in kernel else "fp32-pipe", "achieved": ach, "peak": peak,
+                "unit": "TFLOP/s", "frac": ach / peak if peak else None, "traffic": None, "kernel": kernel,
+                "peak_source": "probed FMA throughput of this GPU (mw_probe_fma_peak); MEASURED_PEAKS.json "
+                               "holds no FP64/FP32 figure"}
+
+    roofline = roof(st["flops_fp64"], st["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>")
+    roofline_fp32 = roof(st["flops_fp32"], st["kernel_ms_fp32"], fp32_tf, "apply_kernel<float,10>")
     line = {
         "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -255,15 +271,19 @@ def run(args):
                    "output_nodes": nodes, "l2": "inputs larger than L2 (%.1f GB of FP64 blocks)"
                    % (sum(in_nodes) * 8 * (ORDER + 1) ** 3 * 8 / 1e9),
                    "operator_terms": [o.nterms for o in ops], "operator_build_s": op_build_s},
-        "fp64": {"value": st64["out_nodes"] * world / fp64_s, "unit": "nodes/s", "seconds": fp64_s,
-                 "items": st64["items"]},
-        "speedup_mixed_vs_fp64": (st64["out_nodes"] / fp64_s) / (nodes / (ms / 1e3)),
+        "fp64": {"value": st64["out_nodes"] * world / fp64_s, "unit": "nodes/s", "ms_per_step": fp64_ms,
+                 "items": st64["items"], "kernel_ms_per_step": st64["kernel_ms"]},
+        "mixed_near_fp64": {"value": st_near["out_nodes"] * world / (near_ms / 1e3), "unit": "nodes/s",
+                            "ms_per_step": near_ms, "items_fp64": st_near["items_fp64"],
+                            "items_fp32": st_near["items_fp32"], "rel_l2_vs_fp64_max": near_err,
+                            "policy": "every |l|_inf <= 1 item kept in FP64"},
         "rel_l2_vs_fp64_max": max(errs),
         "items": {"total": st["items"], "fp64": st["items_fp64"], "fp32": st["items_fp32"]},
         "kernel_ms_per_step": st["kernel_ms"], "host_ms_per_step": st["host_ms"],
         "gpu_launches": int(st["launches"]),
         "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": roofline,
+        "roofline_fp32": roofline_fp32,
         "clocks": clk.summary(),
     }
     line["speedup_mixed_vs_fp64"] = (nodes / (ms / 1e3)) / (st64["out_nodes"] / fp64_s)
@@ -282,10 +302,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--cpu-levels", type=int, default=4)
+    ap.add_argument("--cpu-levels", type=int, default=-1)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--fp64-peak-tflops", type=float, default=1.25)
+    ap.add_argument("--orbitals", type=int, default=16)
+    ap.add_argument("--fp64-steps", type=int, default=1)
     args = ap.parse_args()
+    global NORB
+    NORB = args.orbitals
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -38,7 +38,8 @@ extern "C" {
 
 /* precision modes of mw_apply / mw_apply_batch */
 #define MW_PREC_FP64 0   /* every contraction in FP64 */
-#define MW_PREC_MIXED 1  /* norm-tiered FP64 / FP32 / BF16 tensor-core contractions */
+#define MW_PREC_MIXED 1  /* norm-tiered: FP64 when the item's bound b > 1e5 x screening threshold, else FP32 */
+#define MW_PREC_MIXED_NEARFP64 2  /* as MW_PREC_MIXED, and every item with |l|_inf <= 1 in FP64 */
 
 typedef struct mw_ctx_s *mw_ctx;
 typedef struct mw_tree_s *mw_tree;
@@ -67,6 +68,10 @@ typedef struct {
     double bytes;            /* algorithmic coefficient + operator bytes */
     double kernel_ms;        /* CUDA-event time of the contraction kernels */
     double host_ms;          /* wall time of the call */
+    double flops_fp64;       /* algorithmic flops of the FP64 tier */
+    double flops_fp32;       /* ... of the FP32 tier */
+    double kernel_ms_fp64;   /* CUDA-event time of the FP64 contraction launches */
+    double kernel_ms_fp32;   /* ... of the FP32 contraction launches */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */
@@ -139,6 +144,11 @@ int mw_multiply(double prec, mw_tree out, double coef, mw_tree a, mw_tree b, int
 int mw_square(double prec, mw_tree out, mw_tree inp, int max_iter, int abs_prec);
 /* mrcpp::add(prec, out, FunctionTreeVector, maxIter) on the union grid (density_utils.cpp:85-86) */
 int mw_add(double prec, mw_tree out, int n, const double *coefs, const mw_tree *trees, int max_iter);
+
+/* ---- diagnostics ---- */
+/* measured FMA throughput of this GPU (TFLOP/s) in FP64 (fp64 = 1) or FP32 (fp64 = 0):
+ * the denominator of the CUDA-core roofline of the contraction kernels */
+int mw_probe_fma_peak(mw_ctx ctx, int fp64, double *tflops);
 
 #ifdef __cplusplus
 }

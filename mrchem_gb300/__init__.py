@@ -28,7 +28,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libmwgb300.so")
 MW_OK = 0
 PREC_FP64 = 0
 PREC_MIXED = 1
-_PREC = {"fp64": PREC_FP64, "mixed": PREC_MIXED}
+PREC_MIXED_NEARFP64 = 2
+_PREC = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "mixed-near64": PREC_MIXED_NEARFP64}
 
 
 class MWError(RuntimeError):
@@ -49,7 +50,8 @@ class Stats(C.Structure):
                 ("items_fp32", C.c_longlong), ("items_bf16", C.c_longlong), ("generated", C.c_longlong),
                 ("levels", C.c_longlong), ("launches", C.c_longlong), ("flops", C.c_double),
                 ("flops_issued", C.c_double), ("bytes", C.c_double), ("kernel_ms", C.c_double),
-                ("host_ms", C.c_double)]
+                ("host_ms", C.c_double), ("flops_fp64", C.c_double), ("flops_fp32", C.c_double),
+                ("kernel_ms_fp64", C.c_double), ("kernel_ms_fp32", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -64,7 +66,7 @@ EXPORTS = [
     "mw_tree_clear", "mw_project_gauss", "mw_project_hydrogen", "mw_copy_grid", "mw_build_grid", "mw_copy_func",
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
-    "mw_multiply", "mw_square", "mw_add",
+    "mw_multiply", "mw_square", "mw_add", "mw_probe_fma_peak",
 ]
 
 
@@ -118,6 +120,7 @@ def load_library(path=None):
         "mw_multiply": [D, P, D, P, P, I, I, I],
         "mw_square": [D, P, P, I, I],
         "mw_add": [D, P, I, dp, pp, I],
+        "mw_probe_fma_peak": [P, I, dp],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -192,6 +195,12 @@ class MultiResolutionAnalysis:
 
     def synchronize(self):
         _check(_lib.mw_ctx_synchronize(self.ptr), self.ptr)
+
+    def probe_fma_peak(self, fp64=True):
+        """Measured FMA throughput of this GPU in TFLOP/s (FP64 or FP32 CUDA cores)."""
+        v = C.c_double()
+        _check(_lib.mw_probe_fma_peak(self.ptr, int(fp64), C.byref(v)), self.ptr)
+        return v.value
 
 
 class FunctionTree:

@@ -15,7 +15,8 @@
 //   - o is split when |wavelet part| * w(o) > thr(o) = prec R 2^{-(n+1)/2};
 //   - afterwards the scales are summed top-down and the tree is compressed.
 // The contractions run on the GPU in deterministic per-node order; with
-// MW_PREC_MIXED the items are split into FP64 / FP32 tiers by their bound b.
+// MW_PREC_MIXED the items are split into FP64 / FP32 tiers by their bound b
+// (MW_PREC_MIXED_NEARFP64 also keeps every |l|_inf <= 1 item in FP64).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -88,8 +89,9 @@ double prec_weight(const std::vector<Tree *> &pt, int n, const int *l) {
 
 struct Cand {
     int t, lx, ly, lz;
-    int src;  // input node index, or generated slot
-    int gen;  // 1: src is a generated slot (ancestor index before generation)
+    int src;   // input node index, or generated slot
+    int gen;   // 1: src is a generated slot (ancestor index before generation)
+    int tier;  // after screening: -1 skipped, 0 FP64, 1 FP32
 };
 
 struct JobState {
@@ -174,7 +176,7 @@ void enumerate_node(JobState &js, int w, int s, bool root, double thr, LookupCac
                     }
                     double bd = item_bound(nx, ny, nz, cn, root);
                     if (!root && bd < thr) continue;
-                    out.push_back(Cand{t, lx, ly, lz, ce >= 0 ? ce : -(ce + 4), ce >= 0 ? 0 : 1});
+                    out.push_back(Cand{t, lx, ly, lz, ce >= 0 ? ce : -(ce + 4), ce >= 0 ? 0 : 1, -1});
                 }
             }
         }
@@ -187,14 +189,14 @@ struct LevelItems {
     std::vector<long long> begin;
     std::vector<const void *> in, ax, ay, az;
     std::vector<double> coef;
-    void clear() {
-        out.clear();
-        begin.assign(1, 0);
-        in.clear();
-        ax.clear();
-        ay.clear();
-        az.clear();
-        coef.clear();
+    void resize(long nodes, long long items) {
+        out.assign(nodes, nullptr);
+        begin.assign(nodes + 1, 0);
+        in.assign(items, nullptr);
+        ax.assign(items, nullptr);
+        ay.assign(items, nullptr);
+        az.assign(items, nullptr);
+        coef.assign(items, 0.0);
     }
 };
 
@@ -235,12 +237,14 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     const Basis &b = ctx.basis;
     const int K = b.K, bs = b.bs, bsz = 4 * K * K;
     const double K4 = (double)K * K * K * K;
-    const bool mixed = precision_mode == MW_PREC_MIXED;
+    const bool mixed = precision_mode != MW_PREC_FP64;
+    const bool near_fp64 = precision_mode == MW_PREC_MIXED_NEARFP64;
     auto t_start = std::chrono::steady_clock::now();
     Arena &arena = ctx.arena;
     arena.reset();
-    cudaEvent_t ev0, ev1;
+    cudaEvent_t ev0, evm, ev1;
     MWG_CUDA(cudaEventCreate(&ev0));
+    MWG_CUDA(cudaEventCreate(&evm));
     MWG_CUDA(cudaEventCreate(&ev1));
     float kernel_ms = 0.0f;
 
@@ -336,52 +340,91 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 st.launches++;
             }
         }
-        // phase C: exact screening, tiers, item lists in node order
-        li64.clear();
-        li32.clear();
-        long long pairs_tot = 0, n64 = 0, n32 = 0;
-        for (auto &s : js) {
+        // phase C: exact screening and tier per candidate (parallel), then the
+        // per-tier item lists in node order (prefix sums + parallel fill)
+        std::vector<std::pair<int, int>> nodes_flat;  // (job, work index) in launch order
+        for (size_t j = 0; j < js.size(); j++)
+            for (size_t w = 0; w < js[j].work.size(); w++) nodes_flat.push_back({(int)j, (int)w});
+        const long NN = (long)nodes_flat.size();
+        std::vector<long long> cnt64(NN + 1, 0), cnt32(NN + 1, 0);
+        long long pairs_tot = 0, pairs64 = 0, pairs32 = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : pairs_tot, pairs64, pairs32)
+        for (long q = 0; q < NN; q++) {
+            JobState &s = js[nodes_flat[q].first];
+            int w = nodes_flat[q].second;
             const Tree &inp = *s.job->inp;
             const Oper &op = *s.job->op;
-            for (size_t w = 0; w < s.work.size(); w++) {
-                int oi = s.work[w];
-                double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / std::max(s.wgt[w], 1e-300);
-                double *ob = s.job->out->block(oi);
-                li64.out.push_back(ob);
-                size_t n32_before = li32.in.size();
-                for (const Cand &c : s.cand[w]) {
-                    const double *cn = c.gen ? &s.gcn[8 * (size_t)c.src] : &inp.cn[8 * (size_t)c.src];
-                    const double *nx = op.norm(c.t, sidx, c.lx), *ny = op.norm(c.t, sidx, c.ly),
-                                 *nz = op.norm(c.t, sidx, c.lz);
-                    double bd = item_bound(nx, ny, nz, cn, root);
-                    if (!root && bd < thr) continue;
-                    pairs_tot += item_pairs(nx, ny, nz, cn, root);
-                    long bxi = op.block_index(c.t, sidx, c.lx), byi = op.block_index(c.t, sidx, c.ly),
-                         bzi = op.block_index(c.t, sidx, c.lz);
-                    bool near = std::max(std::abs(c.lx), std::max(std::abs(c.ly), std::abs(c.lz))) <= 1;
-                    bool use64 = !mixed || root || near || bd > TIER_FP64 * thr;
-                    if (use64) {
-                        li64.in.push_back(c.gen ? (const void *)(s.gbase + (size_t)c.src * bs)
-                                                : (const void *)inp.block(c.src));
-                        li64.ax.push_back(op.d_blocks + (size_t)bxi * bsz);
-                        li64.ay.push_back(op.d_blocks + (size_t)byi * bsz);
-                        li64.az.push_back(op.d_blocks + (size_t)bzi * bsz);
-                        li64.coef.push_back(op.c[c.t]);
-                        n64++;
-                    } else {
-                        li32.in.push_back(c.gen ? (const void *)(s.gbase32 + (size_t)c.src * bs)
-                                                : (const void *)(inp.d_coefs32 + (size_t)c.src * bs));
-                        li32.ax.push_back(op.d_blocks32 + (size_t)bxi * bsz);
-                        li32.ay.push_back(op.d_blocks32 + (size_t)byi * bsz);
-                        li32.az.push_back(op.d_blocks32 + (size_t)bzi * bsz);
-                        li32.coef.push_back(op.c[c.t]);
-                        n32++;
-                    }
+            double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / std::max(s.wgt[w], 1e-300);
+            long long c64 = 0, c32 = 0;
+            for (Cand &c : s.cand[w]) {
+                const double *cn = c.gen ? &s.gcn[8 * (size_t)c.src] : &inp.cn[8 * (size_t)c.src];
+                const double *nx = op.norm(c.t, sidx, c.lx), *ny = op.norm(c.t, sidx, c.ly),
+                             *nz = op.norm(c.t, sidx, c.lz);
+                double bd = item_bound(nx, ny, nz, cn, root);
+                if (!root && bd < thr) {
+                    c.tier = -1;
+                    continue;
                 }
-                li64.begin.push_back((long long)li64.in.size());
-                if (li32.in.size() > n32_before) {
-                    li32.out.push_back(ob);
-                    li32.begin.push_back((long long)li32.in.size());
+                int np_ = item_pairs(nx, ny, nz, cn, root);
+                pairs_tot += np_;
+                bool near = std::max(std::abs(c.lx), std::max(std::abs(c.ly), std::abs(c.lz))) <= 1;
+                bool use64 = !mixed || root || bd > TIER_FP64 * thr || (near_fp64 && near);
+                c.tier = use64 ? 0 : 1;
+                if (use64) {
+                    c64++;
+                    pairs64 += np_;
+                } else {
+                    c32++;
+                    pairs32 += np_;
+                }
+            }
+            cnt64[q + 1] = c64;
+            cnt32[q + 1] = c32;
+        }
+        std::vector<long> slot32(NN, -1);  // node position in the FP32 launch
+        long nn32 = 0;
+        for (long q = 0; q < NN; q++) {
+            if (cnt32[q + 1] > 0) slot32[q] = nn32++;
+            cnt64[q + 1] += cnt64[q];
+            cnt32[q + 1] += cnt32[q];
+        }
+        const long long n64 = cnt64[NN], n32 = cnt32[NN];
+        li64.resize(NN, n64);
+        li32.resize(nn32, n32);
+        li32.begin[0] = 0;
+#pragma omp parallel for schedule(dynamic, 4)
+        for (long q = 0; q < NN; q++) {
+            JobState &s = js[nodes_flat[q].first];
+            int w = nodes_flat[q].second;
+            const Tree &inp = *s.job->inp;
+            const Oper &op = *s.job->op;
+            double *ob = s.job->out->block(s.work[w]);
+            li64.out[q] = ob;
+            li64.begin[q + 1] = cnt64[q + 1];
+            if (slot32[q] >= 0) {
+                li32.out[slot32[q]] = ob;
+                li32.begin[slot32[q] + 1] = cnt32[q + 1];
+            }
+            long long p64 = cnt64[q], p32 = cnt32[q];
+            for (const Cand &c : s.cand[w]) {
+                if (c.tier < 0) continue;
+                long bxi = op.block_index(c.t, sidx, c.lx), byi = op.block_index(c.t, sidx, c.ly),
+                     bzi = op.block_index(c.t, sidx, c.lz);
+                if (c.tier == 0) {
+                    li64.in[p64] = c.gen ? (const void *)(s.gbase + (size_t)c.src * bs) : (const void *)inp.block(c.src);
+                    li64.ax[p64] = op.d_blocks + (size_t)bxi * bsz;
+                    li64.ay[p64] = op.d_blocks + (size_t)byi * bsz;
+                    li64.az[p64] = op.d_blocks + (size_t)bzi * bsz;
+                    li64.coef[p64] = op.c[c.t];
+                    p64++;
+                } else {
+                    li32.in[p32] = c.gen ? (const void *)(s.gbase32 + (size_t)c.src * bs)
+                                         : (const void *)(inp.d_coefs32 + (size_t)c.src * bs);
+                    li32.ax[p32] = op.d_blocks32 + (size_t)bxi * bsz;
+                    li32.ay[p32] = op.d_blocks32 + (size_t)byi * bsz;
+                    li32.az[p32] = op.d_blocks32 + (size_t)bzi * bsz;
+                    li32.coef[p32] = op.c[c.t];
+                    p32++;
                 }
             }
         }
@@ -390,9 +433,11 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         st.items_fp32 += n32;
         st.flops += 6.0 * K4 * (double)pairs_tot;
         st.flops_issued += 96.0 * K4 * (double)(n64 + n32);
-        st.bytes += 8.0 * bs * (double)(n64 + n32) * 0.0;  // coefficient bytes are counted per node below
+        st.flops_fp64 += 6.0 * K4 * (double)pairs64;
+        st.flops_fp32 += 6.0 * K4 * (double)pairs32;
         MWG_CUDA(cudaEventRecord(ev0, ctx.stream));
         launch_tier(ctx, li64, root, true, 0, st);
+        MWG_CUDA(cudaEventRecord(evm, ctx.stream));
         launch_tier(ctx, li32, root, false, 1, st);
         MWG_CUDA(cudaEventRecord(ev1, ctx.stream));
         // norms of the level's output nodes
@@ -416,9 +461,12 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                                      ctx.stream));
         }
         ctx.sync();
-        float ms = 0.0f;
+        float ms = 0.0f, ms64 = 0.0f;
         MWG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        MWG_CUDA(cudaEventElapsedTime(&ms64, ev0, evm));
         kernel_ms += ms;
+        st.kernel_ms_fp64 += ms64;
+        st.kernel_ms_fp32 += ms - ms64;
         // refinement
         for (auto &s : js) {
             Tree &out = *s.job->out;
@@ -514,6 +562,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     ctx.sync();
     arena.reset();
     cudaEventDestroy(ev0);
+    cudaEventDestroy(evm);
     cudaEventDestroy(ev1);
     st.kernel_ms += kernel_ms;
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();

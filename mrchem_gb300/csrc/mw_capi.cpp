@@ -362,7 +362,7 @@ int mw_op_block(mw_op o, int term, int scale, int l, double *blk, double *norms4
 int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const mw_tree *prec_trees, int max_iter,
              int abs_prec, int precision_mode) {
     if (!out || !op || !inp || !(prec > 0.0) || nprec < 0 || (nprec > 0 && !prec_trees)) return MW_ERR_ARG;
-    if (precision_mode != MW_PREC_FP64 && precision_mode != MW_PREC_MIXED) return MW_ERR_ARG;
+    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_MIXED_NEARFP64) return MW_ERR_ARG;
     if (out == inp) return MW_ERR_ARG;
     mwg::Ctx *ctx = ctx_of(out);
     return guard(ctx, [&] {
@@ -381,7 +381,7 @@ int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const m
 int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, int max_iter, int abs_prec,
                    int precision_mode) {
     if (n < 1 || !precs || !outs || !ops || !inps) return MW_ERR_ARG;
-    if (precision_mode != MW_PREC_FP64 && precision_mode != MW_PREC_MIXED) return MW_ERR_ARG;
+    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_MIXED_NEARFP64) return MW_ERR_ARG;
     for (int i = 0; i < n; i++)
         if (!outs[i] || !ops[i] || !inps[i] || !(precs[i] > 0.0) || outs[i] == inps[i]) return MW_ERR_ARG;
     mwg::Ctx *ctx = ctx_of(outs[0]);
@@ -397,7 +397,7 @@ int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tre
 
 int mw_apply_fixed(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec, int precision_mode) {
     if (!out || !op || !inp || !(prec > 0.0) || out == inp) return MW_ERR_ARG;
-    if (precision_mode != MW_PREC_FP64 && precision_mode != MW_PREC_MIXED) return MW_ERR_ARG;
+    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_MIXED_NEARFP64) return MW_ERR_ARG;
     mwg::Ctx *ctx = ctx_of(out);
     return guard(ctx, [&] {
         std::vector<mwg::ApplyJob> jobs(1);
@@ -452,6 +452,11 @@ int mw_add(double prec, mw_tree out, int n, const double *coefs, const mw_tree *
         mwg::add(out->tree, v, c, st);
         ctx->last = st;
     });
+}
+
+int mw_probe_fma_peak(mw_ctx c, int fp64, double *tflops) {
+    if (!c || !tflops) return MW_ERR_ARG;
+    return guard(&c->ctx, [&] { *tflops = mwg::probe_fma_tflops(fp64, c->ctx.nsm, c->ctx.stream); });
 }
 
 }  // extern "C"

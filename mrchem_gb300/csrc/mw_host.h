@@ -244,6 +244,7 @@ void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);
 void k_dot(const double *const *a, const double *const *b, const int *start, int n, int bs, double *partial,
            cudaStream_t s);
 void k_scale(double *x, size_t n, double c, cudaStream_t s);
+double probe_fma_tflops(int fp64, int nsm, cudaStream_t s);
 void k_eval(const DevBasis &b, const double *const *blocks, const int *keys, const double *pts, int npts,
             double *out, cudaStream_t s);
 

@@ -640,3 +640,49 @@ void k_eval(const DevBasis &b, const double *const *blocks, const int *keys, con
 }
 
 }  // namespace mwg
+
+// ------------------------------------------------------------------ peak probe
+namespace mwg {
+namespace {
+template <typename T>
+__global__ void fma_probe_kernel(T *out, int iters, T seed) {
+    T a0 = seed + threadIdx.x, a1 = a0 + T(1), a2 = a0 + T(2), a3 = a0 + T(3);
+    T a4 = a0 + T(4), a5 = a0 + T(5), a6 = a0 + T(6), a7 = a0 + T(7);
+    const T m = T(0.999999), c = T(1e-7);
+    for (int i = 0; i < iters; i++) {
+        a0 = a0 * m + c; a1 = a1 * m + c; a2 = a2 * m + c; a3 = a3 * m + c;
+        a4 = a4 * m + c; a5 = a5 * m + c; a6 = a6 * m + c; a7 = a7 * m + c;
+    }
+    T s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == T(-12345)) out[blockIdx.x] = s;  // never true; keeps the chain live
+}
+}  // namespace
+
+double probe_fma_tflops(int fp64, int nsm, cudaStream_t s) {
+    const int threads = 256, blocks = nsm * 8, iters = fp64 ? 1 << 13 : 1 << 16;
+    void *out = nullptr;
+    MWG_CUDA(cudaMalloc(&out, sizeof(double) * blocks));
+    cudaEvent_t e0, e1;
+    MWG_CUDA(cudaEventCreate(&e0));
+    MWG_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        MWG_CUDA(cudaEventRecord(e0, s));
+        if (fp64)
+            fma_probe_kernel<double><<<blocks, threads, 0, s>>>((double *)out, iters, 1.0);
+        else
+            fma_probe_kernel<float><<<blocks, threads, 0, s>>>((float *)out, iters, 1.0f);
+        MWG_CUDA(cudaGetLastError());
+        MWG_CUDA(cudaEventRecord(e1, s));
+        MWG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        MWG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+    return flops / (best * 1e-3) / 1e12;
+}
+}  // namespace mwg

@@ -280,6 +280,18 @@ int orc_apply(double prec, orc_tree *out, const orc_oper *op, orc_tree *inp, int
                     const double *nz = op_norm(op, it->t, s, it->l[2]);
                     if (it->gen && !root && orc_item_bound(nx, ny, nz, cn, root) < thr) continue;
                     items++;
+                    if (!root) {
+                        double r = orc_item_bound(nx, ny, nz, cn, root) / thr;
+                        int bin = r >= 1.0 ? (int)floor(log10(r)) : 0;
+                        if (bin > 15) bin = 15;
+                        int near = abs(it->l[0]) <= 1 && abs(it->l[1]) <= 1 && abs(it->l[2]) <= 1;
+#pragma omp atomic
+                        st.bound_hist[bin]++;
+                        if (near) {
+#pragma omp atomic
+                            st.bound_hist[16 + bin]++;
+                        }
+                    }
                     const double *bx = op_block(op, it->t, s, it->l[0]);
                     const double *by = op_block(op, it->t, s, it->l[1]);
                     const double *bz = op_block(op, it->t, s, it->l[2]);

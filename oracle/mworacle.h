@@ -56,6 +56,9 @@ typedef struct {
     long long generated;      /* generated input nodes */
     double flops;             /* 6K^4 per surviving component pair */
     double seconds;
+    /* surviving items by floor(log10(bound / screening threshold)), 0..15;
+     * [0..15] all items, [16..31] items with |l|_inf <= 1 */
+    long long bound_hist[32];
 } orc_stats;
 
 /* ---- MRA ---- */

@@ -29,7 +29,8 @@ class GTerm(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("out_nodes", C.c_longlong), ("items", C.c_longlong), ("pairs", C.c_longlong),
-                ("generated", C.c_longlong), ("flops", C.c_double), ("seconds", C.c_double)]
+                ("generated", C.c_longlong), ("flops", C.c_double), ("seconds", C.c_double),
+                ("bound_hist", C.c_longlong * 32)]
 
 
 def lib():
@@ -284,7 +285,7 @@ def apply(prec, out, op, inp, max_iter=-1, abs_prec=False, prec_trees=()):
     if rc != 0:
         raise RuntimeError("apply failed")
     return dict(out_nodes=st.out_nodes, items=st.items, pairs=st.pairs, generated=st.generated, flops=st.flops,
-                seconds=st.seconds)
+                seconds=st.seconds, bound_hist=list(st.bound_hist))
 
 
 def multiply(prec, out, coef, a, b, max_iter=-1, abs_prec=False, use_max_norms=False):
