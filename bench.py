@@ -196,6 +196,13 @@ def run(args):
         barrier()
         return e0.elapsed_time(e1) / steps, st_
 
+    if args.profile_mixed:
+        # profiling mode: only the W + K mixed steps run (for a launch list of the headline step)
+        for _ in range(args.warmup + args.steps):
+            st_p = step("mixed", outs)
+        barrier()
+        print(json.dumps({"profile_mixed": True, "steps": args.warmup + args.steps, "stats": st_p}))
+        return
     # plain FP64 GPU apply of the same batch: the baseline of the metric and the error reference
     fp64_ms, st64 = timed("fp64", args.fp64_steps)
     fp64_s = fp64_ms / 1e3
@@ -306,6 +313,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--orbitals", type=int, default=16)
     ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--profile-mixed", action="store_true")
     args = ap.parse_args()
     global NORB
     NORB = args.orbitals

@@ -128,18 +128,27 @@ int mw_op_block(mw_op op, int term, int scale, int l, double *blk, double *norms
 int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const mw_tree *prec_trees, int max_iter,
              int abs_prec, int precision_mode);
 /* n independent applies (own operator, input, output, prec) in lockstep, one launch per level
- * (HelmholtzVector::operator(), src/scf_solver/HelmholtzVector.cpp:70-91) */
-int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, int max_iter, int abs_prec,
-                   int precision_mode);
+ * (HelmholtzVector::operator(), src/scf_solver/HelmholtzVector.cpp:70-91; the exchange pair loop,
+ * src/qmoperators/two_electron/ExchangePotentialD1.cpp:179-240).  nprec[i] precision-steering trees
+ * of job i are consecutive in prec_trees (nprec may be NULL). */
+int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *nprec,
+                   const mw_tree *prec_trees, int max_iter, int abs_prec, int precision_mode);
 /* apply on a fixed output grid (the output's current grid, no refinement) */
 int mw_apply_fixed(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec, int precision_mode);
-/* transpose apply: out = O^T inp on the fixed grid of out (adjoint of mw_apply_fixed) */
-int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec);
+/* L2-adjoint of the fixed-grid FP64 apply y = A x (output grid = seed's grid, absolute precision):
+ * out <- A^T seed on x's grid, with the forward's item set (screened with x's norms).  Transposed
+ * operator blocks, contraction grouped by input node (gather), then the forward's post-processing.
+ * No MRCPP counterpart: it serves the gradient of J = 1/2 <rho, P rho> (pattern 3 of the plan). */
+int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree x, mw_tree seed, int abs_prec);
 
 /* mrcpp::multiply(prec, out, coef, a, b, maxIter, absPrec, useMaxNorms)
  * (QMPotential.cpp:147; ExchangePotential.cpp:175,213,223); out's current grid is the start grid */
 int mw_multiply(double prec, mw_tree out, double coef, mw_tree a, mw_tree b, int max_iter, int abs_prec,
                 int use_max_norms);
+/* n independent products out_i = coef_i a_i b_i, level-synchronous (exchange pair products,
+ * src/qmoperators/two_electron/ExchangePotential.cpp:175) */
+int mw_multiply_batch(int n, const double *precs, mw_tree *outs, const double *coefs, mw_tree *as, mw_tree *bs,
+                      int max_iter, int abs_prec, int use_max_norms);
 /* mrcpp::square(prec, out, inp) (src/qmfunctions/density_utils.cpp:73) */
 int mw_square(double prec, mw_tree out, mw_tree inp, int max_iter, int abs_prec);
 /* mrcpp::add(prec, out, FunctionTreeVector, maxIter) on the union grid (density_utils.cpp:85-86) */

@@ -66,7 +66,7 @@ EXPORTS = [
     "mw_tree_clear", "mw_project_gauss", "mw_project_hydrogen", "mw_copy_grid", "mw_build_grid", "mw_copy_func",
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
-    "mw_multiply", "mw_square", "mw_add", "mw_probe_fma_peak",
+    "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak",
 ]
 
 
@@ -114,9 +114,10 @@ def load_library(path=None):
         "mw_op_band": [P, I, I, ip],
         "mw_op_block": [P, I, I, I, dp, dp],
         "mw_apply": [D, P, P, P, I, pp, I, I, I],
-        "mw_apply_batch": [I, dp, pp, pp, pp, I, I, I],
+        "mw_apply_batch": [I, dp, pp, pp, pp, ip, pp, I, I, I],
+        "mw_multiply_batch": [I, dp, pp, dp, pp, pp, I, I, I],
         "mw_apply_fixed": [D, P, P, P, I, I],
-        "mw_apply_adjoint": [D, P, P, P, I],
+        "mw_apply_adjoint": [D, P, P, P, P, I],
         "mw_multiply": [D, P, D, P, P, I, I, I],
         "mw_square": [D, P, P, I, I],
         "mw_add": [D, P, I, dp, pp, I],
@@ -382,18 +383,43 @@ def apply(prec, out, oper, inp, prec_trees=(), max_iter=-1, abs_prec=False, prec
     return out.mra.last_stats()
 
 
-def apply_batch(precs, outs, opers, inps, max_iter=-1, abs_prec=False, precision="fp64"):
-    """Independent applies (own operator, input, output) run level-synchronously in shared launches."""
+def apply_batch(precs, outs, opers, inps, prec_trees=None, max_iter=-1, abs_prec=False, precision="fp64"):
+    """Independent applies (own operator, input, output) run level-synchronously in shared launches.
+
+    prec_trees: optional list (one entry per job) of lists of precision-steering trees.
+    """
     n = len(outs)
     p = np.ascontiguousarray(precs if np.ndim(precs) else [precs] * n, dtype=np.float64)
-    _check(_lib.mw_apply_batch(n, _dp(p), _ptrs(outs), _ptrs(opers), _ptrs(inps), max_iter, int(abs_prec),
+    if prec_trees is None:
+        npr, flat = None, []
+    else:
+        npr = np.ascontiguousarray([len(pt) for pt in prec_trees], dtype=np.int32)
+        flat = [t for pt in prec_trees for t in pt]
+    _check(_lib.mw_apply_batch(n, _dp(p), _ptrs(outs), _ptrs(opers), _ptrs(inps),
+                               _ip(npr) if npr is not None else None, _ptrs(flat), max_iter, int(abs_prec),
                                _PREC[precision]), outs[0].mra.ptr)
+    return outs[0].mra.last_stats()
+
+
+def multiply_batch(precs, outs, coefs, as_, bs_, max_iter=-1, abs_prec=False, use_max_norms=False):
+    """Independent products out_i = coef_i a_i b_i, refined level-synchronously in shared launches."""
+    n = len(outs)
+    p = np.ascontiguousarray(precs if np.ndim(precs) else [precs] * n, dtype=np.float64)
+    c = np.ascontiguousarray(coefs if np.ndim(coefs) else [coefs] * n, dtype=np.float64)
+    _check(_lib.mw_multiply_batch(n, _dp(p), _ptrs(outs), _dp(c), _ptrs(as_), _ptrs(bs_), max_iter, int(abs_prec),
+                                  int(use_max_norms)), outs[0].mra.ptr)
     return outs[0].mra.last_stats()
 
 
 def apply_fixed(prec, out, oper, inp, abs_prec=False, precision="fp64"):
     """apply on out's current grid (no refinement)."""
     _check(_lib.mw_apply_fixed(prec, out.ptr, oper.ptr, inp.ptr, int(abs_prec), _PREC[precision]), out.mra.ptr)
+    return out.mra.last_stats()
+
+
+def apply_adjoint(prec, out, oper, x, seed):
+    """L2-adjoint of the fixed-grid FP64 apply on seed's grid (absolute precision): out <- A^T seed on x's grid."""
+    _check(_lib.mw_apply_adjoint(prec, out.ptr, oper.ptr, x.ptr, seed.ptr, 1), out.mra.ptr)
     return out.mra.last_stats()
 
 

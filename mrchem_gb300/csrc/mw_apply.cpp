@@ -28,7 +28,11 @@ namespace mwg {
 
 namespace {
 
-constexpr double TIER_FP64 = 1e5;  // b above TIER_FP64 * screening threshold -> FP64
+// An item computed in FP32 (inputs, operator blocks and three passes of 2K-term sums rounded to
+// FP32) is off by at most about (4 + 6K) 2^-24 b <= 4e-6 b for K <= 10.  Items with
+// b <= TIER_FP64 * screening threshold = 2e4 * thr(o) therefore err by at most 0.08 thr(o),
+// a tenth of the refinement tolerance; larger items run in FP64.
+constexpr double TIER_FP64 = 2e6;
 constexpr double BOUND_PRUNE = 8.0 * 2.8285;  // (sum_f |in_f|) / |block| <= sqrt(8); 8 output components
 
 double split_thr(double prec, double R, int n) { return prec * R * std::pow(2.0, -0.5 * (n + 1)); }
@@ -203,9 +207,24 @@ struct LevelItems {
 void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int fp32, mw_stats &st) {
     int nn = (int)li.out.size();
     if (nn == 0) return;
+    // nodes in decreasing item count (longest first) for the persistent grid's dynamic
+    // scheduler; each node's own items keep their order, so results do not change
+    std::vector<int> ord(nn);
+    for (int i = 0; i < nn; i++) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+        return li.begin[a + 1] - li.begin[a] > li.begin[b + 1] - li.begin[b];
+    });
+    std::vector<double *> outp(nn);
+    std::vector<long long> beg(nn), end(nn);
+    for (int i = 0; i < nn; i++) {
+        outp[i] = li.out[ord[i]];
+        beg[i] = li.begin[ord[i]];
+        end[i] = li.begin[ord[i] + 1];
+    }
     Packer pk;
-    pk.add(li.out.data(), li.out.size() * sizeof(double *));
-    pk.add(li.begin.data(), li.begin.size() * sizeof(long long));
+    pk.add(outp.data(), outp.size() * sizeof(double *));
+    pk.add(beg.data(), beg.size() * sizeof(long long));
+    pk.add(end.data(), end.size() * sizeof(long long));
     pk.add(li.in.data(), li.in.size() * sizeof(void *));
     pk.add(li.ax.data(), li.ax.size() * sizeof(void *));
     pk.add(li.ay.data(), li.ay.size() * sizeof(void *));
@@ -219,11 +238,12 @@ void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int fp32, mw_sta
     L.set = set ? 1 : 0;
     L.out = (double *const *)pk.ptr(0);
     L.begin = (const long long *)pk.ptr(1);
-    L.in = (const void *const *)pk.ptr(2);
-    L.ax = (const void *const *)pk.ptr(3);
-    L.ay = (const void *const *)pk.ptr(4);
-    L.az = (const void *const *)pk.ptr(5);
-    L.coef = (const double *)pk.ptr(6);
+    L.end = (const long long *)pk.ptr(2);
+    L.in = (const void *const *)pk.ptr(3);
+    L.ax = (const void *const *)pk.ptr(4);
+    L.ay = (const void *const *)pk.ptr(5);
+    L.az = (const void *const *)pk.ptr(6);
+    L.coef = (const double *)pk.ptr(7);
     L.counter = counter;
     k_apply(ctx.dbasis, L, fp32, ctx.nsm, ctx.stream);
     st.launches++;
@@ -332,12 +352,29 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     c.src = s.gens.request(*s.job->inp, n, p, c.src);
                 }
             }
-            s.gbase = s.gens.generate(*s.job->inp, arena, s.gcn, &st);
-            s.gbase32 = nullptr;
-            if (mixed && s.gbase) {
-                s.gbase32 = (float *)arena.alloc(sizeof(float) * (size_t)bs * s.gens.keys.size());
-                k_to_fp32(s.gbase, s.gbase32, (size_t)bs * s.gens.keys.size(), ctx.stream);
+        }
+        {
+            // one generation launch for all jobs; the blocks are contiguous in job order
+            std::vector<std::pair<GenSet *, const Tree *>> sets;
+            size_t total = 0;
+            for (auto &s : js) {
+                sets.push_back({&s.gens, s.job->inp});
+                total += s.gens.keys.size();
+            }
+            generate_all(sets, arena, &st);
+            double *first = nullptr;
+            for (auto &s : js)
+                if (s.gens.base && !first) first = s.gens.base;
+            float *first32 = nullptr;
+            if (mixed && total > 0) {
+                first32 = (float *)arena.alloc(sizeof(float) * (size_t)bs * total);
+                k_to_fp32(first, first32, (size_t)bs * total, ctx.stream);
                 st.launches++;
+            }
+            for (auto &s : js) {
+                s.gbase = s.gens.base;
+                s.gcn.swap(s.gens.cn);
+                s.gbase32 = (first32 && s.gbase) ? first32 + (s.gbase - first) : nullptr;
             }
         }
         // phase C: exact screening and tier per candidate (parallel), then the
@@ -355,6 +392,11 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             const Tree &inp = *s.job->inp;
             const Oper &op = *s.job->op;
             double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / std::max(s.wgt[w], 1e-300);
+            // tier threshold: the screening threshold; at the root scale (no screening) it is known in
+            // advance only for absolute precision, otherwise root items stay in FP64
+            double tthr = !root ? thr
+                          : s.job->abs_prec ? SCREEN_FAC * split_thr(s.job->prec, 1.0, n) / std::max(s.wgt[w], 1e-300)
+                                            : -1.0;
             long long c64 = 0, c32 = 0;
             for (Cand &c : s.cand[w]) {
                 const double *cn = c.gen ? &s.gcn[8 * (size_t)c.src] : &inp.cn[8 * (size_t)c.src];
@@ -368,7 +410,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 int np_ = item_pairs(nx, ny, nz, cn, root);
                 pairs_tot += np_;
                 bool near = std::max(std::abs(c.lx), std::max(std::abs(c.ly), std::abs(c.lz))) <= 1;
-                bool use64 = !mixed || root || bd > TIER_FP64 * thr || (near_fp64 && near);
+                bool use64 = !mixed || tthr < 0.0 || bd > TIER_FP64 * tthr || (near_fp64 && near);
                 c.tier = use64 ? 0 : 1;
                 if (use64) {
                     c64++;
@@ -569,65 +611,133 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
 }
 
 // ------------------------------------------------------------------ multiply
-void multiply(double prec, Tree &out, double coef, Tree &a, Tree &b, int max_iter, bool abs_prec, bool use_max_norms,
-              mw_stats &st) {
-    Ctx &ctx = *out.ctx;
-    const Basis &bs_ = ctx.basis;
-    int bs = bs_.bs;
+// bottom-up compression of several trees, one launch per scale
+void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st) {
+    if (trees.empty()) return;
+    Ctx &ctx = *trees[0]->ctx;
+    int maxn = ctx.basis.n0;
+    for (Tree *t : trees) maxn = std::max(maxn, t->max_scale());
+    for (int n = maxn - 1; n >= ctx.basis.n0; n--) {
+        std::vector<PairTask> tasks;
+        std::vector<double *> cnp;
+        for (Tree *t : trees)
+            for (int i = 0; i < t->nn(); i++)
+                if (t->nodes[i].n == n && t->nodes[i].child0 >= 0) {
+                    tasks.push_back({t->block(i), t->block(t->nodes[i].child0)});
+                    cnp.push_back(t->d_cn + (size_t)8 * i);
+                }
+        if (tasks.empty()) continue;
+        Packer pk;
+        pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
+        pk.add(cnp.data(), cnp.size() * sizeof(double *));
+        pk.ship(ctx, arena);
+        k_compress(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(), ctx.stream);
+        if (st) st->launches++;
+    }
+    for (Tree *t : trees)
+        MWG_CUDA(cudaMemcpyAsync(t->cn.data(), t->d_cn, sizeof(double) * 8 * t->nn(), cudaMemcpyDeviceToHost,
+                                 ctx.stream));
+    ctx.sync();
+}
+
+namespace {
+
+// unresolved detail below each node: tail^2 = sum over children (|w|^2 + tail^2)
+std::vector<double> detail_tails(const Tree &t) {
+    std::vector<double> tl(t.nn(), 0.0);
+    std::vector<int> order(t.nn());
+    for (int i = 0; i < t.nn(); i++) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return t.nodes[x].n > t.nodes[y].n; });
+    for (int i : order) {
+        if (t.nodes[i].child0 < 0) continue;
+        double s = 0.0;
+        for (int c = 0; c < 8; c++) {
+            int ci = t.nodes[i].child0 + c;
+            double w = wavelet_norm8(&t.cn[8 * (size_t)ci]);
+            s += w * w + tl[ci] * tl[ci];
+        }
+        tl[i] = std::sqrt(s);
+    }
+    return tl;
+}
+
+struct MulState {
+    MulJob *job;
+    std::vector<double> ta, tb;
+    std::vector<int> work;
+    int iter = 0;
+    GenSet ga, gb;
+};
+
+}  // namespace
+
+// Level-synchronous multiply of several (out, a, b) products: per refinement
+// iteration one generation launch, one product launch and one norm download
+// for all products.  Each product follows mrcpp::multiply: the output's current
+// grid is the start grid (end nodes computed), refined while the product's
+// wavelet norm (or, with useMaxNorms, the inputs' unresolved detail times the
+// other input's RMS value) exceeds prec * R * 2^{-(n+1)/2}.
+void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
+    if (jobs.empty()) return;
+    Ctx &ctx = *jobs[0].out->ctx;
+    const Basis &bsis = ctx.basis;
     Arena &arena = ctx.arena;
     auto t_start = std::chrono::steady_clock::now();
-    // unresolved detail below each node: tail^2 = sum over children (|w|^2 + tail^2)
-    auto tails = [&](const Tree &t) {
-        std::vector<double> tl(t.nn(), 0.0);
-        std::vector<int> order(t.nn());
-        for (int i = 0; i < t.nn(); i++) order[i] = i;
-        std::sort(order.begin(), order.end(), [&](int x, int y) { return t.nodes[x].n > t.nodes[y].n; });
-        for (int i : order) {
-            if (t.nodes[i].child0 < 0) continue;
-            double s = 0.0;
-            for (int c = 0; c < 8; c++) {
-                int ci = t.nodes[i].child0 + c;
-                double w = wavelet_norm8(&t.cn[8 * (size_t)ci]);
-                s += w * w + tl[ci] * tl[ci];
-            }
-            tl[i] = std::sqrt(s);
+    std::vector<MulState> ms(jobs.size());
+    for (size_t j = 0; j < jobs.size(); j++) {
+        MulState &s = ms[j];
+        s.job = &jobs[j];
+        if (jobs[j].use_max_norms) {
+            s.ta = detail_tails(*jobs[j].a);
+            s.tb = detail_tails(*jobs[j].b);
         }
-        return tl;
-    };
-    std::vector<double> ta, tb;
-    if (use_max_norms) {
-        ta = tails(a);
-        tb = tails(b);
+        Tree &out = *jobs[j].out;
+        for (int i = 0; i < out.nn(); i++)
+            if (out.nodes[i].child0 < 0) s.work.push_back(i);
     }
-    std::vector<int> work;
-    for (int i = 0; i < out.nn(); i++)
-        if (out.nodes[i].child0 < 0) work.push_back(i);
-    int iter = 0;
-    while (!work.empty()) {
+    while (true) {
+        bool any = false;
+        for (auto &s : ms) any |= !s.work.empty();
+        if (!any) break;
         arena.reset();
-        GenSet ga, gb;
-        for (int oi : work) {
-            const NodeInfo &o = out.nodes[oi];
-            if (a.find(o.n, o.l) < 0) ga.request(a, o.n, o.l, find_ancestor(a, o.n, o.l, nullptr));
-            if (b.find(o.n, o.l) < 0) gb.request(b, o.n, o.l, find_ancestor(b, o.n, o.l, nullptr));
+        std::vector<std::pair<GenSet *, const Tree *>> sets;
+        for (auto &s : ms) {
+            s.ga.clear();
+            s.gb.clear();
+            Tree &out = *s.job->out, &a = *s.job->a, &b = *s.job->b;
+            for (int oi : s.work) {
+                const NodeInfo &o = out.nodes[oi];
+                if (a.find(o.n, o.l) < 0) s.ga.request(a, o.n, o.l, find_ancestor(a, o.n, o.l, nullptr));
+                if (b.find(o.n, o.l) < 0) s.gb.request(b, o.n, o.l, find_ancestor(b, o.n, o.l, nullptr));
+            }
+            sets.push_back({&s.ga, &a});
+            sets.push_back({&s.gb, &b});
         }
-        std::vector<double> gca, gcb;
-        double *baseA = ga.generate(a, arena, gca, &st), *baseB = gb.generate(b, arena, gcb, &st);
-        std::vector<MulTask> tasks(work.size());
-        std::vector<double> crit(work.size(), 0.0);
-        for (size_t w = 0; w < work.size(); w++) {
-            const NodeInfo &o = out.nodes[work[w]];
-            int ia = a.find(o.n, o.l), ib = b.find(o.n, o.l);
-            tasks[w].a = block_at(a, ga, baseA, o.n, o.l);
-            tasks[w].b = block_at(b, gb, baseB, o.n, o.l);
-            tasks[w].out = out.block(work[w]);
-            tasks[w].cn = out.d_cn + (size_t)8 * work[w];
-            tasks[w].scale = coef * std::pow(2.0, 1.5 * (o.n + 1));
-            if (use_max_norms) {
-                const double *cna = ia >= 0 ? &a.cn[8 * (size_t)ia] : &gca[8 * (size_t)ga.slot.at(Key{o.n, {o.l[0], o.l[1], o.l[2]}})];
-                const double *cnb = ib >= 0 ? &b.cn[8 * (size_t)ib] : &gcb[8 * (size_t)gb.slot.at(Key{o.n, {o.l[0], o.l[1], o.l[2]}})];
-                double mna = block_norm8(cna) * std::pow(2.0, 1.5 * o.n), mnb = block_norm8(cnb) * std::pow(2.0, 1.5 * o.n);
-                crit[w] = (ia >= 0 ? ta[ia] : 0.0) * mnb + (ib >= 0 ? tb[ib] : 0.0) * mna;
+        generate_all(sets, arena, &st);
+        std::vector<MulTask> tasks;
+        std::vector<std::vector<double>> crit(ms.size());
+        for (auto &s : ms) {
+            Tree &out = *s.job->out, &a = *s.job->a, &b = *s.job->b;
+            std::vector<double> &cr = crit[&s - &ms[0]];
+            cr.assign(s.work.size(), 0.0);
+            for (size_t w = 0; w < s.work.size(); w++) {
+                const NodeInfo &o = out.nodes[s.work[w]];
+                int ia = a.find(o.n, o.l), ib = b.find(o.n, o.l);
+                MulTask tk;
+                tk.a = block_at(a, s.ga, s.ga.base, o.n, o.l);
+                tk.b = block_at(b, s.gb, s.gb.base, o.n, o.l);
+                tk.out = out.block(s.work[w]);
+                tk.cn = out.d_cn + (size_t)8 * s.work[w];
+                tk.scale = s.job->coef * std::pow(2.0, 1.5 * (o.n + 1));
+                tasks.push_back(tk);
+                if (s.job->use_max_norms) {
+                    Key k{o.n, {o.l[0], o.l[1], o.l[2]}};
+                    const double *cna = ia >= 0 ? &a.cn[8 * (size_t)ia] : &s.ga.cn[8 * (size_t)s.ga.slot.at(k)];
+                    const double *cnb = ib >= 0 ? &b.cn[8 * (size_t)ib] : &s.gb.cn[8 * (size_t)s.gb.slot.at(k)];
+                    double sc = std::pow(2.0, 1.5 * o.n);
+                    cr[w] = (ia >= 0 ? s.ta[ia] : 0.0) * block_norm8(cnb) * sc +
+                            (ib >= 0 ? s.tb[ib] : 0.0) * block_norm8(cna) * sc;
+                }
             }
         }
         Packer pk;
@@ -635,29 +745,175 @@ void multiply(double prec, Tree &out, double coef, Tree &a, Tree &b, int max_ite
         pk.ship(ctx, arena);
         k_multiply(ctx.dbasis, (const MulTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
         st.launches++;
-        st.out_nodes += (long long)work.size();
-        MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
-                                 ctx.stream));
-        ctx.sync();
-        double R = abs_prec ? 1.0 : std::sqrt(out.sqnorm_leaves());
-        std::vector<int> next;
-        if (max_iter < 0 || iter < max_iter) {
-            for (size_t w = 0; w < work.size(); w++) {
-                int oi = work[w];
-                int n = out.nodes[oi].n;
-                if (n >= bs_.max_scale()) continue;
-                double thr = split_thr(prec, R, n);
-                if (wavelet_norm8(&out.cn[8 * (size_t)oi]) > thr || crit[w] > thr) {
-                    int c0 = out.split(oi);
-                    for (int c = 0; c < 8; c++) next.push_back(c0 + c);
-                }
-            }
-            if (!next.empty()) tree_zero(out, out.nn() - (int)next.size(), (int)next.size());
+        st.out_nodes += (long long)tasks.size();
+        for (auto &s : ms) {
+            Tree &out = *s.job->out;
+            MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
+                                     ctx.stream));
         }
-        work.swap(next);
-        iter++;
+        ctx.sync();
+        for (auto &s : ms) {
+            Tree &out = *s.job->out;
+            const std::vector<double> &cr = crit[&s - &ms[0]];
+            double R = s.job->abs_prec ? 1.0 : std::sqrt(out.sqnorm_leaves());
+            std::vector<int> next;
+            if (s.job->max_iter < 0 || s.iter < s.job->max_iter) {
+                for (size_t w = 0; w < s.work.size(); w++) {
+                    int oi = s.work[w];
+                    int n = out.nodes[oi].n;
+                    if (n >= bsis.max_scale()) continue;
+                    double thr = split_thr(s.job->prec, R, n);
+                    if (wavelet_norm8(&out.cn[8 * (size_t)oi]) > thr || cr[w] > thr) {
+                        int c0 = out.split(oi);
+                        for (int c = 0; c < 8; c++) next.push_back(c0 + c);
+                    }
+                }
+                if (!next.empty()) tree_zero(out, out.nn() - (int)next.size(), (int)next.size());
+            }
+            s.work.swap(next);
+            s.iter++;
+        }
+        st.levels++;
     }
-    tree_compress(out, arena, &st);
+    std::vector<Tree *> outs;
+    for (auto &j : jobs) outs.push_back(j.out);
+    arena.reset();
+    compress_batch(outs, arena, &st);
+    arena.reset();
+    st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+}
+
+// ------------------------------------------------------------------ adjoint apply
+// L2-adjoint of the fixed-grid apply y = A x (output grid = y's grid, input x,
+// absolute precision, FP64).  The forward output is the function
+//     A x = sum_o (s_o phi_o + d_o psi_o),   (s_o, d_o) = sum_{items (o,i,t)} c_t B_t(l_o - l_i) x_i,
+// with x_i the block of x at input position i (a node or a generated node), so
+//     <y, A x> = sum_items <c_t B_t(l)^T y_o, x_i>,   y_o = y's block at o.
+// The adjoint function is therefore A^T y = sum_i (g_i^s phi_i + g_i^d psi_i) with
+// g_i = sum_{items at i} c_t B_t(-l) y_o (NS(-l) = NS(l)^T), i.e. the same contraction
+// with the roles of output and input swapped ("scatter turned into gather": items are
+// grouped by input position), followed by the forward's top-down sum and compression,
+// and the projection onto x's grid (the space the forward map acts on).  The item set is
+// the forward's, screened with x's norms.
+void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats &st) {
+    Ctx &ctx = *res.ctx;
+    const Basis &b = ctx.basis;
+    const int bsz = 4 * b.K * b.K;
+    const double K4 = (double)b.K * b.K * b.K * b.K;
+    Arena &arena = ctx.arena;
+    auto t_start = std::chrono::steady_clock::now();
+    if (x.ctx != &ctx || y.ctx != &ctx || op.ctx != &ctx) throw Error(MW_ERR_ARG, "adjoint: mixed contexts");
+    // extended result grid: x's grid, grown below x's leaves where generated input positions occur
+    Tree ext;
+    ext.ctx = &ctx;
+    copy_grid(ext, x);
+    ApplyJob job{&y, &op, &x, prec, true, 0, {}};
+    JobState s;
+    s.job = &job;
+    for (int i = 0; i < x.nn(); i++) s.fmax = std::max(s.fmax, block_norm8(&x.cn[8 * (size_t)i]));
+    LevelItems li;
+    const int maxn = y.max_scale();
+    for (int n = b.n0; n <= maxn; n++) {
+        const int sidx = n - b.n0;
+        const bool root = (n == b.n0);
+        arena.reset();
+        s.work.clear();
+        for (int i = 0; i < y.nn(); i++)
+            if (y.nodes[i].n == n) s.work.push_back(i);
+        if (s.work.empty()) continue;
+        s.wgt.assign(s.work.size(), 1.0);
+        s.cand.assign(s.work.size(), {});
+        const double thr = root ? 0.0 : SCREEN_FAC * split_thr(prec, 1.0, n);
+#pragma omp parallel
+        {
+            LookupCache cache;
+#pragma omp for schedule(dynamic, 4)
+            for (long w = 0; w < (long)s.work.size(); w++) enumerate_node(s, (int)w, sidx, root, thr, cache);
+        }
+        s.gens.clear();
+        for (size_t w = 0; w < s.work.size(); w++) {
+            const NodeInfo &o = y.nodes[s.work[w]];
+            for (Cand &c : s.cand[w]) {
+                if (!c.gen) continue;
+                int p[3] = {o.l[0] - c.lx, o.l[1] - c.ly, o.l[2] - c.lz};
+                c.src = s.gens.request(x, n, p, c.src);
+            }
+        }
+        generate_all({{&s.gens, &x}}, arena, &st);
+        // surviving items, each with its input position; grow the result grid to hold every position
+        struct TItem {
+            int target, o;
+            const Cand *c;
+        };
+        std::vector<TItem> items;
+        for (size_t w = 0; w < s.work.size(); w++) {
+            const NodeInfo &o = y.nodes[s.work[w]];
+            for (const Cand &c : s.cand[w]) {
+                const double *cn = c.gen ? &s.gens.cn[8 * (size_t)c.src] : &x.cn[8 * (size_t)c.src];
+                const double *nx = op.norm(c.t, sidx, c.lx), *ny = op.norm(c.t, sidx, c.ly),
+                             *nz = op.norm(c.t, sidx, c.lz);
+                if (!root && item_bound(nx, ny, nz, cn, root) < thr) continue;
+                int p[3] = {o.l[0] - c.lx, o.l[1] - c.ly, o.l[2] - c.lz};
+                int t = ext.find(n, p);
+                while (t < 0) {  // split the deepest existing ancestor until the position exists
+                    int an = n, al[3] = {p[0], p[1], p[2]}, a = -1;
+                    while (a < 0) {
+                        an--;
+                        for (int d = 0; d < 3; d++) al[d] = floordiv2(al[d]);
+                        a = ext.find(an, al);
+                    }
+                    int first = ext.nn();
+                    ext.split(a);
+                    tree_zero(ext, first, 8);
+                    t = ext.find(n, p);
+                }
+                items.push_back({t, s.work[w], &c});
+                st.flops += 6.0 * K4 * item_pairs(nx, ny, nz, cn, root);
+            }
+        }
+        std::stable_sort(items.begin(), items.end(), [](const TItem &a, const TItem &b2) { return a.target < b2.target; });
+        li.resize(0, 0);
+        li.begin.assign(1, 0);
+        for (size_t q = 0; q < items.size(); q++) {
+            const TItem &it = items[q];
+            if (q == 0 || it.target != items[q - 1].target) {
+                if (q > 0) li.begin.push_back((long long)q);
+                li.out.push_back(ext.block(it.target));
+            }
+            li.in.push_back(y.block(it.o));
+            li.ax.push_back(op.d_blocks + (size_t)op.block_index(it.c->t, sidx, -it.c->lx) * bsz);
+            li.ay.push_back(op.d_blocks + (size_t)op.block_index(it.c->t, sidx, -it.c->ly) * bsz);
+            li.az.push_back(op.d_blocks + (size_t)op.block_index(it.c->t, sidx, -it.c->lz) * bsz);
+            li.coef.push_back(op.c[it.c->t]);
+        }
+        if (!items.empty()) li.begin.push_back((long long)items.size());
+        st.items += (long long)items.size();
+        st.items_fp64 += (long long)items.size();
+        st.out_nodes += (long long)li.out.size();
+        launch_tier(ctx, li, root, true, 0, st);
+        ctx.sync();
+        st.levels++;
+    }
+    // the forward's post-processing: top-down sum over scales, bottom-up compression
+    arena.reset();
+    for (int n = b.n0; n < ext.max_scale(); n++) {
+        std::vector<PairTask> tasks;
+        for (int i = 0; i < ext.nn(); i++)
+            if (ext.nodes[i].n == n && ext.nodes[i].child0 >= 0)
+                tasks.push_back({ext.block(i), ext.block(ext.nodes[i].child0)});
+        if (tasks.empty()) continue;
+        Packer pk;
+        pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
+        pk.ship(ctx, arena);
+        k_topdown(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
+        st.launches++;
+    }
+    compress_batch({&ext}, arena, &st);
+    // projection onto x's grid: keep x's nodes (their blocks now carry the finer parts)
+    copy_grid(res, x);
+    arena.reset();
+    combine_on_grid(res, {&ext}, {1.0}, arena, &st);
+    ext.free_device();
     arena.reset();
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }

@@ -378,8 +378,8 @@ int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const m
     });
 }
 
-int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, int max_iter, int abs_prec,
-                   int precision_mode) {
+int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *nprec,
+                   const mw_tree *prec_trees, int max_iter, int abs_prec, int precision_mode) {
     if (n < 1 || !precs || !outs || !ops || !inps) return MW_ERR_ARG;
     if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_MIXED_NEARFP64) return MW_ERR_ARG;
     for (int i = 0; i < n; i++)
@@ -387,8 +387,16 @@ int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tre
     mwg::Ctx *ctx = ctx_of(outs[0]);
     return guard(ctx, [&] {
         std::vector<mwg::ApplyJob> jobs(n);
-        for (int i = 0; i < n; i++)
+        int off = 0;
+        for (int i = 0; i < n; i++) {
             jobs[i] = mwg::ApplyJob{&outs[i]->tree, &ops[i]->op, &inps[i]->tree, precs[i], abs_prec != 0, max_iter, {}};
+            int np = nprec ? nprec[i] : 0;
+            for (int k = 0; k < np; k++) {
+                if (!prec_trees || !prec_trees[off + k]) throw mwg::Error(MW_ERR_ARG, "null precision tree");
+                jobs[i].prec_trees.push_back(&prec_trees[off + k]->tree);
+            }
+            off += np;
+        }
         mw_stats st{};
         mwg::apply_batch(jobs, precision_mode, false, st);
         ctx->last = st;
@@ -408,25 +416,44 @@ int mw_apply_fixed(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec
     });
 }
 
-int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec) {
-    (void)prec;
-    (void)abs_prec;
-    if (!out || !op || !inp) return MW_ERR_ARG;
+int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree x, mw_tree seed, int abs_prec) {
+    if (!out || !op || !x || !seed || !(prec > 0.0) || out == x || out == seed) return MW_ERR_ARG;
     mwg::Ctx *ctx = ctx_of(out);
-    ctx->err = "mw_apply_adjoint: not available in this build";
-    return MW_ERR_STATE;
+    if (!abs_prec) {
+        ctx->err = "mw_apply_adjoint: absolute precision only (the relative threshold depends on the forward output)";
+        return MW_ERR_ARG;
+    }
+    return guard(ctx, [&] {
+        check_same(out->tree, x->tree);
+        check_same(out->tree, seed->tree);
+        mw_stats st{};
+        mwg::apply_adjoint(prec, out->tree, op->op, x->tree, seed->tree, st);
+        ctx->last = st;
+    });
 }
 
 int mw_multiply(double prec, mw_tree out, double coef, mw_tree a, mw_tree b, int max_iter, int abs_prec,
                 int use_max_norms) {
-    if (!out || !a || !b || !(prec > 0.0)) return MW_ERR_ARG;
-    if (out == a || out == b) return MW_ERR_ARG;
-    mwg::Ctx *ctx = ctx_of(out);
+    return mw_multiply_batch(1, &prec, &out, &coef, &a, &b, max_iter, abs_prec, use_max_norms);
+}
+
+int mw_multiply_batch(int n, const double *precs, mw_tree *outs, const double *coefs, mw_tree *as, mw_tree *bs,
+                      int max_iter, int abs_prec, int use_max_norms) {
+    if (n < 1 || !precs || !outs || !coefs || !as || !bs) return MW_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (!outs[i] || !as[i] || !bs[i] || !(precs[i] > 0.0) || outs[i] == as[i] || outs[i] == bs[i])
+            return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(outs[0]);
     return guard(ctx, [&] {
-        check_same(out->tree, a->tree);
-        check_same(out->tree, b->tree);
+        std::vector<mwg::MulJob> jobs(n);
+        for (int i = 0; i < n; i++) {
+            check_same(outs[i]->tree, as[i]->tree);
+            check_same(outs[i]->tree, bs[i]->tree);
+            jobs[i] = mwg::MulJob{&outs[i]->tree, &as[i]->tree, &bs[i]->tree, coefs[i], precs[i], max_iter,
+                                  abs_prec != 0, use_max_norms != 0};
+        }
         mw_stats st{};
-        mwg::multiply(prec, out->tree, coef, a->tree, b->tree, max_iter, abs_prec != 0, use_max_norms != 0, st);
+        mwg::multiply_batch(jobs, st);
         ctx->last = st;
     });
 }

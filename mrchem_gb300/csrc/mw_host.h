@@ -204,7 +204,8 @@ struct ApplyLaunch {
     int root;                     // 1: include the (0,0) component pair
     int set;                      // 1: write the block, 0: add to it
     double *const *out;           // per node: output block
-    const long long *begin;       // per node + 1: item range
+    const long long *begin;       // per node: first item
+    const long long *end;         // per node: one past the last item
     const void *const *in;        // per item: input block (double or float)
     const void *const *ax;        // per item: operator blocks (double or float)
     const void *const *ay;

@@ -11,11 +11,14 @@ struct GenSet {
     std::vector<Key> keys;
     std::vector<int> anc;
     std::vector<GenTask> tasks;
+    double *base = nullptr;       // device blocks after generation
+    std::vector<double> cn;       // their component norms
     void clear();
     int request(const Tree &src, int n, const int *l, int ancestor);
     double *generate(const Tree &src, Arena &arena, std::vector<double> &cn_out, mw_stats *st);
 };
 
+void generate_all(const std::vector<std::pair<GenSet *, const Tree *>> &sets, Arena &arena, mw_stats *st);
 int find_ancestor(const Tree &t, int n, const int *l, int *an_out);
 const double *block_at(const Tree &src, const GenSet &gs, const double *gbase, int n, const int *l);
 bool key_less(const Basis &b, const NodeInfo &x, const NodeInfo &y);
@@ -53,9 +56,18 @@ struct ApplyJob {
     std::vector<Tree *> prec_trees;
 };
 
+struct MulJob {
+    Tree *out;
+    Tree *a, *b;
+    double coef, prec;
+    int max_iter;
+    bool abs_prec, use_max_norms;
+};
+
 void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st);
-void multiply(double prec, Tree &out, double coef, Tree &a, Tree &b, int max_iter, bool abs_prec, bool use_max_norms,
-              mw_stats &st);
+void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st);
+void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats &st);
+void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st);
 void add(Tree &out, const std::vector<const Tree *> &trees, const std::vector<double> &coefs, mw_stats &st);
 
 }  // namespace mwg

@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32) apply_kernel(App
         T acc[N2];
 #pragma unroll
         for (int z = 0; z < N2; z++) acc[z] = T(0);
-        const long long b0 = L.begin[w], b1 = L.begin[w + 1];
+        const long long b0 = L.begin[w], b1 = L.end[w];
         for (long long j = b0; j < b1; j++) {
             __syncthreads();
             const T *gin = reinterpret_cast<const T *>(L.in[j]);
@@ -365,12 +365,155 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32) apply_kernel(App
     }
 }
 
+// N contiguous floats from shared memory, with the widest aligned vector loads
+template <int N>
+__device__ __forceinline__ void lds_row(float (&r)[N], const float *p) {
+    if constexpr (N % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < N / 4; i++) {
+            float4 v = reinterpret_cast<const float4 *>(p)[i];
+            r[4 * i] = v.x;
+            r[4 * i + 1] = v.y;
+            r[4 * i + 2] = v.z;
+            r[4 * i + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N / 2; i++) {
+            float2 v = reinterpret_cast<const float2 *>(p)[i];
+            r[2 * i] = v.x;
+            r[2 * i + 1] = v.y;
+        }
+    }
+}
+
+// FP32 tier of the NS-form apply.  Same contraction and exclusion as
+// apply_kernel, arranged so that every shared-memory read is a vector read of
+// a contiguous row: the x pass stores t1 transposed as t1T[Z][X'][Y], the
+// y pass reads rows of t1T, the z pass reads rows of A_z.  The FP32 partial
+// sum of the node is added once to its FP64 block.
+template <int K>
+__global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kernel(ApplyLaunch L) {
+    constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K, U = ((K3 + 3) / 4) * 4;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *s_in = reinterpret_cast<float *>(smem_raw);
+    float *s_t1 = s_in + C;   // t1T[Z][X'][Y]
+    float *s_acc = s_t1 + C;  // node accumulator acc[Z'][Y'][X'] (kept in shared memory: two CTAs per SM)
+    float *s_u = s_acc + C;   // u[Z][X'][Y], Z, X', Y < K
+    float *s_A = s_u + U;
+    __shared__ int s_node;
+    const int tid = threadIdx.x;
+    const bool active = tid < NC;
+    const int Yp = tid / N2, Xp = tid % N2;
+    const bool excl = !L.root && active && (Yp < K) && (Xp < K);
+
+    while (true) {
+        if (tid == 0) s_node = atomicAdd(L.counter, 1);
+        __syncthreads();
+        const int w = s_node;
+        if (w >= L.nnodes) break;
+        for (int i = tid; i < C; i += blockDim.x) s_acc[i] = 0.0f;
+        const long long b0 = L.begin[w], b1 = L.end[w];
+        for (long long j = b0; j < b1; j++) {
+            __syncthreads();
+            const float *gin = reinterpret_cast<const float *>(L.in[j]);
+            for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
+                int c = gi / K3, r = gi - c * K3;
+                int iz = r / (K * K), iy = (r / K) % K, ix = r % K;
+                int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
+                s_in[(Z * N2 + Y) * N2 + X] = gin[gi];
+            }
+            const float *ax = reinterpret_cast<const float *>(L.ax[j]);
+            const float *ay = reinterpret_cast<const float *>(L.ay[j]);
+            const float *az = reinterpret_cast<const float *>(L.az[j]);
+            for (int i = tid; i < NC; i += blockDim.x) {
+                s_A[i] = ax[i];
+                s_A[NC + i] = ay[i];
+                s_A[2 * NC + i] = az[i];
+            }
+            const float cf = float(L.coef[j]);
+            __syncthreads();
+            if (active) {  // x pass, thread (Y = Yp, X' = Xp)
+                float a[N2];
+                lds_row<N2>(a, s_A + Xp * N2);
+#pragma unroll 2
+                for (int Z = 0; Z < N2; Z++) {
+                    float row[N2];
+                    lds_row<N2>(row, s_in + (Z * N2 + Yp) * N2);
+                    float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+                    for (int X = 0; X < K; X++) s0 = fmaf(a[X], row[X], s0);
+#pragma unroll
+                    for (int X = K; X < N2; X++) s1 = fmaf(a[X], row[X], s1);
+                    s_t1[(Z * N2 + Xp) * N2 + Yp] = s0 + s1;
+                    if (excl && Z < K) s_u[(Z * K + Xp) * K + Yp] = s1;
+                }
+            }
+            __syncthreads();
+            if (active) {  // y and z passes, thread (Y' = Yp, X' = Xp)
+                float ayr[N2], t2[N2], t2x[K];
+                lds_row<N2>(ayr, s_A + NC + Yp * N2);
+#pragma unroll
+                for (int Z = 0; Z < N2; Z++) {
+                    float row[N2];
+                    lds_row<N2>(row, s_t1 + (Z * N2 + Xp) * N2);
+                    float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+                    for (int Y = 0; Y < K; Y++) s0 = fmaf(ayr[Y], row[Y], s0);
+#pragma unroll
+                    for (int Y = K; Y < N2; Y++) s1 = fmaf(ayr[Y], row[Y], s1);
+                    t2[Z] = s0 + s1;
+                    if (Z < K) {
+                        float su = 0.0f;
+                        if (excl) {
+                            const float *urow = s_u + (Z * K + Xp) * K;
+#pragma unroll
+                            for (int Y = 0; Y < K; Y++) su = fmaf(ayr[Y], urow[Y], su);
+                        }
+                        t2x[Z < K ? Z : 0] = su + s1;
+                    }
+                }
+#pragma unroll
+                for (int Zp = 0; Zp < N2; Zp++) {
+                    float azr[N2];
+                    lds_row<N2>(azr, s_A + 2 * NC + Zp * N2);
+                    float sacc = 0.0f;
+#pragma unroll
+                    for (int Z = 0; Z < N2; Z++) {
+                        float v = t2[Z];
+                        if (Zp < K && Z < K) v = excl ? t2x[Z < K ? Z : 0] : v;
+                        sacc = fmaf(azr[Z], v, sacc);
+                    }
+                    float &a_ = s_acc[(Zp * N2 + Yp) * N2 + Xp];
+                    a_ = fmaf(cf, sacc, a_);
+                }
+            }
+        }
+        __syncthreads();
+        if (active) {
+            double *out = L.out[w];
+#pragma unroll
+            for (int Zp = 0; Zp < N2; Zp++) {
+                int c = (Xp >= K ? 1 : 0) | (Yp >= K ? 2 : 0) | (Zp >= K ? 4 : 0);
+                int gi = c * K3 + (Zp % K) * K * K + (Yp % K) * K + (Xp % K);
+                double v = double(s_acc[(Zp * N2 + Yp) * N2 + Xp]);
+                if (L.set)
+                    out[gi] = v;
+                else
+                    out[gi] += v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 template <typename T, int K>
 void launch_apply_t(const ApplyLaunch &L, int nsm, cudaStream_t s) {
     constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K;
     const int threads = ((NC + 31) / 32) * 32;
-    const size_t smem = sizeof(T) * (2 * C + K3 + 3 * NC);
-    auto fn = apply_kernel<T, K>;
+    const bool f32 = sizeof(T) == 4;
+    const size_t smem = f32 ? sizeof(float) * (3 * C + ((K3 + 3) / 4) * 4 + 3 * NC) : sizeof(T) * (2 * C + K3 + 3 * NC);
+    auto fn = f32 ? apply32_kernel<K> : apply_kernel<T, K>;
     MWG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     MWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));

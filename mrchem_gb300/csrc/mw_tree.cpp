@@ -306,45 +306,70 @@ int find_ancestor(const Tree &t, int n, const int *l, int *an_out) {
     return a;
 }
 
-// Generates the requested blocks of `src` into arena memory; returns device base.
-double *GenSet::generate(const Tree &src, Arena &arena, std::vector<double> &cn_out, mw_stats *st) {
-    Ctx &ctx = *src.ctx;
-    int ng = (int)keys.size();
-    cn_out.assign((size_t)8 * ng, 0.0);
-    if (ng == 0) return nullptr;
-    int bs = ctx.basis.bs;
-    double *blocks = (double *)arena.alloc(sizeof(double) * (size_t)bs * ng);
-    double *cnd = (double *)arena.alloc(sizeof(double) * 8 * (size_t)ng);
-    tasks.resize(ng);
-    for (int g = 0; g < ng; g++) {
-        const Key &k = keys[g];
-        int a = anc[g];
-        int an = src.nodes[a].n;
-        GenTask &tk = tasks[g];
-        tk.anc = src.block(a);
-        tk.out = blocks + (size_t)g * bs;
-        tk.cn = cnd + (size_t)8 * g;
-        tk.steps = k.n - an;
-        tk.path = 0;
-        for (int s = 0; s < tk.steps; s++) {
-            int sh = k.n - (an + s + 1);
-            uint64_t c = 0;
-            for (int d = 0; d < 3; d++) c |= (uint64_t)((k.l[d] >> sh) & 1) << d;
-            tk.path |= c << (3 * s);
+// Generates the requested blocks of several (set, source tree) pairs with one
+// launch and one norm download; each set gets its device base and host norms.
+void generate_all(const std::vector<std::pair<GenSet *, const Tree *>> &sets, Arena &arena, mw_stats *st) {
+    if (sets.empty()) return;
+    Ctx &ctx = *sets[0].second->ctx;
+    const int bs = ctx.basis.bs;
+    long total = 0;
+    for (auto &p : sets) total += (long)p.first->keys.size();
+    for (auto &p : sets) {
+        p.first->base = nullptr;
+        p.first->cn.assign(8 * p.first->keys.size(), 0.0);
+    }
+    if (total == 0) return;
+    double *blocks = (double *)arena.alloc(sizeof(double) * (size_t)bs * total);
+    double *cnd = (double *)arena.alloc(sizeof(double) * 8 * (size_t)total);
+    std::vector<GenTask> tasks(total);
+    long off = 0;
+    for (auto &p : sets) {
+        GenSet &gs = *p.first;
+        const Tree &src = *p.second;
+        gs.base = blocks + (size_t)off * bs;
+        for (size_t g = 0; g < gs.keys.size(); g++) {
+            const Key &k = gs.keys[g];
+            int a = gs.anc[g];
+            int an = src.nodes[a].n;
+            GenTask &tk = tasks[off + g];
+            tk.anc = src.block(a);
+            tk.out = blocks + (size_t)(off + g) * bs;
+            tk.cn = cnd + (size_t)8 * (off + g);
+            tk.steps = k.n - an;
+            tk.path = 0;
+            for (int s = 0; s < tk.steps; s++) {
+                int sh = k.n - (an + s + 1);
+                uint64_t c = 0;
+                for (int d = 0; d < 3; d++) c |= (uint64_t)((k.l[d] >> sh) & 1) << d;
+                tk.path |= c << (3 * s);
+            }
+            tk.pad = 0;
         }
-        tk.pad = 0;
+        off += (long)gs.keys.size();
     }
     Packer pk;
     pk.add(tasks.data(), tasks.size() * sizeof(GenTask));
     pk.ship(ctx, arena);
-    k_generate(ctx.dbasis, (const GenTask *)pk.ptr(0), ng, ctx.stream);
+    k_generate(ctx.dbasis, (const GenTask *)pk.ptr(0), (int)total, ctx.stream);
     if (st) {
         st->launches++;
-        st->generated += ng;
+        st->generated += total;
     }
-    MWG_CUDA(cudaMemcpyAsync(cn_out.data(), cnd, sizeof(double) * 8 * ng, cudaMemcpyDeviceToHost, ctx.stream));
+    std::vector<double> h((size_t)8 * total);
+    MWG_CUDA(cudaMemcpyAsync(h.data(), cnd, sizeof(double) * 8 * total, cudaMemcpyDeviceToHost, ctx.stream));
     ctx.sync();
-    return blocks;
+    off = 0;
+    for (auto &p : sets) {
+        std::copy(h.begin() + 8 * off, h.begin() + 8 * (off + (long)p.first->keys.size()), p.first->cn.begin());
+        off += (long)p.first->keys.size();
+    }
+}
+
+// Generates the requested blocks of `src` into arena memory; returns device base.
+double *GenSet::generate(const Tree &src, Arena &arena, std::vector<double> &cn_out, mw_stats *st) {
+    generate_all({{this, &src}}, arena, st);
+    cn_out = cn;
+    return base;
 }
 
 // block pointer of src at (n,l): the node's block or a generated one (gens must be generated)
