@@ -72,6 +72,9 @@ typedef struct {
     double flops_fp32;       /* ... of the FP32 tier */
     double kernel_ms_fp64;   /* CUDA-event time of the FP64 contraction launches */
     double kernel_ms_fp32;   /* ... of the FP32 contraction launches */
+    double host_enum_ms;     /* host: candidate enumeration (screening bounds, lookups) */
+    double host_items_ms;    /* host: generation requests, exact screening, tiers, item lists */
+    double host_wait_ms;     /* host: waiting for the level's kernels and norm downloads */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */

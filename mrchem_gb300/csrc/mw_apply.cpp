@@ -288,7 +288,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 MWG_CUDA(cudaMalloc(&in.d_coefs32, sizeof(float) * (size_t)bs * in.cap));
                 in.cap32 = in.cap;
             }
-            k_to_fp32(in.d_coefs, in.d_coefs32, (size_t)bs * in.nn(), ctx.stream);
+            k_to_fp32_cube(in.d_coefs, in.d_coefs32, (size_t)in.nn(), b.K, ctx.stream);
             st.launches++;
         }
         for (int i = 0; i < job.out->nroots; i++) s.work.push_back(i);
@@ -323,6 +323,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             s.cand.assign(s.work.size(), {});
         }
         // phase A: candidate enumeration (host, all jobs' nodes in parallel)
+        auto tA = std::chrono::steady_clock::now();
         std::vector<std::pair<int, int>> flat;
         for (size_t j = 0; j < js.size(); j++)
             for (size_t w = 0; w < js[j].work.size(); w++) flat.push_back({(int)j, (int)w});
@@ -341,6 +342,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 enumerate_node(s, w, sidx, root, thr, cache);
             }
         }
+        auto tB = std::chrono::steady_clock::now();
+        st.host_enum_ms += std::chrono::duration<double, std::milli>(tB - tA).count();
         // phase B: generated input nodes
         for (auto &s : js) {
             s.gens.clear();
@@ -368,7 +371,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             float *first32 = nullptr;
             if (mixed && total > 0) {
                 first32 = (float *)arena.alloc(sizeof(float) * (size_t)bs * total);
-                k_to_fp32(first, first32, (size_t)bs * total, ctx.stream);
+                k_to_fp32_cube(first, first32, total, b.K, ctx.stream);
                 st.launches++;
             }
             for (auto &s : js) {

@@ -139,9 +139,12 @@ struct Arena {
         void *ptr = nullptr;
         size_t size = 0, used = 0;
     };
-    std::vector<Chunk> chunks;
+    std::vector<Chunk> chunks;   // device memory
+    std::vector<Chunk> hchunks;  // pinned host staging for the copies that fill it
     size_t total = 0;
     void *alloc(size_t bytes);
+    void *halloc(size_t bytes);
+    // call only when the GPU no longer reads anything allocated since the last reset
     void reset();
     void release();
 };
@@ -242,6 +245,8 @@ void k_multiply(const DevBasis &b, const MulTask *tasks, int n, cudaStream_t s);
 void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
            cudaStream_t s);
 void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);
+// FP32 copy of whole blocks, each written in cube order cube[Z][Y][X] (X = cx*K + ix)
+void k_to_fp32_cube(const double *in, float *out, size_t nblocks, int K, cudaStream_t s);
 void k_dot(const double *const *a, const double *const *b, const int *start, int n, int bs, double *partial,
            cudaStream_t s);
 void k_scale(double *x, size_t n, double c, cudaStream_t s);

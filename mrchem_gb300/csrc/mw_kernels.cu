@@ -416,13 +416,10 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kerne
         const long long b0 = L.begin[w], b1 = L.end[w];
         for (long long j = b0; j < b1; j++) {
             __syncthreads();
-            const float *gin = reinterpret_cast<const float *>(L.in[j]);
-            for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
-                int c = gi / K3, r = gi - c * K3;
-                int iz = r / (K * K), iy = (r / K) % K, ix = r % K;
-                int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
-                s_in[(Z * N2 + Y) * N2 + X] = gin[gi];
-            }
+            // FP32 input blocks are stored in cube order: a straight 16-byte vector copy
+            const float4 *gin4 = reinterpret_cast<const float4 *>(L.in[j]);
+            float4 *sin4 = reinterpret_cast<float4 *>(s_in);
+            for (int i = tid; i < C / 4; i += blockDim.x) sin4[i] = __ldg(gin4 + i);
             const float *ax = reinterpret_cast<const float *>(L.ax[j]);
             const float *ay = reinterpret_cast<const float *>(L.ay[j]);
             const float *az = reinterpret_cast<const float *>(L.az[j]);
@@ -623,6 +620,16 @@ __global__ void to_fp32_kernel(const double *in, float *out, size_t n) {
         out[i] = (float)in[i];
 }
 
+// FP32 copy of nblocks blocks, each written in cube order cube[Z][Y][X]
+__global__ void to_fp32_cube_kernel(const double *in, float *out, size_t nblocks, int K) {
+    const size_t bs = 8 * (size_t)K * K * K, n = nblocks * bs;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        size_t b = i / bs;
+        int gi = (int)(i - b * bs);
+        out[b * bs + cube_of_block(gi, K)] = (float)in[i];
+    }
+}
+
 __global__ void scale_kernel(double *x, size_t n, double c) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
         x[i] *= c;
@@ -757,6 +764,12 @@ void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, co
 void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s) {
     if (n == 0) return;
     to_fp32_kernel<<<4096, 256, 0, s>>>(in, out, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_to_fp32_cube(const double *in, float *out, size_t nblocks, int K, cudaStream_t s) {
+    if (nblocks == 0) return;
+    to_fp32_cube_kernel<<<4096, 256, 0, s>>>(in, out, nblocks, K);
     MWG_CUDA(cudaGetLastError());
 }
 

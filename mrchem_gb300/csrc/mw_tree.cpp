@@ -35,6 +35,24 @@ void *Arena::alloc(size_t bytes) {
     return c.ptr;
 }
 
+void *Arena::halloc(size_t bytes) {
+    bytes = (bytes + 255) & ~size_t(255);
+    if (bytes == 0) bytes = 256;
+    if (!hchunks.empty() && hchunks.back().used + bytes <= hchunks.back().size) {
+        Chunk &c = hchunks.back();
+        void *p = (char *)c.ptr + c.used;
+        c.used += bytes;
+        return p;
+    }
+    size_t sz = std::max(bytes, hchunks.empty() ? (size_t)64 << 20 : hchunks.back().size * 2);
+    Chunk c;
+    c.size = sz;
+    MWG_CUDA(cudaMallocHost(&c.ptr, sz));
+    c.used = bytes;
+    hchunks.push_back(c);
+    return c.ptr;
+}
+
 void Arena::reset() {
     if (chunks.size() > 1) {
         size_t need = 0;
@@ -49,12 +67,27 @@ void Arena::reset() {
     } else if (!chunks.empty()) {
         chunks.back().used = 0;
     }
+    if (hchunks.size() > 1) {
+        size_t need = 0;
+        for (auto &c : hchunks) need += c.size;
+        for (auto &c : hchunks) cudaFreeHost(c.ptr);
+        hchunks.clear();
+        Chunk c;
+        c.size = need;
+        MWG_CUDA(cudaMallocHost(&c.ptr, need));
+        c.used = 0;
+        hchunks.push_back(c);
+    } else if (!hchunks.empty()) {
+        hchunks.back().used = 0;
+    }
     total = 0;
 }
 
 void Arena::release() {
     for (auto &c : chunks) cudaFree(c.ptr);
+    for (auto &c : hchunks) cudaFreeHost(c.ptr);
     chunks.clear();
+    hchunks.clear();
     total = 0;
 }
 
@@ -84,8 +117,9 @@ void *Packer::add(const void *src, size_t bytes) {
 void Packer::ship(Ctx &ctx, Arena &arena) {
     size_t total = size.empty() ? 0 : offs.back() + size.back();
     if (total == 0) return;
-    ctx.sync();  // the pinned buffer may still feed an earlier copy
-    char *h = (char *)ctx.pinned(total);
+    // staging lives in the arena's pinned chunks until the arena is reset, so packing never
+    // waits for earlier copies or kernels
+    char *h = (char *)arena.halloc(total);
     for (size_t i = 0; i < srcs.size(); i++)
         if (size[i]) std::memcpy(h + offs[i], srcs[i], size[i]);
     dev = (char *)arena.alloc(total);
