@@ -287,6 +287,9 @@ def run(args):
         "rel_l2_vs_fp64_max": max(errs),
         "items": {"total": st["items"], "fp64": st["items_fp64"], "fp32": st["items_fp32"]},
         "kernel_ms_per_step": st["kernel_ms"], "host_ms_per_step": st["host_ms"],
+        "host_breakdown_ms": {"enumerate": st["host_enum_ms"], "items": st["host_items_ms"],
+                              "wait_level": st["host_wait_ms"], "kernel_fp64": st["kernel_ms_fp64"],
+                              "kernel_fp32": st["kernel_ms_fp32"]},
         "gpu_launches": int(st["launches"]),
         "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": roofline,

@@ -80,6 +80,8 @@ typedef struct {
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */
 int mw_ctx_create(int device, int root_scale, const int corner[3], const int boxes[3], int order, int basis,
                   int max_depth, mw_ctx *out);
+/* Handles may be destroyed in any order: a destroyed context is released when the last of its
+ * trees and operators is destroyed. */
 int mw_ctx_destroy(mw_ctx ctx);
 const char *mw_last_error(mw_ctx ctx);
 int mw_ctx_basis(mw_ctx ctx, double *qx, double *qw, double *filter, double *c2v, double *v2c);
@@ -157,10 +159,24 @@ int mw_square(double prec, mw_tree out, mw_tree inp, int max_iter, int abs_prec)
 /* mrcpp::add(prec, out, FunctionTreeVector, maxIter) on the union grid (density_utils.cpp:85-86) */
 int mw_add(double prec, mw_tree out, int n, const double *coefs, const mw_tree *trees, int max_iter);
 
+/* ---- composite steps around the path, device-resident ---- */
+/* rho <- sum_i occ_i |phi_i|^2 (density::compute, src/qmfunctions/density_utils.cpp:64-150): squares
+ * on copies of the orbitals' grids (one batched multiply), added on their union grid, cropped at
+ * prec / sum(occ) when crop != 0 */
+int mw_density(double prec, mw_tree rho, int n, const mw_tree *orbitals, const double *occ, int crop);
+/* out_i <- sum_j U[i*nin + j] in_j on the inputs' union grid (orbital rotation,
+ * src/qmfunctions/orbital_utils.cpp:242-248) */
+int mw_rotate(int nout, mw_tree *outs, int nin, const mw_tree *ins, const double *U);
+/* one tree to / from a file (checkpoint, src/qmfunctions/orbital_utils.cpp:1218-1240); format in mw_tree.cpp */
+int mw_tree_save(mw_tree t, const char *path);
+int mw_tree_load(mw_tree t, const char *path);
+
 /* ---- diagnostics ---- */
 /* measured FMA throughput of this GPU (TFLOP/s) in FP64 (fp64 = 1) or FP32 (fp64 = 0):
  * the denominator of the CUDA-core roofline of the contraction kernels */
 int mw_probe_fma_peak(mw_ctx ctx, int fp64, double *tflops);
+/* measured dense warp-MMA throughput (TFLOP/s): kind 0 = TF32 m16n8k8, kind 1 = BF16 m16n8k16 */
+int mw_probe_mma_peak(mw_ctx ctx, int kind, double *tflops);
 
 #ifdef __cplusplus
 }

@@ -51,7 +51,8 @@ class Stats(C.Structure):
                 ("levels", C.c_longlong), ("launches", C.c_longlong), ("flops", C.c_double),
                 ("flops_issued", C.c_double), ("bytes", C.c_double), ("kernel_ms", C.c_double),
                 ("host_ms", C.c_double), ("flops_fp64", C.c_double), ("flops_fp32", C.c_double),
-                ("kernel_ms_fp64", C.c_double), ("kernel_ms_fp32", C.c_double)]
+                ("kernel_ms_fp64", C.c_double), ("kernel_ms_fp32", C.c_double), ("host_enum_ms", C.c_double),
+                ("host_items_ms", C.c_double), ("host_wait_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -66,7 +67,8 @@ EXPORTS = [
     "mw_tree_clear", "mw_project_gauss", "mw_project_hydrogen", "mw_copy_grid", "mw_build_grid", "mw_copy_func",
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
-    "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak",
+    "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
+    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak",
 ]
 
 
@@ -122,6 +124,11 @@ def load_library(path=None):
         "mw_square": [D, P, P, I, I],
         "mw_add": [D, P, I, dp, pp, I],
         "mw_probe_fma_peak": [P, I, dp],
+        "mw_probe_mma_peak": [P, I, dp],
+        "mw_density": [D, P, I, pp, dp, I],
+        "mw_rotate": [I, pp, I, pp, dp],
+        "mw_tree_save": [P, C.c_char_p],
+        "mw_tree_load": [P, C.c_char_p],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -201,6 +208,12 @@ class MultiResolutionAnalysis:
         """Measured FMA throughput of this GPU in TFLOP/s (FP64 or FP32 CUDA cores)."""
         v = C.c_double()
         _check(_lib.mw_probe_fma_peak(self.ptr, int(fp64), C.byref(v)), self.ptr)
+        return v.value
+
+    def probe_mma_peak(self, kind="tf32"):
+        """Measured dense warp-MMA throughput in TFLOP/s ("tf32": m16n8k8, "bf16": m16n8k16)."""
+        v = C.c_double()
+        _check(_lib.mw_probe_mma_peak(self.ptr, {"tf32": 0, "bf16": 1}[kind], C.byref(v)), self.ptr)
         return v.value
 
 
@@ -470,6 +483,31 @@ def clear(trees, dealloc=False):
             t.close()
         else:
             t.clear()
+
+
+def density(prec, rho, orbitals, occupations, crop=True):
+    """rho <- sum_i occ_i |phi_i|^2 on the device (density::compute, src/qmfunctions/density_utils.cpp:64-150)."""
+    occ = np.ascontiguousarray(occupations, dtype=np.float64)
+    _check(_lib.mw_density(prec, rho.ptr, len(orbitals), _ptrs(orbitals), _dp(occ), int(crop)), rho.mra.ptr)
+    return rho.mra.last_stats()
+
+
+def rotate(outs, ins, U):
+    """out_i <- sum_j U[i, j] in_j on the inputs' union grid (orbital rotation)."""
+    U = np.ascontiguousarray(U, dtype=np.float64)
+    if U.shape != (len(outs), len(ins)):
+        raise ValueError("U must be len(outs) x len(ins)")
+    _check(_lib.mw_rotate(len(outs), _ptrs(outs), len(ins), _ptrs(ins), _dp(U)), outs[0].mra.ptr)
+    return outs[0].mra.last_stats()
+
+
+def save_tree(tree, path):
+    _check(_lib.mw_tree_save(tree.ptr, os.fsencode(path)), tree.mra.ptr)
+
+
+def load_tree(tree, path):
+    _check(_lib.mw_tree_load(tree.ptr, os.fsencode(path)), tree.mra.ptr)
+    return tree
 
 
 def dot(a, b):

@@ -480,6 +480,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         st.flops_issued += 96.0 * K4 * (double)(n64 + n32);
         st.flops_fp64 += 6.0 * K4 * (double)pairs64;
         st.flops_fp32 += 6.0 * K4 * (double)pairs32;
+        st.host_items_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tB).count();
         MWG_CUDA(cudaEventRecord(ev0, ctx.stream));
         launch_tier(ctx, li64, root, true, 0, st);
         MWG_CUDA(cudaEventRecord(evm, ctx.stream));
@@ -505,7 +506,9 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
                                      ctx.stream));
         }
+        auto tW = std::chrono::steady_clock::now();
         ctx.sync();
+        st.host_wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tW).count();
         float ms = 0.0f, ms64 = 0.0f;
         MWG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         MWG_CUDA(cudaEventElapsedTime(&ms64, ev0, evm));
@@ -929,6 +932,57 @@ void add(Tree &out, const std::vector<const Tree *> &trees, const std::vector<do
     combine_on_grid(out, trees, coefs, ctx.arena, &st);
     ctx.arena.reset();
     st.out_nodes += out.nn();
+    st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+}
+
+// Electron density rho = sum_i occ_i |phi_i|^2 kept on the device, following
+// density::compute (src/qmfunctions/density_utils.cpp:64-150): every square on a copy of the
+// orbital's grid (refined adaptively at prec), the squares added on their union grid, and the
+// sum cropped at prec / N_el when crop is set.  The squares of all orbitals run as one batched
+// multiply.
+void density(double prec, Tree &rho, const std::vector<Tree *> &orbs, const std::vector<double> &occ, bool crop_sum,
+             mw_stats &st) {
+    Ctx &ctx = *rho.ctx;
+    std::vector<Tree> sq(orbs.size());
+    std::vector<MulJob> jobs(orbs.size());
+    for (size_t i = 0; i < orbs.size(); i++) {
+        sq[i].ctx = &ctx;
+        copy_grid(sq[i], *orbs[i]);
+        jobs[i] = MulJob{&sq[i], orbs[i], orbs[i], 1.0, prec, -1, false, false};
+    }
+    multiply_batch(jobs, st);
+    std::vector<const Tree *> v;
+    for (auto &t : sq) v.push_back(&t);
+    tree_clear(rho);
+    add(rho, v, occ, st);
+    if (crop_sum) {
+        double nel = 0.0;
+        for (double o : occ) nel += o;
+        crop(rho, prec / std::max(nel, 1.0), true, ctx.arena);
+    }
+    for (auto &t : sq) t.free_device();
+}
+
+// Linear combinations out_i = sum_j U_ij in_j for many outputs at once (orbital rotation,
+// src/qmfunctions/orbital_utils.cpp:242-248): every output gets the union grid of the inputs,
+// and each node block is a small matrix product over the inputs' blocks at that node.
+void rotate(const std::vector<Tree *> &outs, const std::vector<const Tree *> &ins, const double *U, mw_stats &st) {
+    Ctx &ctx = *outs[0]->ctx;
+    auto t_start = std::chrono::steady_clock::now();
+    Tree grid;
+    grid.ctx = &ctx;
+    tree_clear(grid);
+    build_grid(grid, ins);
+    const size_t nj = ins.size();
+    for (size_t i = 0; i < outs.size(); i++) {
+        copy_grid(*outs[i], grid);
+        std::vector<double> row(U + i * nj, U + (i + 1) * nj);
+        ctx.arena.reset();
+        combine_on_grid(*outs[i], ins, row, ctx.arena, &st);
+        st.out_nodes += outs[i]->nn();
+    }
+    grid.free_device();
+    ctx.arena.reset();
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }
 

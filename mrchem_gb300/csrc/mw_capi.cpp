@@ -100,12 +100,14 @@ int mw_ctx_create(int device, int root_scale, const int corner[3], const int box
         delete c;
         return rc;
     }
+    c->ctx.owner = c;
     *out = c;
     return MW_OK;
 }
 
-int mw_ctx_destroy(mw_ctx c) {
-    if (!c) return MW_ERR_ARG;
+// A context is released only when the caller destroyed it AND no tree or operator of it is
+// alive, so handles may be destroyed in any order (e.g. by a garbage collector).
+static void ctx_free(mw_ctx c) {
     cudaSetDevice(c->ctx.device);
     cudaStreamSynchronize(c->ctx.stream);
     c->ctx.arena.release();
@@ -113,6 +115,16 @@ int mw_ctx_destroy(mw_ctx c) {
     if (c->ctx.d_basis) cudaFree(c->ctx.d_basis);
     cudaStreamDestroy(c->ctx.stream);
     delete c;
+}
+
+static void ctx_child_gone(mwg::Ctx *ctx) {
+    if (--ctx->live == 0 && ctx->closing) ctx_free(static_cast<mw_ctx>(ctx->owner));
+}
+
+int mw_ctx_destroy(mw_ctx c) {
+    if (!c || c->ctx.closing) return MW_ERR_ARG;
+    c->ctx.closing = true;
+    if (c->ctx.live == 0) ctx_free(c);
     return MW_OK;
 }
 
@@ -153,16 +165,19 @@ int mw_tree_create(mw_ctx c, mw_tree *out) {
         delete t;
         return rc;
     }
+    c->ctx.live++;
     *out = t;
     return MW_OK;
 }
 
 int mw_tree_destroy(mw_tree t) {
     if (!t) return MW_ERR_ARG;
-    cudaSetDevice(t->tree.ctx->device);
-    cudaStreamSynchronize(t->tree.ctx->stream);
+    mwg::Ctx *ctx = t->tree.ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
     t->tree.free_device();
     delete t;
+    ctx_child_gone(ctx);
     return MW_OK;
 }
 
@@ -300,6 +315,7 @@ static int op_create(mw_ctx c, int kind, double mu, double prec, mw_op *out) {
         delete o;
         return rc;
     }
+    c->ctx.live++;
     *out = o;
     return MW_OK;
 }
@@ -315,7 +331,9 @@ int mw_op_destroy(mw_op o) {
     if (o->op.d_blocks) cudaFree(o->op.d_blocks);
     if (o->op.d_blocks32) cudaFree(o->op.d_blocks32);
     if (o->op.d_blocks16) cudaFree(o->op.d_blocks16);
+    mwg::Ctx *ctx = o->op.ctx;
     delete o;
+    ctx_child_gone(ctx);
     return MW_OK;
 }
 
@@ -479,6 +497,60 @@ int mw_add(double prec, mw_tree out, int n, const double *coefs, const mw_tree *
         mwg::add(out->tree, v, c, st);
         ctx->last = st;
     });
+}
+
+int mw_density(double prec, mw_tree rho, int n, const mw_tree *orbitals, const double *occ, int crop) {
+    if (!rho || n < 1 || !orbitals || !occ || !(prec > 0.0)) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(rho);
+    return guard(ctx, [&] {
+        std::vector<mwg::Tree *> v;
+        for (int i = 0; i < n; i++) {
+            if (!orbitals[i] || orbitals[i] == rho) throw mwg::Error(MW_ERR_ARG, "density: null orbital or output");
+            check_same(rho->tree, orbitals[i]->tree);
+            v.push_back(&orbitals[i]->tree);
+        }
+        mw_stats st{};
+        mwg::density(prec, rho->tree, v, std::vector<double>(occ, occ + n), crop != 0, st);
+        ctx->last = st;
+    });
+}
+
+int mw_rotate(int nout, mw_tree *outs, int nin, const mw_tree *ins, const double *U) {
+    if (nout < 1 || nin < 1 || !outs || !ins || !U) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(outs[0]);
+    return guard(ctx, [&] {
+        std::vector<mwg::Tree *> o;
+        std::vector<const mwg::Tree *> in;
+        for (int i = 0; i < nout; i++) {
+            if (!outs[i]) throw mwg::Error(MW_ERR_ARG, "rotate: null output");
+            o.push_back(&outs[i]->tree);
+        }
+        for (int j = 0; j < nin; j++) {
+            if (!ins[j]) throw mwg::Error(MW_ERR_ARG, "rotate: null input");
+            for (int i = 0; i < nout; i++)
+                if (ins[j] == outs[i]) throw mwg::Error(MW_ERR_ARG, "rotate: an output is also an input");
+            check_same(outs[0]->tree, ins[j]->tree);
+            in.push_back(&ins[j]->tree);
+        }
+        mw_stats st{};
+        mwg::rotate(o, in, U, st);
+        ctx->last = st;
+    });
+}
+
+int mw_tree_save(mw_tree t, const char *path) {
+    if (!t || !path) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { mwg::tree_save(t->tree, path); });
+}
+
+int mw_tree_load(mw_tree t, const char *path) {
+    if (!t || !path) return MW_ERR_ARG;
+    return guard(ctx_of(t), [&] { mwg::tree_load(t->tree, path); });
+}
+
+int mw_probe_mma_peak(mw_ctx c, int kind, double *tflops) {
+    if (!c || !tflops || kind < 0 || kind > 1) return MW_ERR_ARG;
+    return guard(&c->ctx, [&] { *tflops = mwg::probe_mma_tflops(kind, c->ctx.nsm, c->ctx.stream); });
 }
 
 int mw_probe_fma_peak(mw_ctx c, int fp64, double *tflops) {

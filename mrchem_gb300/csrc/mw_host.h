@@ -158,6 +158,9 @@ struct Ctx {
     std::string err;
     mw_stats last{};
     int nsm = 0;
+    void *owner = nullptr;  // the C-ABI handle holding this context
+    int live = 0;           // trees and operators created through the C ABI and not yet destroyed
+    bool closing = false;   // destroyed by the caller; released when live drops to 0
     Arena arena;
     void *h_pinned = nullptr;
     size_t pinned_bytes = 0;
@@ -251,6 +254,7 @@ void k_dot(const double *const *a, const double *const *b, const int *start, int
            cudaStream_t s);
 void k_scale(double *x, size_t n, double c, cudaStream_t s);
 double probe_fma_tflops(int fp64, int nsm, cudaStream_t s);
+double probe_mma_tflops(int kind, int nsm, cudaStream_t s);
 void k_eval(const DevBasis &b, const double *const *blocks, const int *keys, const double *pts, int npts,
             double *out, cudaStream_t s);
 

@@ -67,6 +67,11 @@ struct MulJob {
 void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st);
 void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st);
 void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats &st);
+void density(double prec, Tree &rho, const std::vector<Tree *> &orbs, const std::vector<double> &occ, bool crop_sum,
+             mw_stats &st);
+void rotate(const std::vector<Tree *> &outs, const std::vector<const Tree *> &ins, const double *U, mw_stats &st);
+void tree_save(Tree &t, const char *path);
+void tree_load(Tree &t, const char *path);
 void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st);
 void add(Tree &out, const std::vector<const Tree *> &trees, const std::vector<double> &coefs, mw_stats &st);
 

@@ -814,6 +814,68 @@ __global__ void fma_probe_kernel(T *out, int iters, T seed) {
 }
 }  // namespace
 
+namespace {
+// register-only warp MMA chains: kind 0 = m16n8k8 TF32, kind 1 = m16n8k16 BF16 (FP32 accumulate)
+__global__ void mma_probe_kernel(float *out, int iters, int kind) {
+    uint32_t a[4], b[2];
+    for (int i = 0; i < 4; i++) a[i] = 0x3c003c00u + threadIdx.x + i;
+    for (int i = 0; i < 2; i++) b[i] = 0x3c003c00u + threadIdx.x * 3 + i;
+    float c[4][4];
+    for (int j = 0; j < 4; j++)
+        for (int i = 0; i < 4; i++) c[j][i] = 0.0f;
+    if (kind == 0) {
+        for (int it = 0; it < iters; it++)
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                asm volatile(
+                    "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                    "{%0,%1,%2,%3};\n"
+                    : "+f"(c[j][0]), "+f"(c[j][1]), "+f"(c[j][2]), "+f"(c[j][3])
+                    : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+    } else {
+        for (int it = 0; it < iters; it++)
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                asm volatile(
+                    "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                    "{%0,%1,%2,%3};\n"
+                    : "+f"(c[j][0]), "+f"(c[j][1]), "+f"(c[j][2]), "+f"(c[j][3])
+                    : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+    }
+    float s = 0.0f;
+    for (int j = 0; j < 4; j++)
+        for (int i = 0; i < 4; i++) s += c[j][i];
+    if (s == -12345.0f) out[blockIdx.x] = s;
+}
+}  // namespace
+
+// Dense warp-MMA throughput (TFLOP/s, 2 flops per MAC) of the legacy mma.sync path.
+double probe_mma_tflops(int kind, int nsm, cudaStream_t s) {
+    const int threads = 256, blocks = nsm * 8, iters = 1 << 12;
+    float *out = nullptr;
+    MWG_CUDA(cudaMalloc(&out, sizeof(float) * blocks));
+    cudaEvent_t e0, e1;
+    MWG_CUDA(cudaEventCreate(&e0));
+    MWG_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        MWG_CUDA(cudaEventRecord(e0, s));
+        mma_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, kind);
+        MWG_CUDA(cudaGetLastError());
+        MWG_CUDA(cudaEventRecord(e1, s));
+        MWG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        MWG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    const double macs_per_mma = kind == 0 ? 16.0 * 8 * 8 : 16.0 * 8 * 16;
+    double flops = 2.0 * macs_per_mma * 4.0 * iters * (threads / 32.0) * blocks;
+    return flops / (best * 1e-3) / 1e12;
+}
+
 double probe_fma_tflops(int fp64, int nsm, cudaStream_t s) {
     const int threads = 256, blocks = nsm * 8, iters = fp64 ? 1 << 13 : 1 << 16;
     void *out = nullptr;

@@ -7,6 +7,7 @@
 // (density_utils.cpp:147); dot (src/qmfunctions/orbital_utils.cpp:79-82).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 
@@ -600,6 +601,57 @@ void tree_download(Tree &t, int *keys, double *coefs, unsigned char *leaf) {
         }
         if (leaf) leaf[j] = nd.child0 < 0;
     }
+}
+
+// ------------------------------------------------------------------ files
+// Tree file (checkpoint of one function tree, the role of MRCPP's saveTree in
+// orbital::save_orbitals, src/qmfunctions/orbital_utils.cpp:1218-1240):
+//   char[8] "MWGB300T", int32 version (1), int32 order, int32 basis, int32 root_scale,
+//   int32 corner[3], int32 boxes[3], int64 nnodes,
+//   int32 keys[nnodes][4] (n, lx, ly, lz), float64 coefs[nnodes][8 (order+1)^3]
+// little-endian, nodes in canonical order.
+void tree_save(Tree &t, const char *path) {
+    const Basis &b = t.ctx->basis;
+    int64_t n = t.nn();
+    std::vector<int> keys(4 * n);
+    std::vector<double> coefs((size_t)n * b.bs);
+    tree_download(t, keys.data(), coefs.data(), nullptr);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) throw Error(MW_ERR_ARG, std::string("cannot open ") + path);
+    int32_t hdr[11] = {1, b.k, b.type, b.n0, b.corner[0], b.corner[1], b.corner[2], b.boxes[0], b.boxes[1], b.boxes[2], 0};
+    bool ok = std::fwrite("MWGB300T", 1, 8, f) == 8 && std::fwrite(hdr, sizeof(int32_t), 10, f) == 10 &&
+              std::fwrite(&n, sizeof(n), 1, f) == 1 && std::fwrite(keys.data(), sizeof(int), keys.size(), f) == keys.size() &&
+              std::fwrite(coefs.data(), sizeof(double), coefs.size(), f) == coefs.size();
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) throw Error(MW_ERR_STATE, std::string("write failed: ") + path);
+}
+
+void tree_load(Tree &t, const char *path) {
+    const Basis &b = t.ctx->basis;
+    FILE *f = std::fopen(path, "rb");
+    if (!f) throw Error(MW_ERR_ARG, std::string("cannot open ") + path);
+    char magic[8];
+    int32_t hdr[10];
+    int64_t n = 0;
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, "MWGB300T", 8) == 0 &&
+              std::fread(hdr, sizeof(int32_t), 10, f) == 10 && std::fread(&n, sizeof(n), 1, f) == 1;
+    if (ok && (hdr[0] != 1 || hdr[1] != b.k || hdr[2] != b.type || hdr[3] != b.n0 || hdr[4] != b.corner[0] ||
+               hdr[5] != b.corner[1] || hdr[6] != b.corner[2] || hdr[7] != b.boxes[0] || hdr[8] != b.boxes[1] ||
+               hdr[9] != b.boxes[2] || n < 1 || n > (1LL << 31))) {
+        std::fclose(f);
+        throw Error(MW_ERR_ARG, std::string("tree file does not match this context: ") + path);
+    }
+    std::vector<int> keys;
+    std::vector<double> coefs;
+    if (ok) {
+        keys.resize(4 * n);
+        coefs.resize((size_t)n * b.bs);
+        ok = std::fread(keys.data(), sizeof(int), keys.size(), f) == keys.size() &&
+             std::fread(coefs.data(), sizeof(double), coefs.size(), f) == coefs.size();
+    }
+    std::fclose(f);
+    if (!ok) throw Error(MW_ERR_ARG, std::string("truncated or foreign tree file: ") + path);
+    tree_upload(t, (int)n, keys.data(), coefs.data(), t.ctx->arena);
 }
 
 // ------------------------------------------------------------------ grids

@@ -92,7 +92,7 @@ def test_gradient_equals_potential(engine, setup):
             d = np.linalg.norm(ca - cb)
             g = math.sqrt(a * b / (a + b))
             ex += 2 * g / math.sqrt(math.pi) if d < 1e-12 else math.erf(g * d) / d
-    assert abs(float(J) - 0.5 * ex) <= 20 * PREC * abs(0.5 * ex)
+    assert abs(float(J.detach()) - 0.5 * ex) <= 20 * PREC * abs(0.5 * ex)
 
 
 def test_centre_gradient_vs_finite_differences(engine, setup):

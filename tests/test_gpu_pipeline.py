@@ -1,0 +1,120 @@
+"""The steps either side of the apply, on the device: density build (density::compute), the
+Coulomb potential from it (CoulombPotential::setupGlobalPotential), V*phi followed by the
+Helmholtz update (QMPotential::apply + HelmholtzVector::apply), orbital rotation, and the tree
+file round trip (checkpoint)."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_values.json")))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_density_and_coulomb_reference_values(engine):
+    """tests/qmoperators/coulomb_operator.cpp:78-84 through the device-resident pipeline."""
+    ref = GOLDEN["coulomb"]
+    prec = ref["prec"]
+    mra = engine.MultiResolutionAnalysis(GOLDEN["mra"]["order"])
+    phis = [engine.project_hydrogen(prec, engine.FunctionTree(mra), *o) for o in ref["orbitals"]]
+    rho = engine.FunctionTree(mra)
+    engine.density(prec, rho, phis, [ref["occupation"]] * len(phis), crop=False)
+    assert abs(rho.integrate() - 10.0) < 1e-4
+    J = engine.FunctionTree(mra)
+    engine.apply(prec / rho.norm(), J, engine.PoissonOperator(mra, prec), rho)
+    E = ref["E_P"]
+    for i, p in enumerate(phis):
+        jp = engine.FunctionTree(mra)
+        engine.copy_grid(jp, p)
+        engine.multiply(prec, jp, 1.0, J, p)
+        v = engine.dot(p, jp)
+        assert abs(v - E["%d,%d" % (i, i)]) < 1e-5 * E["%d,%d" % (i, i)], (i, v)
+
+
+def test_density_matches_oracle(engine, oracle):
+    prec = 1e-5
+    mra, omra = engine.MultiResolutionAnalysis(7), oracle.MRA(7)
+    terms = [[(1.0, 1.2, (0.3, 0.0, 0.0), (0, 0, 0))], [(1.0, 0.8, (-0.4, 0.2, 0.0), (1, 0, 0))]]
+    ophis = [oracle.project_gauss(prec, oracle.Tree(omra), t) for t in terms]
+    phis = [engine.FunctionTree(mra).upload(*o.export()[:2]) for o in ophis]
+    rho = engine.FunctionTree(mra)
+    engine.density(prec, rho, phis, [2.0, 1.0], crop=False)
+    sq = []
+    for p in ophis:
+        r = oracle.Tree(omra)
+        oracle.copy_grid(r, p)
+        oracle.multiply(prec, r, 1.0, p, p)
+        sq.append(r)
+    orho = oracle.Tree(omra)
+    oracle.add(prec, orho, [2.0, 1.0], sq)
+    k1, c1, _ = rho.download()
+    k2, c2, _ = orho.export()
+    assert np.array_equal(k1, k2) and rel_l2(c1, c2) <= 1e-12
+
+
+def test_potential_times_orbital_then_helmholtz(engine, oracle):
+    """psi = -1/(2 pi) H_mu[V phi] on the device against the same steps in the oracle."""
+    prec, mu = 1e-5, 1.1
+    mra, omra = engine.MultiResolutionAnalysis(7), oracle.MRA(7)
+    oV = oracle.project_gauss(prec, oracle.Tree(omra), [(-2.0, 0.7, (0.0, 0.0, 0.0), (0, 0, 0))])
+    ophi = oracle.project_gauss(prec, oracle.Tree(omra), [(1.0, 1.5, (0.2, 0.1, 0.0), (0, 0, 0))])
+    V = engine.FunctionTree(mra).upload(*oV.export()[:2])
+    phi = engine.FunctionTree(mra).upload(*ophi.export()[:2])
+    vphi = engine.FunctionTree(mra)
+    engine.copy_grid(vphi, phi)
+    engine.multiply_batch(prec, [vphi], 1.0, [V], [phi])
+    out = engine.FunctionTree(mra)
+    engine.apply_batch(prec, [out], [engine.HelmholtzOperator(mra, mu, prec)], [vphi], abs_prec=True)
+    out.rescale(-1.0 / (2.0 * math.pi))
+    ovphi = oracle.Tree(omra)
+    oracle.copy_grid(ovphi, ophi)
+    oracle.multiply(prec, ovphi, 1.0, oV, ophi)
+    oout = oracle.Tree(omra)
+    oracle.apply(prec, oout, oracle.helmholtz(omra, mu, prec), ovphi, abs_prec=True)
+    oout.rescale(-1.0 / (2.0 * math.pi))
+    k1, c1, _ = out.download()
+    k2, c2, _ = oout.export()
+    assert np.array_equal(k1, k2) and rel_l2(c1, c2) <= 1e-10
+
+
+def test_rotation(engine):
+    prec = 1e-6
+    mra = engine.MultiResolutionAnalysis(7)
+    ins = [engine.project(prec, engine.FunctionTree(mra), [(1.0, a, (0.2 * i, 0.0, 0.0), (0, 0, 0))])
+           for i, a in enumerate((0.5, 2.0, 8.0))]
+    th = 0.3
+    U = np.array([[math.cos(th), math.sin(th), 0.0], [-math.sin(th), math.cos(th), 0.0], [0.0, 0.0, 1.0]])
+    outs = [engine.FunctionTree(mra) for _ in range(3)]
+    engine.rotate(outs, ins, U)
+    # orthogonal U preserves the Gram matrix
+    G_in = np.array([[engine.dot(a, b) for b in ins] for a in ins])
+    G_out = np.array([[engine.dot(a, b) for b in outs] for a in outs])
+    assert np.abs(G_out - U @ G_in @ U.T).max() < 1e-12
+    pts = np.random.default_rng(4).uniform(-1, 1, (20, 3))
+    vin = np.stack([t.evalf(pts) for t in ins])
+    vout = np.stack([t.evalf(pts) for t in outs])
+    assert np.abs(vout - U @ vin).max() < 1e-12
+
+
+def test_tree_file_roundtrip(engine, tmp_path):
+    mra = engine.MultiResolutionAnalysis(7)
+    f = engine.project(1e-6, engine.FunctionTree(mra), [(1.0, 2.0, (0.1, 0.2, 0.3), (1, 0, 0))])
+    path = str(tmp_path / "f.mwt")
+    engine.save_tree(f, path)
+    g = engine.load_tree(engine.FunctionTree(mra), path)
+    k1, c1, l1 = f.download()
+    k2, c2, l2 = g.download()
+    assert np.array_equal(k1, k2) and np.array_equal(c1, c2) and np.array_equal(l1, l2)
+    other = engine.MultiResolutionAnalysis(5)
+    with pytest.raises(engine.MWError):
+        engine.load_tree(engine.FunctionTree(other), path)
+    with open(path, "r+b") as fh:
+        fh.truncate(100)
+    with pytest.raises(engine.MWError):
+        engine.load_tree(engine.FunctionTree(mra), path)
