@@ -116,6 +116,14 @@ int mw_copy_func(mw_tree out, mw_tree inp);
 int mw_crop(mw_tree t, double prec, int abs_prec);
 /* mrcpp::dot (src/qmfunctions/orbital_utils.cpp:79-82) */
 int mw_dot(mw_tree a, mw_tree b, double *out);
+/* The same inner product as mw_dot, for callers that cannot allocate at the moment they need it
+ * (device memory held by another runtime's caching allocator; code that must not let cudaMalloc /
+ * cudaFree synchronise the device).  No counterpart in the reference.  Allocates nothing: the
+ * node-pair lists and partial sums live in a fixed 1 MiB device array that every GPU loading this
+ * library holds until exit, so at most 32768 nodes common to both trees (MW_ERR_ARG beyond that).
+ * All calls share that array: calls that overlap on the GPU or across host threads race.  The
+ * first call on each device looks up the array's address; make it before any stream capture. */
+int mw_dot_noalloc(mw_tree a, mw_tree b, double *out);
 
 /* ---- operators (src/driver.cpp:1131,1283; src/scf_solver/HelmholtzVector.cpp:144) ---- */
 int mw_op_create_poisson(mw_ctx ctx, double prec, mw_op *out);

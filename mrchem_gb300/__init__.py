@@ -68,7 +68,7 @@ EXPORTS = [
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
     "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
-    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak",
+    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc",
 ]
 
 
@@ -108,6 +108,7 @@ def load_library(path=None):
         "mw_copy_func": [P, P],
         "mw_crop": [P, D, I],
         "mw_dot": [P, P, dp],
+        "mw_dot_noalloc": [P, P, dp],
         "mw_op_create_poisson": [P, D, pp],
         "mw_op_create_helmholtz": [P, D, D, pp],
         "mw_op_destroy": [P],
@@ -514,6 +515,17 @@ def dot(a, b):
     """mrcpp::dot(a, b) = <a|b>."""
     v = C.c_double()
     _check(_lib.mw_dot(a.ptr, b.ptr, C.byref(v)), a.mra.ptr)
+    return v.value
+
+
+def dot_noalloc(a, b):
+    """<a|b> without allocating anything, for callers that cannot allocate GPU memory at that point.
+
+    Uses a fixed 1 MiB device array held for the life of the process: at most 32768 nodes common
+    to both trees; calls that overlap race on that array.
+    """
+    v = C.c_double()
+    _check(_lib.mw_dot_noalloc(a.ptr, b.ptr, C.byref(v)), a.mra.ptr)
     return v.value
 
 

@@ -297,6 +297,14 @@ int mw_dot(mw_tree a, mw_tree b, double *out) {
     });
 }
 
+int mw_dot_noalloc(mw_tree a, mw_tree b, double *out) {
+    if (!a || !b || !out) return MW_ERR_ARG;
+    return guard(ctx_of(a), [&] {
+        check_same(a->tree, b->tree);
+        *out = mwg::dot_noalloc(a->tree, b->tree);
+    });
+}
+
 // ---------------------------------------------------------------- operators
 static int op_create(mw_ctx c, int kind, double mu, double prec, mw_op *out) {
     if (!c || !out || !(prec > 0.0) || prec >= 1.0) return MW_ERR_ARG;

@@ -70,6 +70,7 @@ void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats 
 void density(double prec, Tree &rho, const std::vector<Tree *> &orbs, const std::vector<double> &occ, bool crop_sum,
              mw_stats &st);
 void rotate(const std::vector<Tree *> &outs, const std::vector<const Tree *> &ins, const double *U, mw_stats &st);
+double dot_noalloc(const Tree &a, const Tree &b);
 void tree_save(Tree &t, const char *path);
 void tree_load(Tree &t, const char *path);
 void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st);
