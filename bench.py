@@ -206,9 +206,20 @@ def run(args):
     # plain FP64 GPU apply of the same batch: the baseline of the metric and the error reference
     fp64_ms, st64 = timed("fp64", args.fp64_steps)
     fp64_s = fp64_ms / 1e3
-    ref = [o.download()[1] for o in outs]
+    ref = [mw.FunctionTree(mra) for _ in outs]
+    for r, o in zip(ref, outs):
+        mw.add(-1.0, r, [(1.0, o)])  # copy of the FP64 result
+
+    def rel_err(a, r):
+        """relative L2 norm of a - r, on the union grid (the grids may differ)"""
+        d = mw.FunctionTree(mra)
+        mw.add(-1.0, d, [(1.0, a), (-1.0, r)])
+        return d.norm() / r.norm()
+
     near_ms, st_near = timed("mixed-near64", 1)
-    near_err = max(float(np.linalg.norm(o.download()[1] - r) / np.linalg.norm(r)) for o, r in zip(outs, ref))
+    near_err = max(rel_err(o, r) for o, r in zip(outs, ref))
+    f32_ms, st_f32 = timed("mixed-fp32", 1)
+    f32_err = max(rel_err(o, r) for o, r in zip(outs, ref))
 
     for _ in range(args.warmup):
         step("mixed", outs)
@@ -223,10 +234,7 @@ def run(args):
         barrier()
     ms = start.elapsed_time(end) / args.steps
     nodes = stats[-1]["out_nodes"]
-    errs = []
-    for o, r in zip(outs, ref):
-        c = o.download()[1]
-        errs.append(float(np.linalg.norm(c - r) / np.linalg.norm(r)) if c.shape == r.shape else float("inf"))
+    errs = [rel_err(o, r) for o, r in zip(outs, ref)]
     local_v = nodes / (ms / 1e3)
     t_max = ms
     if world > 1:
@@ -259,20 +267,26 @@ def run(args):
     st = stats[-1]
     fp64_tf = mra.probe_fma_peak(True)
     fp32_tf = mra.probe_fma_peak(False)
+    tf32_tf = mra.probe_mma_peak("tf32")
 
-    def roof(flops, ms, peak, kernel):
+    def roof(flops, ms, peak, kernel, bound, source):
         ach = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
-        return {"bound": "fp64-pipe" if "double" in kernel else "fp32-pipe", "achieved": ach, "peak": peak,
-                "unit": "TFLOP/s", "frac": ach / peak if peak else None, "traffic": None, "kernel": kernel,
-                "peak_source": "probed FMA throughput of this GPU (mw_probe_fma_peak); MEASURED_PEAKS.json "
-                               "holds no FP64/FP32 figure"}
+        return {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak if peak else None,
+                "traffic": None, "kernel": kernel, "kernel_ms_per_step": ms, "peak_source": source}
 
-    roofline = roof(st["flops_fp64"], st["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>")
-    roofline_fp32 = roof(st["flops_fp32"], st["kernel_ms_fp32"], fp32_tf, "apply_kernel<float,10>")
+    fma_src = "probed FMA throughput of this GPU (mw_probe_fma_peak); MEASURED_PEAKS.json holds no FP64/FP32 figure"
+    mma_src = ("probed dense m16n8k8 TF32 warp-MMA throughput of this GPU (mw_probe_mma_peak); "
+               "MEASURED_PEAKS.json holds no TF32 figure")
+    roofs = {
+        "fp64": roof(st["flops_fp64"], st["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
+        "fp32": roof(st["flops_fp32"], st["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src),
+        "tf32": roof(st["flops_tf32"], st["kernel_ms_tf32"], tf32_tf, "apply_tc_kernel<10>", "tensor", mma_src),
+    }
+    dominant = max(roofs, key=lambda k: roofs[k]["kernel_ms_per_step"])
     line = {
         "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64+f32+tf32", "data": "synthetic",
         "config": {"workload": "helmholtz-batch16-k9-prec1e-6", "orbitals": NORB, "order": ORDER, "prec": PREC,
                    "basis": "interpolating", "box": "[-32,32]^3", "input_nodes": in_nodes,
                    "output_nodes": nodes, "l2": "inputs larger than L2 (%.1f GB of FP64 blocks)"
@@ -284,16 +298,19 @@ def run(args):
                             "ms_per_step": near_ms, "items_fp64": st_near["items_fp64"],
                             "items_fp32": st_near["items_fp32"], "rel_l2_vs_fp64_max": near_err,
                             "policy": "every |l|_inf <= 1 item kept in FP64"},
+        "mixed_fp32": {"value": st_f32["out_nodes"] * world / (f32_ms / 1e3), "unit": "nodes/s",
+                       "ms_per_step": f32_ms, "items_fp64": st_f32["items_fp64"], "items_fp32": st_f32["items_fp32"],
+                       "rel_l2_vs_fp64_max": f32_err, "policy": "FP64 / FP32 tiers only (no tensor cores)"},
         "rel_l2_vs_fp64_max": max(errs),
-        "items": {"total": st["items"], "fp64": st["items_fp64"], "fp32": st["items_fp32"]},
+        "items": {"total": st["items"], "fp64": st["items_fp64"], "fp32": st["items_fp32"], "tf32": st["items_tf32"]},
         "kernel_ms_per_step": st["kernel_ms"], "host_ms_per_step": st["host_ms"],
         "host_breakdown_ms": {"enumerate": st["host_enum_ms"], "items": st["host_items_ms"],
                               "wait_level": st["host_wait_ms"], "kernel_fp64": st["kernel_ms_fp64"],
-                              "kernel_fp32": st["kernel_ms_fp32"]},
+                              "kernel_fp32": st["kernel_ms_fp32"], "kernel_tf32": st["kernel_ms_tf32"]},
         "gpu_launches": int(st["launches"]),
         "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": roofline,
-        "roofline_fp32": roofline_fp32,
+        "roofline": dict(roofs[dominant], tier=dominant),
+        "roofline_tiers": roofs,
         "clocks": clk.summary(),
     }
     line["speedup_mixed_vs_fp64"] = (nodes / (ms / 1e3)) / (st64["out_nodes"] / fp64_s)

@@ -38,8 +38,12 @@ extern "C" {
 
 /* precision modes of mw_apply / mw_apply_batch */
 #define MW_PREC_FP64 0   /* every contraction in FP64 */
-#define MW_PREC_MIXED 1  /* norm-tiered: FP64 when the item's bound b > 1e5 x screening threshold, else FP32 */
+/* norm-tiered by the item's bound b against the screening threshold tau: FP64 when b > 2e6 tau,
+ * TF32 tensor cores (FP32 accumulation) when b <= 2e3 tau below the root scale, FP32 CUDA cores
+ * otherwise */
+#define MW_PREC_MIXED 1
 #define MW_PREC_MIXED_NEARFP64 2  /* as MW_PREC_MIXED, and every item with |l|_inf <= 1 in FP64 */
+#define MW_PREC_MIXED_FP32 3      /* as MW_PREC_MIXED without the tensor-core tier: FP64 or FP32 only */
 
 typedef struct mw_ctx_s *mw_ctx;
 typedef struct mw_tree_s *mw_tree;
@@ -59,7 +63,7 @@ typedef struct {
     long long items;         /* (output node, input node, term) contractions */
     long long items_fp64;    /* ... of which in FP64 */
     long long items_fp32;    /* ... in FP32 */
-    long long items_bf16;    /* ... in BF16 tensor-core */
+    long long items_tf32;    /* ... in TF32 on the tensor cores */
     long long generated;     /* generated input nodes */
     long long levels;        /* refinement iterations */
     long long launches;      /* kernels launched */
@@ -75,6 +79,8 @@ typedef struct {
     double host_enum_ms;     /* host: candidate enumeration (screening bounds, lookups) */
     double host_items_ms;    /* host: generation requests, exact screening, tiers, item lists */
     double host_wait_ms;     /* host: waiting for the level's kernels and norm downloads */
+    double flops_tf32;       /* algorithmic flops of the TF32 tier */
+    double kernel_ms_tf32;   /* CUDA-event time of the TF32 contraction launches */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */

@@ -29,7 +29,9 @@ MW_OK = 0
 PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_MIXED_NEARFP64 = 2
-_PREC = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "mixed-near64": PREC_MIXED_NEARFP64}
+PREC_MIXED_FP32 = 3
+_PREC = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "mixed-near64": PREC_MIXED_NEARFP64,
+         "mixed-fp32": PREC_MIXED_FP32}
 
 
 class MWError(RuntimeError):
@@ -47,12 +49,13 @@ class GTerm(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("out_nodes", C.c_longlong), ("items", C.c_longlong), ("items_fp64", C.c_longlong),
-                ("items_fp32", C.c_longlong), ("items_bf16", C.c_longlong), ("generated", C.c_longlong),
+                ("items_fp32", C.c_longlong), ("items_tf32", C.c_longlong), ("generated", C.c_longlong),
                 ("levels", C.c_longlong), ("launches", C.c_longlong), ("flops", C.c_double),
                 ("flops_issued", C.c_double), ("bytes", C.c_double), ("kernel_ms", C.c_double),
                 ("host_ms", C.c_double), ("flops_fp64", C.c_double), ("flops_fp32", C.c_double),
                 ("kernel_ms_fp64", C.c_double), ("kernel_ms_fp32", C.c_double), ("host_enum_ms", C.c_double),
-                ("host_items_ms", C.c_double), ("host_wait_ms", C.c_double)]
+                ("host_items_ms", C.c_double), ("host_wait_ms", C.c_double), ("flops_tf32", C.c_double),
+                ("kernel_ms_tf32", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

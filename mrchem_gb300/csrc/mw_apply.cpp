@@ -33,6 +33,15 @@ namespace {
 // b <= TIER_FP64 * screening threshold = 2e4 * thr(o) therefore err by at most 0.08 thr(o),
 // a tenth of the refinement tolerance; larger items run in FP64.
 constexpr double TIER_FP64 = 2e6;
+// An item on the TF32 tensor cores (input values, operator blocks and the two intermediates
+// rounded to TF32, unit roundoff 2^-11; FP32 accumulation) is off by at most about
+// 6 * 2^-11 b = 2.9e-3 b.  Items with b <= TIER_TF32 * screening threshold err by at most
+// 0.06 thr(o), the same per-item bound as the FP32 tier.  Root-scale items never take this tier:
+// nothing is screened there and, with precision-steering trees, the threshold is divided by the
+// small weight of the large root boxes, so many items just under it would add up to more than
+// prec relative to a small output.
+constexpr double TIER_TF32 = 2e3;
+constexpr int NTIER = 3;
 constexpr double BOUND_PRUNE = 8.0 * 2.8285;  // (sum_f |in_f|) / |block| <= sqrt(8); 8 output components
 
 double split_thr(double prec, double R, int n) { return prec * R * std::pow(2.0, -0.5 * (n + 1)); }
@@ -95,7 +104,7 @@ struct Cand {
     int t, lx, ly, lz;
     int src;   // input node index, or generated slot
     int gen;   // 1: src is a generated slot (ancestor index before generation)
-    int tier;  // after screening: -1 skipped, 0 FP64, 1 FP32
+    int tier;  // after screening: -1 skipped, 0 FP64, 1 FP32, 2 TF32 tensor cores
 };
 
 struct JobState {
@@ -204,7 +213,8 @@ struct LevelItems {
     }
 };
 
-void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int fp32, mw_stats &st) {
+// tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores
+void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int tier, mw_stats &st) {
     int nn = (int)li.out.size();
     if (nn == 0) return;
     // nodes in decreasing item count (longest first) for the persistent grid's dynamic
@@ -245,7 +255,10 @@ void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int fp32, mw_sta
     L.az = (const void *const *)pk.ptr(6);
     L.coef = (const double *)pk.ptr(7);
     L.counter = counter;
-    k_apply(ctx.dbasis, L, fp32, ctx.nsm, ctx.stream);
+    if (tier == 2)
+        k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
+    else
+        k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
     st.launches++;
 }
 
@@ -259,13 +272,12 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     const double K4 = (double)K * K * K * K;
     const bool mixed = precision_mode != MW_PREC_FP64;
     const bool near_fp64 = precision_mode == MW_PREC_MIXED_NEARFP64;
+    const bool tensor = mixed && precision_mode != MW_PREC_MIXED_FP32;
     auto t_start = std::chrono::steady_clock::now();
     Arena &arena = ctx.arena;
     arena.reset();
-    cudaEvent_t ev0, evm, ev1;
-    MWG_CUDA(cudaEventCreate(&ev0));
-    MWG_CUDA(cudaEventCreate(&evm));
-    MWG_CUDA(cudaEventCreate(&ev1));
+    cudaEvent_t ev[NTIER + 1];
+    for (auto &e : ev) MWG_CUDA(cudaEventCreate(&e));
     float kernel_ms = 0.0f;
 
     std::vector<JobState> js(jobs.size());
@@ -302,7 +314,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             if (s.job->out->nodes[i].n == n) s.work.push_back(i);
     };
 
-    LevelItems li64, li32;
+    LevelItems lt[NTIER];
     int level = 0;
     while (true) {
         const int n = b.n0 + level, sidx = level;
@@ -386,9 +398,11 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         for (size_t j = 0; j < js.size(); j++)
             for (size_t w = 0; w < js[j].work.size(); w++) nodes_flat.push_back({(int)j, (int)w});
         const long NN = (long)nodes_flat.size();
-        std::vector<long long> cnt64(NN + 1, 0), cnt32(NN + 1, 0);
-        long long pairs_tot = 0, pairs64 = 0, pairs32 = 0;
-#pragma omp parallel for schedule(dynamic, 4) reduction(+ : pairs_tot, pairs64, pairs32)
+        // per tier (0 FP64, 1 FP32, 2 TF32): per-node item counts, then prefix sums
+        std::vector<long long> cnt[NTIER];
+        for (int k = 0; k < NTIER; k++) cnt[k].assign(NN + 1, 0);
+        long long pairs_tot = 0, pairs_t0 = 0, pairs_t1 = 0, pairs_t2 = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : pairs_tot, pairs_t0, pairs_t1, pairs_t2)
         for (long q = 0; q < NN; q++) {
             JobState &s = js[nodes_flat[q].first];
             int w = nodes_flat[q].second;
@@ -400,43 +414,47 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             double tthr = !root ? thr
                           : s.job->abs_prec ? SCREEN_FAC * split_thr(s.job->prec, 1.0, n) / std::max(s.wgt[w], 1e-300)
                                             : -1.0;
-            long long c64 = 0, c32 = 0;
-            for (Cand &c : s.cand[w]) {
-                const double *cn = c.gen ? &s.gcn[8 * (size_t)c.src] : &inp.cn[8 * (size_t)c.src];
-                const double *nx = op.norm(c.t, sidx, c.lx), *ny = op.norm(c.t, sidx, c.ly),
-                             *nz = op.norm(c.t, sidx, c.lz);
+            long long c[NTIER] = {0, 0, 0};
+            for (Cand &cd : s.cand[w]) {
+                const double *cn = cd.gen ? &s.gcn[8 * (size_t)cd.src] : &inp.cn[8 * (size_t)cd.src];
+                const double *nx = op.norm(cd.t, sidx, cd.lx), *ny = op.norm(cd.t, sidx, cd.ly),
+                             *nz = op.norm(cd.t, sidx, cd.lz);
                 double bd = item_bound(nx, ny, nz, cn, root);
                 if (!root && bd < thr) {
-                    c.tier = -1;
+                    cd.tier = -1;
                     continue;
                 }
                 int np_ = item_pairs(nx, ny, nz, cn, root);
                 pairs_tot += np_;
-                bool near = std::max(std::abs(c.lx), std::max(std::abs(c.ly), std::abs(c.lz))) <= 1;
-                bool use64 = !mixed || tthr < 0.0 || bd > TIER_FP64 * tthr || (near_fp64 && near);
-                c.tier = use64 ? 0 : 1;
-                if (use64) {
-                    c64++;
-                    pairs64 += np_;
-                } else {
-                    c32++;
-                    pairs32 += np_;
-                }
+                bool near = std::max(std::abs(cd.lx), std::max(std::abs(cd.ly), std::abs(cd.lz))) <= 1;
+                int tier;
+                if (!mixed || tthr < 0.0 || bd > TIER_FP64 * tthr || (near_fp64 && near))
+                    tier = 0;
+                else if (tensor && !root && bd <= TIER_TF32 * tthr)
+                    tier = 2;
+                else
+                    tier = 1;
+                cd.tier = tier;
+                c[tier]++;
+                (tier == 0 ? pairs_t0 : tier == 1 ? pairs_t1 : pairs_t2) += np_;
             }
-            cnt64[q + 1] = c64;
-            cnt32[q + 1] = c32;
+            for (int k = 0; k < NTIER; k++) cnt[k][q + 1] = c[k];
         }
-        std::vector<long> slot32(NN, -1);  // node position in the FP32 launch
-        long nn32 = 0;
+        // FP64 launch: every node (it writes the block); other tiers: nodes that have items there
+        std::vector<long> slot[NTIER];
+        long nnt[NTIER] = {NN, 0, 0};
+        for (int k = 0; k < NTIER; k++) slot[k].assign(NN, -1);
         for (long q = 0; q < NN; q++) {
-            if (cnt32[q + 1] > 0) slot32[q] = nn32++;
-            cnt64[q + 1] += cnt64[q];
-            cnt32[q + 1] += cnt32[q];
+            slot[0][q] = q;
+            for (int k = 1; k < NTIER; k++)
+                if (cnt[k][q + 1] > 0) slot[k][q] = nnt[k]++;
+            for (int k = 0; k < NTIER; k++) cnt[k][q + 1] += cnt[k][q];
         }
-        const long long n64 = cnt64[NN], n32 = cnt32[NN];
-        li64.resize(NN, n64);
-        li32.resize(nn32, n32);
-        li32.begin[0] = 0;
+        long long ntot[NTIER];
+        for (int k = 0; k < NTIER; k++) {
+            ntot[k] = cnt[k][NN];
+            lt[k].resize(nnt[k], ntot[k]);
+        }
 #pragma omp parallel for schedule(dynamic, 4)
         for (long q = 0; q < NN; q++) {
             JobState &s = js[nodes_flat[q].first];
@@ -444,48 +462,52 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             const Tree &inp = *s.job->inp;
             const Oper &op = *s.job->op;
             double *ob = s.job->out->block(s.work[w]);
-            li64.out[q] = ob;
-            li64.begin[q + 1] = cnt64[q + 1];
-            if (slot32[q] >= 0) {
-                li32.out[slot32[q]] = ob;
-                li32.begin[slot32[q] + 1] = cnt32[q + 1];
-            }
-            long long p64 = cnt64[q], p32 = cnt32[q];
-            for (const Cand &c : s.cand[w]) {
-                if (c.tier < 0) continue;
-                long bxi = op.block_index(c.t, sidx, c.lx), byi = op.block_index(c.t, sidx, c.ly),
-                     bzi = op.block_index(c.t, sidx, c.lz);
-                if (c.tier == 0) {
-                    li64.in[p64] = c.gen ? (const void *)(s.gbase + (size_t)c.src * bs) : (const void *)inp.block(c.src);
-                    li64.ax[p64] = op.d_blocks + (size_t)bxi * bsz;
-                    li64.ay[p64] = op.d_blocks + (size_t)byi * bsz;
-                    li64.az[p64] = op.d_blocks + (size_t)bzi * bsz;
-                    li64.coef[p64] = op.c[c.t];
-                    p64++;
-                } else {
-                    li32.in[p32] = c.gen ? (const void *)(s.gbase32 + (size_t)c.src * bs)
-                                         : (const void *)(inp.d_coefs32 + (size_t)c.src * bs);
-                    li32.ax[p32] = op.d_blocks32 + (size_t)bxi * bsz;
-                    li32.ay[p32] = op.d_blocks32 + (size_t)byi * bsz;
-                    li32.az[p32] = op.d_blocks32 + (size_t)bzi * bsz;
-                    li32.coef[p32] = op.c[c.t];
-                    p32++;
+            long long p[NTIER];
+            for (int k = 0; k < NTIER; k++) {
+                p[k] = cnt[k][q];
+                if (slot[k][q] >= 0) {
+                    lt[k].out[slot[k][q]] = ob;
+                    lt[k].begin[slot[k][q] + 1] = cnt[k][q + 1];
                 }
             }
+            for (const Cand &cd : s.cand[w]) {
+                if (cd.tier < 0) continue;
+                long bxi = op.block_index(cd.t, sidx, cd.lx), byi = op.block_index(cd.t, sidx, cd.ly),
+                     bzi = op.block_index(cd.t, sidx, cd.lz);
+                LevelItems &T = lt[cd.tier];
+                long long &pi = p[cd.tier];
+                if (cd.tier == 0) {
+                    T.in[pi] = cd.gen ? (const void *)(s.gbase + (size_t)cd.src * bs) : (const void *)inp.block(cd.src);
+                    T.ax[pi] = op.d_blocks + (size_t)bxi * bsz;
+                    T.ay[pi] = op.d_blocks + (size_t)byi * bsz;
+                    T.az[pi] = op.d_blocks + (size_t)bzi * bsz;
+                } else {
+                    // FP32 and TF32 tiers read the FP32 cube-order shadows and the FP32 operator blocks
+                    T.in[pi] = cd.gen ? (const void *)(s.gbase32 + (size_t)cd.src * bs)
+                                      : (const void *)(inp.d_coefs32 + (size_t)cd.src * bs);
+                    T.ax[pi] = op.d_blocks32 + (size_t)bxi * bsz;
+                    T.ay[pi] = op.d_blocks32 + (size_t)byi * bsz;
+                    T.az[pi] = op.d_blocks32 + (size_t)bzi * bsz;
+                }
+                T.coef[pi] = op.c[cd.t];
+                pi++;
+            }
         }
-        st.items += n64 + n32;
-        st.items_fp64 += n64;
-        st.items_fp32 += n32;
+        st.items += ntot[0] + ntot[1] + ntot[2];
+        st.items_fp64 += ntot[0];
+        st.items_fp32 += ntot[1];
+        st.items_tf32 += ntot[2];
         st.flops += 6.0 * K4 * (double)pairs_tot;
-        st.flops_issued += 96.0 * K4 * (double)(n64 + n32);
-        st.flops_fp64 += 6.0 * K4 * (double)pairs64;
-        st.flops_fp32 += 6.0 * K4 * (double)pairs32;
+        st.flops_issued += 96.0 * K4 * (double)(ntot[0] + ntot[1] + ntot[2]);
+        st.flops_fp64 += 6.0 * K4 * (double)pairs_t0;
+        st.flops_fp32 += 6.0 * K4 * (double)pairs_t1;
+        st.flops_tf32 += 6.0 * K4 * (double)pairs_t2;
         st.host_items_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tB).count();
-        MWG_CUDA(cudaEventRecord(ev0, ctx.stream));
-        launch_tier(ctx, li64, root, true, 0, st);
-        MWG_CUDA(cudaEventRecord(evm, ctx.stream));
-        launch_tier(ctx, li32, root, false, 1, st);
-        MWG_CUDA(cudaEventRecord(ev1, ctx.stream));
+        MWG_CUDA(cudaEventRecord(ev[0], ctx.stream));
+        for (int k = 0; k < NTIER; k++) {
+            launch_tier(ctx, lt[k], root, k == 0, k, st);
+            MWG_CUDA(cudaEventRecord(ev[k + 1], ctx.stream));
+        }
         // norms of the level's output nodes
         std::vector<double *> bl, cnp;
         for (auto &s : js)
@@ -509,12 +531,12 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         auto tW = std::chrono::steady_clock::now();
         ctx.sync();
         st.host_wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tW).count();
-        float ms = 0.0f, ms64 = 0.0f;
-        MWG_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-        MWG_CUDA(cudaEventElapsedTime(&ms64, ev0, evm));
-        kernel_ms += ms;
-        st.kernel_ms_fp64 += ms64;
-        st.kernel_ms_fp32 += ms - ms64;
+        float ms_t[NTIER];
+        for (int k = 0; k < NTIER; k++) MWG_CUDA(cudaEventElapsedTime(&ms_t[k], ev[k], ev[k + 1]));
+        kernel_ms += ms_t[0] + ms_t[1] + ms_t[2];
+        st.kernel_ms_fp64 += ms_t[0];
+        st.kernel_ms_fp32 += ms_t[1];
+        st.kernel_ms_tf32 += ms_t[2];
         // refinement
         for (auto &s : js) {
             Tree &out = *s.job->out;
@@ -609,9 +631,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     }
     ctx.sync();
     arena.reset();
-    cudaEventDestroy(ev0);
-    cudaEventDestroy(evm);
-    cudaEventDestroy(ev1);
+    for (auto &e : ev) cudaEventDestroy(e);
     st.kernel_ms += kernel_ms;
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }

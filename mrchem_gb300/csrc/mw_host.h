@@ -241,6 +241,8 @@ struct AddTask {
 void k_project(const DevBasis &b, const ProjFunc &f, const ProjTask *tasks, int n, cudaStream_t s);
 void k_generate(const DevBasis &b, const GenTask *tasks, int n, cudaStream_t s);
 void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s);
+// TF32 tensor-core tier: FP32 cube-order input blocks and FP32 operator blocks, as the FP32 tier
+void k_apply_tc(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s);
 void k_norms(const DevBasis &b, double *const *blocks, double *const *cn, int n, cudaStream_t s);
 void k_topdown(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s);
 void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s);

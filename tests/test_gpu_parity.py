@@ -167,7 +167,7 @@ def test_mixed_precision_close_to_fp64(engine, k7):
     v64, vmx = engine.FunctionTree(mra), engine.FunctionTree(mra)
     engine.apply(prec, v64, P, rho, precision="fp64")
     st = engine.apply(prec, vmx, P, rho, precision="mixed")
-    assert st["items_fp32"] > 0
+    assert st["items_fp32"] + st["items_tf32"] > 0
     k1, c1, _ = v64.download()
     k2, c2, _ = vmx.download()
     assert np.array_equal(k1, k2)

@@ -1,0 +1,77 @@
+"""The TF32 tensor-core tier of the norm-tiered apply (precision "mixed").
+
+Items whose screening bound b is at most 2e3 x the screening threshold run on the tensor cores
+(operands rounded to TF32, FP32 accumulation), so each is off by at most about 3e-3 b.  Checked:
+- every basis order (k = 3..9, both tile tails of the kernel) with absolute and relative
+  precision: the tier is used, and the result is within prec of the FP64 apply (relative L2 of
+  the difference tree, computed on the union grid);
+- the error stays within a small multiple of the FP32-only tiering ("mixed-fp32");
+- a function with only wavelet content below the root scale still excludes the scaling-scaling
+  path exactly (a wrong exclusion gives an O(1) error);
+- reruns are bit-identical.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GAUSS = [(1.0, 3.0, (0.15, -0.1, 0.05), (0, 0, 0)), (0.6, 12.0, (-0.4, 0.3, 0.2), (1, 0, 0)),
+         (0.3, 40.0, (0.5, 0.25, -0.35), (0, 1, 1))]
+
+
+def diff_norm(engine, mra, a, b):
+    d = engine.FunctionTree(mra)
+    engine.add(-1.0, d, [(1.0, a), (-1.0, b)])
+    return d.norm()
+
+
+def run(engine, mra, op, inp, prec, precision, abs_prec):
+    out = engine.FunctionTree(mra)
+    st = engine.apply(prec, out, op, inp, abs_prec=abs_prec, precision=precision)
+    return out, st
+
+
+@pytest.mark.parametrize("order", [3, 4, 5, 6, 7, 8, 9])
+@pytest.mark.parametrize("abs_prec", [True, False])
+def test_tensor_tier_every_order(engine, order, abs_prec):
+    prec = 1e-5
+    mra = engine.MultiResolutionAnalysis(order)
+    f = engine.project(prec, engine.FunctionTree(mra), GAUSS, abs_prec=True)
+    f.rescale(1.0 / f.norm())
+    H = engine.HelmholtzOperator(mra, 1.3, prec)
+    v64, s64 = run(engine, mra, H, f, prec, "fp64", abs_prec)
+    vtc, stc = run(engine, mra, H, f, prec, "mixed", abs_prec)
+    v32, s32 = run(engine, mra, H, f, prec, "mixed-fp32", abs_prec)
+    assert s64["items_tf32"] == 0 and s32["items_tf32"] == 0
+    assert stc["items_tf32"] > 0
+    n64 = v64.norm()
+    e_tc = diff_norm(engine, mra, vtc, v64) / n64
+    e_32 = diff_norm(engine, mra, v32, v64) / n64
+    assert e_tc <= prec, (e_tc, stc)
+    assert e_32 <= prec
+    assert e_tc <= max(300.0 * e_32, 0.05 * prec), (e_tc, e_32)
+
+
+def test_tensor_tier_poisson_wavelet_input(engine):
+    # input: the difference of two nearby Gaussians (little scaling content at coarse scales)
+    prec = 1e-6
+    mra = engine.MultiResolutionAnalysis(7)
+    terms = [(1.0, 20.0, (0.0, 0.0, 0.0), (0, 0, 0)), (-1.0, 20.0, (0.02, -0.01, 0.015), (0, 0, 0))]
+    f = engine.project(prec, engine.FunctionTree(mra), terms, abs_prec=True)
+    P = engine.PoissonOperator(mra, prec)
+    v64, _ = run(engine, mra, P, f, prec, "fp64", True)
+    vtc, stc = run(engine, mra, P, f, prec, "mixed", True)
+    assert stc["items_tf32"] > 0
+    assert diff_norm(engine, mra, vtc, v64) <= prec * max(v64.norm(), 1.0)
+
+
+def test_tensor_tier_rerun_bit_identical(engine):
+    prec = 1e-5
+    mra = engine.MultiResolutionAnalysis(9)
+    f = engine.project(prec, engine.FunctionTree(mra), GAUSS, abs_prec=True)
+    H = engine.HelmholtzOperator(mra, 0.7, prec)
+    a, _ = run(engine, mra, H, f, prec, "mixed", True)
+    b, _ = run(engine, mra, H, f, prec, "mixed", True)
+    ka, ca, _ = a.download()
+    kb, cb, _ = b.download()
+    assert np.array_equal(ka, kb) and np.array_equal(ca, cb)

@@ -76,7 +76,7 @@ def test_config3_mixed_error_per_orbital(engine, prec):
     omx = [engine.FunctionTree(mra) for _ in phis]
     engine.apply_batch([prec] * 16, o64, ops, phis, abs_prec=True, precision="fp64")
     st = engine.apply_batch([prec] * 16, omx, ops, phis, abs_prec=True, precision="mixed")
-    assert st["items_fp32"] > st["items_fp64"]
+    assert st["items_fp32"] + st["items_tf32"] > st["items_fp64"]
     for a, b in zip(omx, o64):
         ka, ca, _ = a.download()
         kb, cb, _ = b.download()
@@ -108,11 +108,18 @@ def test_config4_exchange_pairs(engine, oracle):
     engine.apply_batch(prec_p, v64, [P] * 528, rhos, prec_trees=pt, abs_prec=True, precision="fp64")
     st = engine.apply_batch(prec_p, vmx, [P] * 528, rhos, prec_trees=pt, abs_prec=True, precision="mixed")
     assert st["out_nodes"] > 528 * 8
+    # The applies run at absolute precision: the tiering bounds each item's error against the
+    # absolute screening threshold, so the difference to FP64 is bounded by prec_p in absolute
+    # terms, and relative to the output where the output's norm exceeds 1.  Pairs of distant
+    # orbitals have outputs of norm << 1, where a relative bound would be stricter than the call's.
+    worst = 0.0
     for a, b in zip(vmx, v64):
         ka, ca, _ = a.download()
         kb, cb, _ = b.download()
         assert np.array_equal(ka, kb)
-        assert rel_l2(ca, cb) <= prec_p
+        err = float(np.linalg.norm(ca - cb))
+        worst = max(worst, err / max(float(np.linalg.norm(cb)), 1.0))
+    assert worst <= prec_p, worst
     # one pair against the oracle, from the same input trees
     omra = oracle.MRA(order)
     i, j = pairs[37]
