@@ -213,10 +213,11 @@ struct LevelItems {
     }
 };
 
-// tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores
-void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int tier, mw_stats &st) {
+// tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores.  Returns the pinned host copy of the
+// launch's status word (read it after the stream has been synchronised), or nullptr.
+int *launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int tier, mw_stats &st) {
     int nn = (int)li.out.size();
-    if (nn == 0) return;
+    if (nn == 0) return nullptr;
     // nodes in decreasing item count (longest first) for the persistent grid's dynamic
     // scheduler; each node's own items keep their order, so results do not change
     std::vector<int> ord(nn);
@@ -241,7 +242,7 @@ void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int tier, mw_sta
     pk.add(li.az.data(), li.az.size() * sizeof(void *));
     pk.add(li.coef.data(), li.coef.size() * sizeof(double));
     pk.ship(ctx, ctx.arena);
-    int *counter = (int *)ctx.arena.alloc(sizeof(int));
+    int *counter = (int *)ctx.arena.alloc(2 * sizeof(int));
     ApplyLaunch L;
     L.nnodes = nn;
     L.root = root ? 1 : 0;
@@ -255,11 +256,22 @@ void launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int tier, mw_sta
     L.az = (const void *const *)pk.ptr(6);
     L.coef = (const double *)pk.ptr(7);
     L.counter = counter;
-    if (tier == 2)
-        k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
-    else
-        k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
+    L.status = counter + 1;
     st.launches++;
+    if (tier != 2) {
+        k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
+        return nullptr;
+    }
+    k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
+    int *hs = (int *)ctx.arena.halloc(sizeof(int));
+    *hs = 0;
+    MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+    return hs;
+}
+
+void check_status(const int *hs) {
+    if (hs && *hs != 0)
+        throw Error(MW_ERR_TIMEOUT, "apply: a bounded wait for an asynchronous copy ran out (tensor-core tier)");
 }
 
 }  // namespace
@@ -504,8 +516,10 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         st.flops_tf32 += 6.0 * K4 * (double)pairs_t2;
         st.host_items_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tB).count();
         MWG_CUDA(cudaEventRecord(ev[0], ctx.stream));
+        int *tc_status = nullptr;
         for (int k = 0; k < NTIER; k++) {
-            launch_tier(ctx, lt[k], root, k == 0, k, st);
+            int *hs = launch_tier(ctx, lt[k], root, k == 0, k, st);
+            if (hs) tc_status = hs;
             MWG_CUDA(cudaEventRecord(ev[k + 1], ctx.stream));
         }
         // norms of the level's output nodes
@@ -531,6 +545,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         auto tW = std::chrono::steady_clock::now();
         ctx.sync();
         st.host_wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tW).count();
+        check_status(tc_status);
         float ms_t[NTIER];
         for (int k = 0; k < NTIER; k++) MWG_CUDA(cudaEventElapsedTime(&ms_t[k], ev[k], ev[k + 1]));
         kernel_ms += ms_t[0] + ms_t[1] + ms_t[2];

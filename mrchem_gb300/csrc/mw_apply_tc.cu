@@ -50,16 +50,21 @@ struct TcGeo {
     static constexpr int NTS = (K + 7) / 8;                   // column tiles holding scaling columns
     static constexpr int W = MT < 5 ? MT : 5;                 // warps per CTA
     static constexpr int MPW = (MT + W - 1) / W;              // row tiles per warp
+    static constexpr bool EVEN = MT % W == 0;                 // every warp has MPW row tiles
     // T1[Z][Y][X'] and u[Z][Y][X'] (Z, Y, X' < K): Y stride 24
     static constexpr int SY1 = 24, SZ1 = N2 * SY1, SZU = K * SY1;
     // T2[Z][Y'][X'] and t2x[Z][Y'][X']: Y' stride 20 (= 4 mod 16), Z stride = 8 mod 16
     static constexpr int SY2 = 20, SZ2 = pad8mod16(N2 * SY2), SZX = pad8mod16(K * SY2);
-    static constexpr int OT1 = ((cmax(C, N2 * SZ2) + 3) / 4) * 4;  // IN and T2 share the first region
-    static constexpr int OU = OT1 + N2 * SZ1;
+    // two regions that take turns: item j has IN and T2 in region j%2 and T1 in the other one,
+    // so item j+1's input can be copied into that other region during item j's z pass
+    static constexpr int REG = ((cmax(cmax(C, N2 * SZ1), N2 * SZ2) + 3) / 4) * 4;
+    static constexpr int OU = 2 * REG;
     static constexpr int OT2X = OU + K * SZU;
-    static constexpr int OA = ((OT2X + K * SZX + 3) / 4) * 4;
-    static constexpr int TOTAL = OA + 3 * NC;
+    static constexpr int OA = ((OT2X + K * SZX + 3) / 4) * 4;  // two sets of A_x, A_y, A_z
+    static constexpr int TOTAL = OA + 6 * NC;
+    static constexpr uint32_t TX_BYTES = 4u * (C + 3 * NC);    // one item's copies
     static_assert(N2 <= SY2 && N2 <= SY1, "row strides too short for this order");
+    static_assert(TX_BYTES < (1u << 20), "transaction count out of range");
 };
 
 __device__ __forceinline__ uint32_t to_tf32(float x) {
@@ -154,25 +159,84 @@ __device__ __forceinline__ void mma_steps(float (&c)[4], const uint32_t (&a)[TcG
     }
 }
 
+// ---- asynchronous bulk copies (TMA engine) into shared memory, completed on an mbarrier
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// global -> shared, 16-byte aligned addresses and a size that is a multiple of 16
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Waits for the copies of the current phase, at most TC_WAIT_LIMIT polls.  A wait that runs
+// out marks the launch failed (the host turns the status into MW_ERR_TIMEOUT) and every later
+// wait of the CTA returns at once, so the kernel still ends with all threads on the same path.
+constexpr int TC_WAIT_LIMIT = 1 << 20;
+
+__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, volatile int *fail, int *status) {
+    if (*fail) return;
+    for (int it = 0; it < TC_WAIT_LIMIT; it++)
+        if (mbar_try_wait(bar, parity)) return;
+    *fail = 1;
+    atomicExch(status, 1);
+}
+
 template <int K>
 __global__ void __launch_bounds__(TcGeo<K>::W * 32, 2) apply_tc_kernel(ApplyLaunch L) {
     using G = TcGeo<K>;
     extern __shared__ __align__(16) float smem_tc[];
-    float *s_in = smem_tc;  // IN[Z][Y][X] (cube order), later T2
-    float *s_t2 = smem_tc;
-    float *s_t1 = smem_tc + G::OT1;
     float *s_u = smem_tc + G::OU;
     float *s_t2x = smem_tc + G::OT2X;
-    float *s_A = smem_tc + G::OA;  // A_x, A_y, A_z
+    __shared__ __align__(8) uint64_t s_bar;
     __shared__ int s_node;
+    __shared__ volatile int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
     const bool excl = !L.root;
+    // item j's input block and operator blocks -> region / operator set `buf` (thread 0 only)
+    auto issue = [&](const void *in, const void *ax, const void *ay, const void *az, int buf) {
+        float *A = smem_tc + G::OA + buf * 3 * G::NC;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&s_bar, G::TX_BYTES);
+        bulk_copy(smem_tc + buf * G::REG, in, 4u * G::C, &s_bar);
+        bulk_copy(A, ax, 4u * G::NC, &s_bar);
+        bulk_copy(A + G::NC, ay, 4u * G::NC, &s_bar);
+        bulk_copy(A + 2 * G::NC, az, 4u * G::NC, &s_bar);
+    };
+    if (tid == 0) {
+        mbar_init(&s_bar);
+        s_fail = 0;
+    }
+    __syncthreads();
+    uint32_t parity = 0;
 
     while (true) {
         if (tid == 0) s_node = atomicAdd(L.counter, 1);
         __syncthreads();
         const int w = s_node;
         if (w >= L.nnodes) break;
+        const long long b0 = L.begin[w], b1 = L.end[w];
+        if (tid == 0 && b0 < b1) issue(L.in[b0], L.ax[b0], L.ay[b0], L.az[b0], 0);
         float acc[G::MPW][G::NT][4];
 #pragma unroll
         for (int i = 0; i < G::MPW; i++)
@@ -180,25 +244,24 @@ __global__ void __launch_bounds__(TcGeo<K>::W * 32, 2) apply_tc_kernel(ApplyLaun
             for (int nt = 0; nt < G::NT; nt++)
 #pragma unroll
                 for (int e = 0; e < 4; e++) acc[i][nt][e] = 0.0f;
-        const long long b0 = L.begin[w], b1 = L.end[w];
         for (long long j = b0; j < b1; j++) {
-            __syncthreads();  // the previous item's z pass is done with s_t2 and s_A
-            {
-                const float4 *gin4 = reinterpret_cast<const float4 *>(L.in[j]);
-                float4 *sin4 = reinterpret_cast<float4 *>(s_in);
-                for (int i = tid; i < G::C / 4; i += blockDim.x) sin4[i] = __ldg(gin4 + i);
-                const float4 *ax4 = reinterpret_cast<const float4 *>(L.ax[j]);
-                const float4 *ay4 = reinterpret_cast<const float4 *>(L.ay[j]);
-                const float4 *az4 = reinterpret_cast<const float4 *>(L.az[j]);
-                float4 *sa4 = reinterpret_cast<float4 *>(s_A);
-                for (int i = tid; i < G::NC / 4; i += blockDim.x) {
-                    sa4[i] = __ldg(ax4 + i);
-                    sa4[G::NC / 4 + i] = __ldg(ay4 + i);
-                    sa4[2 * (G::NC / 4) + i] = __ldg(az4 + i);
-                }
+            const int p = (int)((j - b0) & 1);
+            float *s_in = smem_tc + p * G::REG;        // IN, then T2
+            float *s_t2 = s_in;
+            float *s_t1 = smem_tc + (p ^ 1) * G::REG;  // T1, then item j+1's input
+            const float *s_A = smem_tc + G::OA + p * 3 * G::NC;
+            // item j+1's pointers, read early so that their latency is hidden by the x and y passes
+            const bool more = j + 1 < b1;
+            const void *nin = nullptr, *nax = nullptr, *nay = nullptr, *naz = nullptr;
+            if (tid == 0 && more) {
+                nin = L.in[j + 1];
+                nax = L.ax[j + 1];
+                nay = L.ay[j + 1];
+                naz = L.az[j + 1];
             }
             const float cf = float(L.coef[j]);
-            __syncthreads();
+            mbar_wait(&s_bar, parity, &s_fail, L.status);
+            parity ^= 1u;
             // ---- x pass: rows (Z, Y), contraction X, columns X'
             {
                 uint32_t bf[G::NT][G::NKS][2];
@@ -206,7 +269,7 @@ __global__ void __launch_bounds__(TcGeo<K>::W * 32, 2) apply_tc_kernel(ApplyLaun
 #pragma unroll
                 for (int i = 0; i < G::MPW; i++) {
                     const int mt = warp + G::W * i;
-                    if (mt >= G::MT) break;
+                    if (!G::EVEN && mt >= G::MT) break;
                     const int r0 = mt * 16 + g;
                     int z[2], y[2];
                     row_ab<K>(r0, z[0], y[0]);
@@ -266,7 +329,7 @@ __global__ void __launch_bounds__(TcGeo<K>::W * 32, 2) apply_tc_kernel(ApplyLaun
 #pragma unroll
                 for (int i = 0; i < G::MPW; i++) {
                     const int mt = warp + G::W * i;
-                    if (mt >= G::MT) break;
+                    if (!G::EVEN && mt >= G::MT) break;
                     const int r0 = mt * 16 + g;
                     int z[2], xp[2];
                     row_ab<K>(r0, z[0], xp[0]);
@@ -329,6 +392,8 @@ __global__ void __launch_bounds__(TcGeo<K>::W * 32, 2) apply_tc_kernel(ApplyLaun
                 }
             }
             __syncthreads();
+            // T1's region is free: item j+1's blocks are copied into it during the z pass
+            if (tid == 0 && more) issue(nin, nax, nay, naz, p ^ 1);
             // ---- z pass: rows (Y', X'), contraction Z, columns Z'; accumulate c_t * ... into acc
             {
                 uint32_t bf[G::NT][G::NKS][2];
@@ -336,7 +401,7 @@ __global__ void __launch_bounds__(TcGeo<K>::W * 32, 2) apply_tc_kernel(ApplyLaun
 #pragma unroll
                 for (int i = 0; i < G::MPW; i++) {
                     const int mt = warp + G::W * i;
-                    if (mt >= G::MT) break;
+                    if (!G::EVEN && mt >= G::MT) break;
                     const int r0 = mt * 16 + g;
                     int yp[2], xp[2];
                     row_ab<K>(r0, yp[0], xp[0]);
@@ -375,6 +440,7 @@ __global__ void __launch_bounds__(TcGeo<K>::W * 32, 2) apply_tc_kernel(ApplyLaun
                     }
                 }
             }
+            __syncthreads();  // item j+1's x pass writes T1 into this item's IN / T2 region
         }
         // ---- node epilogue: acc rows (Y', X'), columns Z' -> component-major FP64 block
         {
@@ -382,7 +448,7 @@ __global__ void __launch_bounds__(TcGeo<K>::W * 32, 2) apply_tc_kernel(ApplyLaun
 #pragma unroll
             for (int i = 0; i < G::MPW; i++) {
                 const int mt = warp + G::W * i;
-                if (mt >= G::MT) break;
+                if (!G::EVEN && mt >= G::MT) break;
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int r = mt * 16 + g + 8 * h;
@@ -431,6 +497,7 @@ void launch_tc(const ApplyLaunch &L, int nsm, cudaStream_t s) {
 void k_apply_tc(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s) {
     if (L.nnodes <= 0) return;
     MWG_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(int), s));
+    MWG_CUDA(cudaMemsetAsync(L.status, 0, sizeof(int), s));
     switch (b.K) {
         case 4: launch_tc<4>(L, nsm, s); break;
         case 5: launch_tc<5>(L, nsm, s); break;

@@ -218,6 +218,7 @@ struct ApplyLaunch {
     const void *const *az;
     const double *coef;           // per item
     int *counter;                 // dynamic node counter (persistent grid)
+    int *status;                  // 0, or 1 when a bounded wait of the launch ran out (tensor-core tier)
 };
 
 struct PairTask {  // parent -> children (8 consecutive blocks)
