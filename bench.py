@@ -265,6 +265,11 @@ def run(args):
     e2e_v = nodes * world / e2e_s
 
     st = stats[-1]
+    # one step with the job groups not overlapped: its tier kernels run alone, so their
+    # CUDA-event times are exclusive (the rooflines and the kernel split below use them)
+    mra.set_overlap(False)
+    serial_ms, st_ser = timed("mixed", 1)
+    mra.set_overlap(True)
     fp64_tf = mra.probe_fma_peak(True)
     fp32_tf = mra.probe_fma_peak(False)
     tf32_tf = mra.probe_mma_peak("tf32")
@@ -278,9 +283,9 @@ def run(args):
     mma_src = ("probed dense m16n8k8 TF32 warp-MMA throughput of this GPU (mw_probe_mma_peak); "
                "MEASURED_PEAKS.json holds no TF32 figure")
     roofs = {
-        "fp64": roof(st["flops_fp64"], st["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
-        "fp32": roof(st["flops_fp32"], st["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src),
-        "tf32": roof(st["flops_tf32"], st["kernel_ms_tf32"], tf32_tf, "apply_tc_kernel<10>", "tensor", mma_src),
+        "fp64": roof(st_ser["flops_fp64"], st_ser["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
+        "fp32": roof(st_ser["flops_fp32"], st_ser["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src),
+        "tf32": roof(st_ser["flops_tf32"], st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc_kernel<10>", "tensor", mma_src),
     }
     dominant = max(roofs, key=lambda k: roofs[k]["kernel_ms_per_step"])
     line = {
@@ -303,10 +308,14 @@ def run(args):
                        "rel_l2_vs_fp64_max": f32_err, "policy": "FP64 / FP32 tiers only (no tensor cores)"},
         "rel_l2_vs_fp64_max": max(errs),
         "items": {"total": st["items"], "fp64": st["items_fp64"], "fp32": st["items_fp32"], "tf32": st["items_tf32"]},
-        "kernel_ms_per_step": st["kernel_ms"], "host_ms_per_step": st["host_ms"],
+        "kernel_ms_per_step": st_ser["kernel_ms"], "host_ms_per_step": st["host_ms"],
         "host_breakdown_ms": {"enumerate": st["host_enum_ms"], "items": st["host_items_ms"],
-                              "wait_level": st["host_wait_ms"], "kernel_fp64": st["kernel_ms_fp64"],
-                              "kernel_fp32": st["kernel_ms_fp32"], "kernel_tf32": st["kernel_ms_tf32"]},
+                              "wait_level": st["host_wait_ms"], "kernel_fp64": st_ser["kernel_ms_fp64"],
+                              "kernel_fp32": st_ser["kernel_ms_fp32"], "kernel_tf32": st_ser["kernel_ms_tf32"],
+                              "note": "host phases from the timed (overlapped) steps; exclusive kernel times "
+                                      "from one step without overlap"},
+        "no_overlap": {"value": st_ser["out_nodes"] * world / (serial_ms / 1e3), "unit": "nodes/s",
+                       "ms_per_step": serial_ms, "policy": "job groups not pipelined (mw_ctx_set_overlap 0)"},
         "gpu_launches": int(st["launches"]),
         "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": dict(roofs[dominant], tier=dominant),

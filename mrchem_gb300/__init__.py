@@ -71,7 +71,7 @@ EXPORTS = [
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
     "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
-    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc",
+    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap",
 ]
 
 
@@ -92,6 +92,7 @@ def load_library(path=None):
         "mw_ctx_basis": [P, dp, dp, dp, dp, dp],
         "mw_ctx_last_stats": [P, C.POINTER(Stats)],
         "mw_ctx_synchronize": [P],
+        "mw_ctx_set_overlap": [P, I],
         "mw_tree_create": [P, pp],
         "mw_tree_destroy": [P],
         "mw_tree_nnodes": [P, ip],
@@ -207,6 +208,10 @@ class MultiResolutionAnalysis:
 
     def synchronize(self):
         _check(_lib.mw_ctx_synchronize(self.ptr), self.ptr)
+
+    def set_overlap(self, on=True):
+        """Pipelined job groups in batched applies (default on); off gives exclusive kernel times."""
+        _check(_lib.mw_ctx_set_overlap(self.ptr, int(bool(on))), self.ptr)
 
     def probe_fma_peak(self, fp64=True):
         """Measured FMA throughput of this GPU in TFLOP/s (FP64 or FP32 CUDA cores)."""

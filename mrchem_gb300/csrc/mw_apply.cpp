@@ -215,7 +215,7 @@ struct LevelItems {
 
 // tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores.  Returns the pinned host copy of the
 // launch's status word (read it after the stream has been synchronised), or nullptr.
-int *launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int tier, mw_stats &st) {
+int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, int tier, mw_stats &st) {
     int nn = (int)li.out.size();
     if (nn == 0) return nullptr;
     // nodes in decreasing item count (longest first) for the persistent grid's dynamic
@@ -241,8 +241,8 @@ int *launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int tier, mw_sta
     pk.add(li.ay.data(), li.ay.size() * sizeof(void *));
     pk.add(li.az.data(), li.az.size() * sizeof(void *));
     pk.add(li.coef.data(), li.coef.size() * sizeof(double));
-    pk.ship(ctx, ctx.arena);
-    int *counter = (int *)ctx.arena.alloc(2 * sizeof(int));
+    pk.ship(ctx, arena);
+    int *counter = (int *)arena.alloc(2 * sizeof(int));
     ApplyLaunch L;
     L.nnodes = nn;
     L.root = root ? 1 : 0;
@@ -263,7 +263,7 @@ int *launch_tier(Ctx &ctx, LevelItems &li, bool root, bool set, int tier, mw_sta
         return nullptr;
     }
     k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
-    int *hs = (int *)ctx.arena.halloc(sizeof(int));
+    int *hs = (int *)arena.halloc(sizeof(int));
     *hs = 0;
     MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
     return hs;
@@ -288,8 +288,6 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     auto t_start = std::chrono::steady_clock::now();
     Arena &arena = ctx.arena;
     arena.reset();
-    cudaEvent_t ev[NTIER + 1];
-    for (auto &e : ev) MWG_CUDA(cudaEventCreate(&e));
     float kernel_ms = 0.0f;
 
     std::vector<JobState> js(jobs.size());
@@ -326,37 +324,96 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             if (s.job->out->nodes[i].n == n) s.work.push_back(i);
     };
 
-    LevelItems lt[NTIER];
-    int level = 0;
-    while (true) {
+    // The jobs are split into two groups that take turns: while the GPU runs one group's level,
+    // the host enumerates, screens and builds the items of the other group's level.  Group 0
+    // works on the context's stream and arena, group 1 on a second stream and arena of the
+    // context.  A single job runs as one group.
+    struct Group {
+        std::vector<int> jobs;
+        cudaStream_t stream = nullptr;
+        Arena *arena = nullptr;
+        int level = 0;
+        bool pending = false, done = false;
+        LevelItems lt[NTIER];
+        cudaEvent_t ev[NTIER + 1];
+        int *tc_status = nullptr;
+        std::vector<double *> h_cn;  // pinned staging of each job's component norms
+    };
+    // runs the host side with the context's stream pointing at the group's stream
+    struct StreamSwap {
+        Ctx &c;
+        cudaStream_t saved;
+        StreamSwap(Ctx &c_, cudaStream_t s) : c(c_), saved(c_.stream) { c.stream = s; }
+        ~StreamSwap() { c.stream = saved; }
+    };
+    const int ngroups = (ctx.overlap && jobs.size() >= 2) ? 2 : 1;
+    std::vector<Group> groups(ngroups);
+    {
+        // balance the groups by input size, largest jobs first
+        std::vector<int> ord(jobs.size());
+        for (size_t j = 0; j < jobs.size(); j++) ord[j] = (int)j;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return jobs[a].inp->nn() > jobs[c].inp->nn(); });
+        long load[2] = {0, 0};
+        for (int j : ord) {
+            int g = (ngroups == 2 && load[1] < load[0]) ? 1 : 0;
+            groups[g].jobs.push_back(j);
+            load[g] += jobs[j].inp->nn();
+        }
+        for (auto &g : groups) std::sort(g.jobs.begin(), g.jobs.end());
+    }
+    groups[0].stream = ctx.stream;
+    groups[0].arena = &arena;
+    cudaEvent_t ev_start = nullptr, ev_g1 = nullptr;
+    if (ngroups == 2) {
+        if (!ctx.stream2) MWG_CUDA(cudaStreamCreateWithFlags(&ctx.stream2, cudaStreamNonBlocking));
+        ctx.arena2.reset();
+        groups[1].stream = ctx.stream2;
+        groups[1].arena = &ctx.arena2;
+        // group 1 starts after the set-up queued on the context's stream (FP32 shadows, zeroed roots)
+        MWG_CUDA(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
+        MWG_CUDA(cudaEventCreateWithFlags(&ev_g1, cudaEventDisableTiming));
+        MWG_CUDA(cudaEventRecord(ev_start, ctx.stream));
+        MWG_CUDA(cudaStreamWaitEvent(ctx.stream2, ev_start, 0));
+    }
+    for (auto &g : groups)
+        for (auto &e : g.ev) MWG_CUDA(cudaEventCreate(&e));
+
+    // host phases of the group's next level and its launches; false when the group has no work left
+    auto launch_level = [&](Group &G) -> bool {
+        StreamSwap swap(ctx, G.stream);
+        Arena &ar = *G.arena;
+        const int level = G.level;
         const int n = b.n0 + level, sidx = level;
+        std::vector<JobState *> jp;
+        for (int j : G.jobs) jp.push_back(&js[j]);
         if (fixed_grid) {
-            if (level >= max_levels) break;
-            for (auto &s : js) fixed_level_nodes(s, n);
+            if (level >= max_levels) return false;
+            for (JobState *sp : jp) fixed_level_nodes(*sp, n);
         }
         bool any = false;
-        for (auto &s : js) any |= !s.work.empty();
-        if (!any) break;
+        for (JobState *sp : jp) any |= !sp->work.empty();
+        if (!any) return false;
         const bool root = (level == 0);
         // thresholds and precision-steering weights
-        for (auto &s : js) {
+        for (JobState *sp : jp) {
+            JobState &s = *sp;
             s.wgt.assign(s.work.size(), 1.0);
             if (!s.job->prec_trees.empty())
                 for (size_t w = 0; w < s.work.size(); w++)
                     s.wgt[w] = prec_weight(s.job->prec_trees, n, s.job->out->nodes[s.work[w]].l);
             s.cand.assign(s.work.size(), {});
         }
-        // phase A: candidate enumeration (host, all jobs' nodes in parallel)
+        // phase A: candidate enumeration (host, all the group's nodes in parallel)
         auto tA = std::chrono::steady_clock::now();
         std::vector<std::pair<int, int>> flat;
-        for (size_t j = 0; j < js.size(); j++)
-            for (size_t w = 0; w < js[j].work.size(); w++) flat.push_back({(int)j, (int)w});
+        for (size_t j = 0; j < jp.size(); j++)
+            for (size_t w = 0; w < jp[j]->work.size(); w++) flat.push_back({(int)j, (int)w});
 #pragma omp parallel
         {
             LookupCache cache;
 #pragma omp for schedule(dynamic, 4)
             for (long q = 0; q < (long)flat.size(); q++) {
-                JobState &s = js[flat[q].first];
+                JobState &s = *jp[flat[q].first];
                 int w = flat[q].second;
                 if (!root && s.wgt[w] <= 0.0) {
                     s.cand[w].clear();
@@ -369,7 +426,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         auto tB = std::chrono::steady_clock::now();
         st.host_enum_ms += std::chrono::duration<double, std::milli>(tB - tA).count();
         // phase B: generated input nodes
-        for (auto &s : js) {
+        for (JobState *sp : jp) {
+            JobState &s = *sp;
             s.gens.clear();
             for (size_t w = 0; w < s.work.size(); w++) {
                 const NodeInfo &o = s.job->out->nodes[s.work[w]];
@@ -381,24 +439,25 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             }
         }
         {
-            // one generation launch for all jobs; the blocks are contiguous in job order
+            // one generation launch for the group; the blocks are contiguous in job order
             std::vector<std::pair<GenSet *, const Tree *>> sets;
             size_t total = 0;
-            for (auto &s : js) {
-                sets.push_back({&s.gens, s.job->inp});
-                total += s.gens.keys.size();
+            for (JobState *sp : jp) {
+                sets.push_back({&sp->gens, sp->job->inp});
+                total += sp->gens.keys.size();
             }
-            generate_all(sets, arena, &st);
+            generate_all(sets, ar, &st);
             double *first = nullptr;
-            for (auto &s : js)
-                if (s.gens.base && !first) first = s.gens.base;
+            for (JobState *sp : jp)
+                if (sp->gens.base && !first) first = sp->gens.base;
             float *first32 = nullptr;
             if (mixed && total > 0) {
-                first32 = (float *)arena.alloc(sizeof(float) * (size_t)bs * total);
+                first32 = (float *)ar.alloc(sizeof(float) * (size_t)bs * total);
                 k_to_fp32_cube(first, first32, total, b.K, ctx.stream);
                 st.launches++;
             }
-            for (auto &s : js) {
+            for (JobState *sp : jp) {
+                JobState &s = *sp;
                 s.gbase = s.gens.base;
                 s.gcn.swap(s.gens.cn);
                 s.gbase32 = (first32 && s.gbase) ? first32 + (s.gbase - first) : nullptr;
@@ -407,8 +466,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         // phase C: exact screening and tier per candidate (parallel), then the
         // per-tier item lists in node order (prefix sums + parallel fill)
         std::vector<std::pair<int, int>> nodes_flat;  // (job, work index) in launch order
-        for (size_t j = 0; j < js.size(); j++)
-            for (size_t w = 0; w < js[j].work.size(); w++) nodes_flat.push_back({(int)j, (int)w});
+        for (size_t j = 0; j < jp.size(); j++)
+            for (size_t w = 0; w < jp[j]->work.size(); w++) nodes_flat.push_back({(int)j, (int)w});
         const long NN = (long)nodes_flat.size();
         // per tier (0 FP64, 1 FP32, 2 TF32): per-node item counts, then prefix sums
         std::vector<long long> cnt[NTIER];
@@ -416,7 +475,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         long long pairs_tot = 0, pairs_t0 = 0, pairs_t1 = 0, pairs_t2 = 0;
 #pragma omp parallel for schedule(dynamic, 4) reduction(+ : pairs_tot, pairs_t0, pairs_t1, pairs_t2)
         for (long q = 0; q < NN; q++) {
-            JobState &s = js[nodes_flat[q].first];
+            JobState &s = *jp[nodes_flat[q].first];
             int w = nodes_flat[q].second;
             const Tree &inp = *s.job->inp;
             const Oper &op = *s.job->op;
@@ -453,6 +512,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             for (int k = 0; k < NTIER; k++) cnt[k][q + 1] = c[k];
         }
         // FP64 launch: every node (it writes the block); other tiers: nodes that have items there
+        LevelItems *lt = G.lt;
         std::vector<long> slot[NTIER];
         long nnt[NTIER] = {NN, 0, 0};
         for (int k = 0; k < NTIER; k++) slot[k].assign(NN, -1);
@@ -469,7 +529,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         }
 #pragma omp parallel for schedule(dynamic, 4)
         for (long q = 0; q < NN; q++) {
-            JobState &s = js[nodes_flat[q].first];
+            JobState &s = *jp[nodes_flat[q].first];
             int w = nodes_flat[q].second;
             const Tree &inp = *s.job->inp;
             const Oper &op = *s.job->op;
@@ -515,46 +575,57 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         st.flops_fp32 += 6.0 * K4 * (double)pairs_t1;
         st.flops_tf32 += 6.0 * K4 * (double)pairs_t2;
         st.host_items_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tB).count();
-        MWG_CUDA(cudaEventRecord(ev[0], ctx.stream));
-        int *tc_status = nullptr;
+        MWG_CUDA(cudaEventRecord(G.ev[0], ctx.stream));
+        G.tc_status = nullptr;
         for (int k = 0; k < NTIER; k++) {
-            int *hs = launch_tier(ctx, lt[k], root, k == 0, k, st);
-            if (hs) tc_status = hs;
-            MWG_CUDA(cudaEventRecord(ev[k + 1], ctx.stream));
+            int *hs = launch_tier(ctx, ar, lt[k], root, k == 0, k, st);
+            if (hs) G.tc_status = hs;
+            MWG_CUDA(cudaEventRecord(G.ev[k + 1], ctx.stream));
         }
-        // norms of the level's output nodes
+        // norms of the level's output nodes, downloaded into pinned staging
         std::vector<double *> bl, cnp;
-        for (auto &s : js)
-            for (int oi : s.work) {
-                bl.push_back(s.job->out->block(oi));
-                cnp.push_back(s.job->out->d_cn + (size_t)8 * oi);
+        for (JobState *sp : jp)
+            for (int oi : sp->work) {
+                bl.push_back(sp->job->out->block(oi));
+                cnp.push_back(sp->job->out->d_cn + (size_t)8 * oi);
             }
         {
             Packer pk;
             pk.add(bl.data(), bl.size() * sizeof(double *));
             pk.add(cnp.data(), cnp.size() * sizeof(double *));
-            pk.ship(ctx, arena);
+            pk.ship(ctx, ar);
             k_norms(ctx.dbasis, (double *const *)pk.ptr(0), (double *const *)pk.ptr(1), (int)bl.size(), ctx.stream);
             st.launches++;
         }
-        for (auto &s : js) {
-            Tree &out = *s.job->out;
-            MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
+        G.h_cn.assign(jp.size(), nullptr);
+        for (size_t j = 0; j < jp.size(); j++) {
+            Tree &out = *jp[j]->job->out;
+            G.h_cn[j] = (double *)ar.halloc(sizeof(double) * 8 * out.nn());
+            MWG_CUDA(cudaMemcpyAsync(G.h_cn[j], out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
                                      ctx.stream));
         }
+        return true;
+    };
+
+    // waits for the group's level, then the refinement decisions on its norms
+    auto finish_level = [&](Group &G) {
+        StreamSwap swap(ctx, G.stream);
+        const int n = b.n0 + G.level;
+        const bool root = (G.level == 0);
         auto tW = std::chrono::steady_clock::now();
         ctx.sync();
         st.host_wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tW).count();
-        check_status(tc_status);
+        check_status(G.tc_status);
         float ms_t[NTIER];
-        for (int k = 0; k < NTIER; k++) MWG_CUDA(cudaEventElapsedTime(&ms_t[k], ev[k], ev[k + 1]));
+        for (int k = 0; k < NTIER; k++) MWG_CUDA(cudaEventElapsedTime(&ms_t[k], G.ev[k], G.ev[k + 1]));
         kernel_ms += ms_t[0] + ms_t[1] + ms_t[2];
         st.kernel_ms_fp64 += ms_t[0];
         st.kernel_ms_fp32 += ms_t[1];
         st.kernel_ms_tf32 += ms_t[2];
-        // refinement
-        for (auto &s : js) {
+        for (size_t j = 0; j < G.jobs.size(); j++) {
+            JobState &s = js[G.jobs[j]];
             Tree &out = *s.job->out;
+            std::copy(G.h_cn[j], G.h_cn[j] + (size_t)8 * out.nn(), out.cn.begin());
             st.out_nodes += (long long)s.work.size();
             st.bytes += 8.0 * bs * (double)s.work.size();
             if (root && !s.job->abs_prec) {
@@ -578,9 +649,34 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             s.iter++;
         }
         st.levels++;
-        arena.reset();
-        level++;
+        G.arena->reset();
+        G.level++;
+    };
+
+    while (true) {
+        bool active = false;
+        for (auto &G : groups) {
+            if (G.pending) {
+                finish_level(G);
+                G.pending = false;
+            }
+            if (!G.done) G.done = !launch_level(G);
+            if (!G.done) {
+                G.pending = true;
+                active = true;
+            }
+        }
+        if (!active) break;
     }
+    if (ngroups == 2) {
+        // the post-processing on the context's stream follows group 1's last work
+        MWG_CUDA(cudaEventRecord(ev_g1, ctx.stream2));
+        MWG_CUDA(cudaStreamWaitEvent(ctx.stream, ev_g1, 0));
+    }
+    for (auto &g : groups)
+        for (auto &e : g.ev) cudaEventDestroy(e);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_g1) cudaEventDestroy(ev_g1);
     // input bytes: every distinct input block read once per apply (FP64 or FP32 shadow) + operator blocks
     for (auto &s : js) st.bytes += 8.0 * bs * (double)s.job->inp->nn();
 
@@ -646,7 +742,6 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     }
     ctx.sync();
     arena.reset();
-    for (auto &e : ev) cudaEventDestroy(e);
     st.kernel_ms += kernel_ms;
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }
@@ -931,7 +1026,7 @@ void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats 
         st.items += (long long)items.size();
         st.items_fp64 += (long long)items.size();
         st.out_nodes += (long long)li.out.size();
-        launch_tier(ctx, li, root, true, 0, st);
+        launch_tier(ctx, ctx.arena, li, root, true, 0, st);
         ctx.sync();
         st.levels++;
     }

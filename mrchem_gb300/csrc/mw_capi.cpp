@@ -110,10 +110,13 @@ int mw_ctx_create(int device, int root_scale, const int corner[3], const int box
 static void ctx_free(mw_ctx c) {
     cudaSetDevice(c->ctx.device);
     cudaStreamSynchronize(c->ctx.stream);
+    if (c->ctx.stream2) cudaStreamSynchronize(c->ctx.stream2);
     c->ctx.arena.release();
+    c->ctx.arena2.release();
     if (c->ctx.h_pinned) cudaFreeHost(c->ctx.h_pinned);
     if (c->ctx.d_basis) cudaFree(c->ctx.d_basis);
     cudaStreamDestroy(c->ctx.stream);
+    if (c->ctx.stream2) cudaStreamDestroy(c->ctx.stream2);
     delete c;
 }
 
@@ -151,6 +154,12 @@ int mw_ctx_last_stats(mw_ctx c, mw_stats *st) {
 int mw_ctx_synchronize(mw_ctx c) {
     if (!c) return MW_ERR_ARG;
     return guard(&c->ctx, [&] { c->ctx.sync(); });
+}
+
+int mw_ctx_set_overlap(mw_ctx c, int on) {
+    if (!c || (on != 0 && on != 1)) return MW_ERR_ARG;
+    c->ctx.overlap = on != 0;
+    return MW_OK;
 }
 
 // ---------------------------------------------------------------- trees

@@ -75,3 +75,26 @@ def test_tensor_tier_rerun_bit_identical(engine):
     ka, ca, _ = a.download()
     kb, cb, _ = b.download()
     assert np.array_equal(ka, kb) and np.array_equal(ca, cb)
+
+
+def test_overlapped_groups_bit_identical_to_serial(engine):
+    # the batched apply pipelines two job groups on two streams; results must not depend on it
+    prec = 1e-5
+    mra = engine.MultiResolutionAnalysis(7)
+    rng = np.random.default_rng(11)
+    phis, ops = [], []
+    for i in range(5):
+        c = tuple(rng.uniform(-1.0, 1.0, 3))
+        f = engine.project(prec, engine.FunctionTree(mra), [(1.0, float(rng.uniform(1.0, 20.0)), c, (i % 2, 0, 0))],
+                           abs_prec=True)
+        phis.append(f)
+        ops.append(engine.HelmholtzOperator(mra, float(rng.uniform(0.5, 2.0)), prec))
+    res = {}
+    for on in (True, False):
+        mra.set_overlap(on)
+        outs = [engine.FunctionTree(mra) for _ in phis]
+        engine.apply_batch([prec] * 5, outs, ops, phis, abs_prec=True, precision="mixed")
+        res[on] = [o.download() for o in outs]
+    mra.set_overlap(True)
+    for (k1, c1, l1), (k2, c2, l2) in zip(res[True], res[False]):
+        assert np.array_equal(k1, k2) and np.array_equal(c1, c2) and np.array_equal(l1, l2)
