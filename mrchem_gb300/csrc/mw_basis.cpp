@@ -418,23 +418,14 @@ void Oper::build(const Basis &b) {
             if (q % 4 > 0) xmax[i] = std::max(xmax[i], ts[i].nrm[q]);
         }
     }
-    // device copies: FP64, FP32 and BF16 (round to nearest even)
+    // device copies: FP64, and FP32 for the FP32 and TF32 tiers (the TF32 kernel rounds on load)
     size_t nel = blocks.size();
     std::vector<float> b32(nel);
-    std::vector<uint16_t> b16(nel);
-    for (size_t i = 0; i < nel; i++) {
-        b32[i] = (float)blocks[i];
-        uint32_t u;
-        std::memcpy(&u, &b32[i], 4);
-        u += 0x7FFF + ((u >> 16) & 1);
-        b16[i] = (uint16_t)(u >> 16);
-    }
+    for (size_t i = 0; i < nel; i++) b32[i] = (float)blocks[i];
     MWG_CUDA(cudaMalloc(&d_blocks, sizeof(double) * nel));
     MWG_CUDA(cudaMalloc(&d_blocks32, sizeof(float) * nel));
-    MWG_CUDA(cudaMalloc(&d_blocks16, sizeof(uint16_t) * nel));
     MWG_CUDA(cudaMemcpy(d_blocks, blocks.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
     MWG_CUDA(cudaMemcpy(d_blocks32, b32.data(), sizeof(float) * nel, cudaMemcpyHostToDevice));
-    MWG_CUDA(cudaMemcpy(d_blocks16, b16.data(), sizeof(uint16_t) * nel, cudaMemcpyHostToDevice));
 }
 
 }  // namespace mwg

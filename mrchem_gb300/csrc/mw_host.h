@@ -126,7 +126,6 @@ struct Oper {
     long nblocks = 0;
     double *d_blocks = nullptr;  // (2K)^2 per block, FP64
     float *d_blocks32 = nullptr; // FP32 copy
-    uint16_t *d_blocks16 = nullptr; // BF16 copy (bit patterns)
     const double *norm(int t, int s, int l) const { return &norms[(size_t)(off[t * S + s] + l + band[t * S + s]) * 4]; }
     long block_index(int t, int s, int l) const { return off[t * S + s] + l + band[t * S + s]; }
     void build(const Basis &b);
