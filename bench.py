@@ -286,12 +286,16 @@ def run(args):
         "fp64": roof(st_ser["flops_fp64"], st_ser["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
         "fp32": roof(st_ser["flops_fp32"], st_ser["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src),
         "tf32": roof(st_ser["flops_tf32"], st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc_kernel<10>", "tensor", mma_src),
+        # a double-FP32 multiply-add costs 12 FP32 instructions: peak = FP32 FMA peak * 2 / 24
+        "df32": roof(st_ser["flops_df"], st_ser["kernel_ms_df"], fp32_tf / 12.0, "apply_df_kernel<10>",
+                     "fp32-pipe (double-FP32)", fma_src + "; divided by 12 FP32 instructions per double-FP32 "
+                     "multiply-add"),
     }
     dominant = max(roofs, key=lambda k: roofs[k]["kernel_ms_per_step"])
     line = {
         "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64+f32+tf32", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f64+df32+f32+tf32", "data": "synthetic",
         "config": {"workload": "helmholtz-batch16-k9-prec1e-6", "orbitals": NORB, "order": ORDER, "prec": PREC,
                    "basis": "interpolating", "box": "[-32,32]^3", "input_nodes": in_nodes,
                    "output_nodes": nodes, "l2": "inputs larger than L2 (%.1f GB of FP64 blocks)"
@@ -307,11 +311,13 @@ def run(args):
                        "ms_per_step": f32_ms, "items_fp64": st_f32["items_fp64"], "items_fp32": st_f32["items_fp32"],
                        "rel_l2_vs_fp64_max": f32_err, "policy": "FP64 / FP32 tiers only (no tensor cores)"},
         "rel_l2_vs_fp64_max": max(errs),
-        "items": {"total": st["items"], "fp64": st["items_fp64"], "fp32": st["items_fp32"], "tf32": st["items_tf32"]},
+        "items": {"total": st["items"], "fp64": st["items_fp64"], "fp32": st["items_fp32"], "tf32": st["items_tf32"],
+                  "df32": st["items_df"]},
         "kernel_ms_per_step": st_ser["kernel_ms"], "host_ms_per_step": st["host_ms"],
         "host_breakdown_ms": {"enumerate": st["host_enum_ms"], "items": st["host_items_ms"],
                               "wait_level": st["host_wait_ms"], "kernel_fp64": st_ser["kernel_ms_fp64"],
                               "kernel_fp32": st_ser["kernel_ms_fp32"], "kernel_tf32": st_ser["kernel_ms_tf32"],
+                              "kernel_df32": st_ser["kernel_ms_df"],
                               "note": "host phases from the timed (overlapped) steps; exclusive kernel times "
                                       "from one step without overlap"},
         "no_overlap": {"value": st_ser["out_nodes"] * world / (serial_ms / 1e3), "unit": "nodes/s",

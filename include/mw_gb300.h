@@ -38,12 +38,15 @@ extern "C" {
 
 /* precision modes of mw_apply / mw_apply_batch */
 #define MW_PREC_FP64 0   /* every contraction in FP64 */
-/* norm-tiered by the item's bound b against the screening threshold tau: FP64 when b > 2e6 tau,
- * TF32 tensor cores (FP32 accumulation) when b <= 2e3 tau below the root scale, FP32 CUDA cores
- * otherwise */
+/* norm-tiered by the item's bound b against the screening threshold tau: double-FP32 (pairs of
+ * FP32 numbers, ~3e-13 b) when 2e6 tau < b <= 1e11 tau, FP64 above that, TF32 tensor cores (FP32
+ * accumulation) when b <= 2e3 tau below the root scale, FP32 CUDA cores otherwise; root-scale
+ * items under relative precision run in FP64 */
 #define MW_PREC_MIXED 1
 #define MW_PREC_MIXED_NEARFP64 2  /* as MW_PREC_MIXED, and every item with |l|_inf <= 1 in FP64 */
-#define MW_PREC_MIXED_FP32 3      /* as MW_PREC_MIXED without the tensor-core tier: FP64 or FP32 only */
+#define MW_PREC_MIXED_FP32 3      /* FP64 or FP32 only: no tensor-core and no double-FP32 tier */
+#define MW_PREC_DF 4              /* double-FP32 for every item with b <= 1e11 tau, FP64 above that and for
+                                   * root-scale items under relative precision (error ~3e-13 b per item) */
 
 typedef struct mw_ctx_s *mw_ctx;
 typedef struct mw_tree_s *mw_tree;
@@ -81,6 +84,9 @@ typedef struct {
     double host_wait_ms;     /* host: waiting for the level's kernels and norm downloads */
     double flops_tf32;       /* algorithmic flops of the TF32 tier */
     double kernel_ms_tf32;   /* CUDA-event time of the TF32 contraction launches */
+    long long items_df;      /* contractions in double-FP32 (pairs of FP32 numbers) */
+    double flops_df;         /* algorithmic flops of the double-FP32 tier */
+    double kernel_ms_df;     /* CUDA-event time of the double-FP32 contraction launches */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */

@@ -30,8 +30,9 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_MIXED_NEARFP64 = 2
 PREC_MIXED_FP32 = 3
+PREC_DF = 4
 _PREC = {"fp64": PREC_FP64, "mixed": PREC_MIXED, "mixed-near64": PREC_MIXED_NEARFP64,
-         "mixed-fp32": PREC_MIXED_FP32}
+         "mixed-fp32": PREC_MIXED_FP32, "df": PREC_DF}
 
 
 class MWError(RuntimeError):
@@ -55,7 +56,8 @@ class Stats(C.Structure):
                 ("host_ms", C.c_double), ("flops_fp64", C.c_double), ("flops_fp32", C.c_double),
                 ("kernel_ms_fp64", C.c_double), ("kernel_ms_fp32", C.c_double), ("host_enum_ms", C.c_double),
                 ("host_items_ms", C.c_double), ("host_wait_ms", C.c_double), ("flops_tf32", C.c_double),
-                ("kernel_ms_tf32", C.c_double)]
+                ("kernel_ms_tf32", C.c_double), ("items_df", C.c_longlong), ("flops_df", C.c_double),
+                ("kernel_ms_df", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

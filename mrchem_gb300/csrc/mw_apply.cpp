@@ -41,7 +41,11 @@ constexpr double TIER_FP64 = 2e6;
 // small weight of the large root boxes, so many items just under it would add up to more than
 // prec relative to a small output.
 constexpr double TIER_TF32 = 2e3;
-constexpr int NTIER = 3;
+// An item in double-FP32 (values as unevaluated FP32 pairs, error-free products and sums) is off
+// by at most about 3e-13 b, so items with TIER_FP64 < b / tau <= TIER_DF err by at most 0.03 tau;
+// larger ones, and root-scale items under relative precision, run in FP64.
+constexpr double TIER_DF = 1e11;
+constexpr int NTIER = 4;  // 0 FP64, 1 FP32, 2 TF32 tensor cores, 3 double-FP32
 constexpr double BOUND_PRUNE = 8.0 * 2.8285;  // (sum_f |in_f|) / |block| <= sqrt(8); 8 output components
 
 double split_thr(double prec, double R, int n) { return prec * R * std::pow(2.0, -0.5 * (n + 1)); }
@@ -104,7 +108,7 @@ struct Cand {
     int t, lx, ly, lz;
     int src;   // input node index, or generated slot
     int gen;   // 1: src is a generated slot (ancestor index before generation)
-    int tier;  // after screening: -1 skipped, 0 FP64, 1 FP32, 2 TF32 tensor cores
+    int tier;  // after screening: -1 skipped, 0 FP64, 1 FP32, 2 TF32 tensor cores, 3 double-FP32
 };
 
 struct JobState {
@@ -213,7 +217,7 @@ struct LevelItems {
     }
 };
 
-// tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores.  Returns the pinned host copy of the
+// tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores, 3 double-FP32.  Returns the pinned host copy of the
 // launch's status word (read it after the stream has been synchronised), or nullptr.
 int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, int tier, mw_stats &st) {
     int nn = (int)li.out.size();
@@ -258,6 +262,10 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     L.counter = counter;
     L.status = counter + 1;
     st.launches++;
+    if (tier == 3) {
+        k_apply_df(ctx.dbasis, L, ctx.nsm, ctx.stream);
+        return nullptr;
+    }
     if (tier != 2) {
         k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
         return nullptr;
@@ -284,7 +292,9 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     const double K4 = (double)K * K * K * K;
     const bool mixed = precision_mode != MW_PREC_FP64;
     const bool near_fp64 = precision_mode == MW_PREC_MIXED_NEARFP64;
-    const bool tensor = mixed && precision_mode != MW_PREC_MIXED_FP32;
+    const bool tensor = mixed && precision_mode != MW_PREC_MIXED_FP32 && precision_mode != MW_PREC_DF;
+    const bool dfp = tensor;  // the double-FP32 tier comes with the tensor-core tier
+    const bool df_only = precision_mode == MW_PREC_DF;
     auto t_start = std::chrono::steady_clock::now();
     Arena &arena = ctx.arena;
     arena.reset();
@@ -307,7 +317,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             Tree &in = *job.inp;
             if (in.cap32 < (size_t)in.nn()) {
                 if (in.d_coefs32) cudaFree(in.d_coefs32);
-                MWG_CUDA(cudaMalloc(&in.d_coefs32, sizeof(float) * (size_t)bs * in.cap));
+                MWG_CUDA(cudaMalloc(&in.d_coefs32, sizeof(float) * 2 * (size_t)bs * in.cap));
                 in.cap32 = in.cap;
             }
             k_to_fp32_cube(in.d_coefs, in.d_coefs32, (size_t)in.nn(), b.K, ctx.stream);
@@ -452,7 +462,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 if (sp->gens.base && !first) first = sp->gens.base;
             float *first32 = nullptr;
             if (mixed && total > 0) {
-                first32 = (float *)ar.alloc(sizeof(float) * (size_t)bs * total);
+                first32 = (float *)ar.alloc(sizeof(float) * 2 * (size_t)bs * total);
                 k_to_fp32_cube(first, first32, total, b.K, ctx.stream);
                 st.launches++;
             }
@@ -460,7 +470,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 JobState &s = *sp;
                 s.gbase = s.gens.base;
                 s.gcn.swap(s.gens.cn);
-                s.gbase32 = (first32 && s.gbase) ? first32 + (s.gbase - first) : nullptr;
+                s.gbase32 = (first32 && s.gbase) ? first32 + 2 * (s.gbase - first) : nullptr;
             }
         }
         // phase C: exact screening and tier per candidate (parallel), then the
@@ -472,8 +482,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         // per tier (0 FP64, 1 FP32, 2 TF32): per-node item counts, then prefix sums
         std::vector<long long> cnt[NTIER];
         for (int k = 0; k < NTIER; k++) cnt[k].assign(NN + 1, 0);
-        long long pairs_tot = 0, pairs_t0 = 0, pairs_t1 = 0, pairs_t2 = 0;
-#pragma omp parallel for schedule(dynamic, 4) reduction(+ : pairs_tot, pairs_t0, pairs_t1, pairs_t2)
+        long long pairs_tot = 0, pairs_t0 = 0, pairs_t1 = 0, pairs_t2 = 0, pairs_t3 = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : pairs_tot, pairs_t0, pairs_t1, pairs_t2, pairs_t3)
         for (long q = 0; q < NN; q++) {
             JobState &s = *jp[nodes_flat[q].first];
             int w = nodes_flat[q].second;
@@ -485,7 +495,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             double tthr = !root ? thr
                           : s.job->abs_prec ? SCREEN_FAC * split_thr(s.job->prec, 1.0, n) / std::max(s.wgt[w], 1e-300)
                                             : -1.0;
-            long long c[NTIER] = {0, 0, 0};
+            long long c[NTIER] = {0, 0, 0, 0};
             for (Cand &cd : s.cand[w]) {
                 const double *cn = cd.gen ? &s.gcn[8 * (size_t)cd.src] : &inp.cn[8 * (size_t)cd.src];
                 const double *nx = op.norm(cd.t, sidx, cd.lx), *ny = op.norm(cd.t, sidx, cd.ly),
@@ -499,22 +509,26 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 pairs_tot += np_;
                 bool near = std::max(std::abs(cd.lx), std::max(std::abs(cd.ly), std::abs(cd.lz))) <= 1;
                 int tier;
-                if (!mixed || tthr < 0.0 || bd > TIER_FP64 * tthr || (near_fp64 && near))
+                if (!mixed || tthr < 0.0 || (near_fp64 && near))
                     tier = 0;
+                else if (df_only)
+                    tier = bd <= TIER_DF * tthr ? 3 : 0;
+                else if (bd > TIER_FP64 * tthr)
+                    tier = (dfp && bd <= TIER_DF * tthr) ? 3 : 0;
                 else if (tensor && !root && bd <= TIER_TF32 * tthr)
                     tier = 2;
                 else
                     tier = 1;
                 cd.tier = tier;
                 c[tier]++;
-                (tier == 0 ? pairs_t0 : tier == 1 ? pairs_t1 : pairs_t2) += np_;
+                (tier == 0 ? pairs_t0 : tier == 1 ? pairs_t1 : tier == 2 ? pairs_t2 : pairs_t3) += np_;
             }
             for (int k = 0; k < NTIER; k++) cnt[k][q + 1] = c[k];
         }
         // FP64 launch: every node (it writes the block); other tiers: nodes that have items there
         LevelItems *lt = G.lt;
         std::vector<long> slot[NTIER];
-        long nnt[NTIER] = {NN, 0, 0};
+        long nnt[NTIER] = {NN, 0, 0, 0};
         for (int k = 0; k < NTIER; k++) slot[k].assign(NN, -1);
         for (long q = 0; q < NN; q++) {
             slot[0][q] = q;
@@ -554,26 +568,29 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     T.ay[pi] = op.d_blocks + (size_t)byi * bsz;
                     T.az[pi] = op.d_blocks + (size_t)bzi * bsz;
                 } else {
-                    // FP32 and TF32 tiers read the FP32 cube-order shadows and the FP32 operator blocks
-                    T.in[pi] = cd.gen ? (const void *)(s.gbase32 + (size_t)cd.src * bs)
-                                      : (const void *)(inp.d_coefs32 + (size_t)cd.src * bs);
-                    T.ax[pi] = op.d_blocks32 + (size_t)bxi * bsz;
-                    T.ay[pi] = op.d_blocks32 + (size_t)byi * bsz;
-                    T.az[pi] = op.d_blocks32 + (size_t)bzi * bsz;
+                    // the reduced tiers read the FP32 cube-order shadows and the FP32 operator blocks
+                    // (high part first, low part after it)
+                    T.in[pi] = cd.gen ? (const void *)(s.gbase32 + 2 * (size_t)cd.src * bs)
+                                      : (const void *)(inp.d_coefs32 + 2 * (size_t)cd.src * bs);
+                    T.ax[pi] = op.d_blocks32 + 2 * (size_t)bxi * bsz;
+                    T.ay[pi] = op.d_blocks32 + 2 * (size_t)byi * bsz;
+                    T.az[pi] = op.d_blocks32 + 2 * (size_t)bzi * bsz;
                 }
                 T.coef[pi] = op.c[cd.t];
                 pi++;
             }
         }
-        st.items += ntot[0] + ntot[1] + ntot[2];
+        st.items += ntot[0] + ntot[1] + ntot[2] + ntot[3];
         st.items_fp64 += ntot[0];
         st.items_fp32 += ntot[1];
         st.items_tf32 += ntot[2];
+        st.items_df += ntot[3];
         st.flops += 6.0 * K4 * (double)pairs_tot;
-        st.flops_issued += 96.0 * K4 * (double)(ntot[0] + ntot[1] + ntot[2]);
+        st.flops_issued += 96.0 * K4 * (double)(ntot[0] + ntot[1] + ntot[2] + ntot[3]);
         st.flops_fp64 += 6.0 * K4 * (double)pairs_t0;
         st.flops_fp32 += 6.0 * K4 * (double)pairs_t1;
         st.flops_tf32 += 6.0 * K4 * (double)pairs_t2;
+        st.flops_df += 6.0 * K4 * (double)pairs_t3;
         st.host_items_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tB).count();
         MWG_CUDA(cudaEventRecord(G.ev[0], ctx.stream));
         G.tc_status = nullptr;
@@ -618,10 +635,11 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         check_status(G.tc_status);
         float ms_t[NTIER];
         for (int k = 0; k < NTIER; k++) MWG_CUDA(cudaEventElapsedTime(&ms_t[k], G.ev[k], G.ev[k + 1]));
-        kernel_ms += ms_t[0] + ms_t[1] + ms_t[2];
+        kernel_ms += ms_t[0] + ms_t[1] + ms_t[2] + ms_t[3];
         st.kernel_ms_fp64 += ms_t[0];
         st.kernel_ms_fp32 += ms_t[1];
         st.kernel_ms_tf32 += ms_t[2];
+        st.kernel_ms_df += ms_t[3];
         for (size_t j = 0; j < G.jobs.size(); j++) {
             JobState &s = js[G.jobs[j]];
             Tree &out = *s.job->out;

@@ -1,0 +1,248 @@
+// mw_apply_df.cu -- double-FP32 tier of the NS-form apply.
+//
+// The contraction of apply_kernel (mw_kernels.cu) with every value held as an
+// unevaluated pair of FP32 numbers (hi + lo, |lo| <= ulp(hi)/2), so that the
+// items whose bound is too large for the FP32 and TF32 tiers run on the FP32
+// pipe instead of GB300's FP64 pipe (1.06 TFLOP/s against 71 TFLOP/s FP32).
+//
+// Arithmetic (Dekker / Knuth error-free transformations, as used in double-
+// double libraries): a product a*b is p + e with p = fl(ah*bh) and
+// e = fma(ah, bh, -p) + ah*bl + al*bh (exact product error plus the cross
+// terms, al*bl dropped); a running sum keeps its high part exact by TwoSum and
+// collects every rounding error in its low part.  Every operation is an
+// explicitly rounded intrinsic (__fmul_rn, __fadd_rn, ...), so the compiler
+// cannot contract a product and a sum into one FMA and break the error terms.
+// Per pass the result is within about (K + 4) 2^-48 of sum |a||x|, so an item
+// is off by at most about 3e-13 b (b = its screening bound); the host gives
+// this tier the items with 2e6 < b / tau <= 1e11.
+//
+// Inputs: FP32 shadows in cube order, hi cube followed by lo cube; operator
+// blocks hi followed by lo.  Layout per CTA (one output node at a time, one
+// thread per output column (Y', X')): the input cube, T1 and the node
+// accumulator as (hi, lo) float2 in shared memory, the operator rows of the
+// x and y passes in registers.
+#include "mw_host.h"
+
+namespace mwg {
+
+namespace {
+
+// (sh, sl) += (ah + al) * (bh + bl)
+__device__ __forceinline__ void df_fma(float &sh, float &sl, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float t = __fadd_rn(sh, p);
+    const float bp = __fsub_rn(t, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+    sh = t;
+}
+
+// (h, l) += (bh, bl)
+__device__ __forceinline__ void df_add(float &h, float &l, float bh, float bl) {
+    const float t = __fadd_rn(h, bh);
+    const float bp = __fsub_rn(t, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bp)), __fsub_rn(bh, bp));
+    l = __fadd_rn(l, __fadd_rn(err, bl));
+    h = t;
+}
+
+// renormalise so that |l| <= ulp(h)/2
+__device__ __forceinline__ float2 df_norm(float h, float l) {
+    const float t = __fadd_rn(h, l);
+    return make_float2(t, __fsub_rn(l, __fsub_rn(t, h)));
+}
+
+template <int K>
+struct DfGeo {
+    static constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K;
+    static constexpr int THREADS = ((NC + 31) / 32) * 32;
+    // float2 units: IN, T1, ACC (C each), U (K^3); then floats: A hi (3 NC), A lo (3 NC)
+    static constexpr size_t SMEM = sizeof(float2) * (3 * (size_t)C + K3) + sizeof(float) * 6 * (size_t)NC;
+};
+
+template <int K>
+__global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLaunch L) {
+    using G = DfGeo<K>;
+    constexpr int N2 = G::N2, NC = G::NC, C = G::C, K3 = G::K3;
+    extern __shared__ __align__(16) float2 smem_df[];
+    float2 *s_in = smem_df;        // IN[Z][Y][X]
+    float2 *s_t1 = s_in + C;       // T1[Z][Y][X']
+    float2 *s_acc = s_t1 + C;      // node accumulator acc[Z'][Y'][X']
+    float2 *s_u = s_acc + C;       // u[Z][Y][X'], Z, Y, X' < K
+    float *s_Ah = reinterpret_cast<float *>(s_u + K3);  // A_x, A_y, A_z high parts
+    float *s_Al = s_Ah + 3 * NC;                        // low parts
+    __shared__ int s_node;
+    const int tid = threadIdx.x;
+    const bool active = tid < NC;
+    const int Yp = tid / N2, Xp = tid % N2;
+    const bool excl = !L.root && active && (Yp < K) && (Xp < K);
+
+    while (true) {
+        if (tid == 0) s_node = atomicAdd(L.counter, 1);
+        __syncthreads();
+        const int w = s_node;
+        if (w >= L.nnodes) break;
+        for (int i = tid; i < C; i += blockDim.x) s_acc[i] = make_float2(0.0f, 0.0f);
+        const long long b0 = L.begin[w], b1 = L.end[w];
+        for (long long j = b0; j < b1; j++) {
+            __syncthreads();
+            {
+                // hi and lo cubes -> interleaved (hi, lo) pairs
+                const float4 *gh = reinterpret_cast<const float4 *>(L.in[j]);
+                const float4 *gl = gh + C / 4;
+                float4 *s4 = reinterpret_cast<float4 *>(s_in);
+                for (int i = tid; i < C / 4; i += blockDim.x) {
+                    const float4 h = __ldg(gh + i), l = __ldg(gl + i);
+                    s4[2 * i] = make_float4(h.x, l.x, h.y, l.y);
+                    s4[2 * i + 1] = make_float4(h.z, l.z, h.w, l.w);
+                }
+                const float *ax = reinterpret_cast<const float *>(L.ax[j]);
+                const float *ay = reinterpret_cast<const float *>(L.ay[j]);
+                const float *az = reinterpret_cast<const float *>(L.az[j]);
+                for (int i = tid; i < 3 * NC; i += blockDim.x) {
+                    const int d = i / NC, r = i - d * NC;
+                    const float *op = d == 0 ? ax : (d == 1 ? ay : az);
+                    s_Ah[i] = __ldg(op + r);
+                    s_Al[i] = __ldg(op + NC + r);
+                }
+            }
+            const double cfd = L.coef[j];
+            const float cfh = (float)cfd, cfl = (float)(cfd - (double)cfh);
+            __syncthreads();
+            if (active) {  // x pass, thread (Y = Yp, X' = Xp)
+                float ah[N2], al[N2];
+#pragma unroll
+                for (int X = 0; X < N2; X++) {
+                    ah[X] = s_Ah[Xp * N2 + X];
+                    al[X] = s_Al[Xp * N2 + X];
+                }
+#pragma unroll 2
+                for (int Z = 0; Z < N2; Z++) {
+                    const float2 *src = s_in + (Z * N2 + Yp) * N2;
+                    float s0h = 0.0f, s0l = 0.0f, s1h = 0.0f, s1l = 0.0f;
+#pragma unroll
+                    for (int X = 0; X < K; X++) {
+                        const float2 v = src[X];
+                        df_fma(s0h, s0l, ah[X], al[X], v.x, v.y);
+                    }
+#pragma unroll
+                    for (int X = K; X < N2; X++) {
+                        const float2 v = src[X];
+                        df_fma(s1h, s1l, ah[X], al[X], v.x, v.y);
+                    }
+                    float th = s0h, tl = s0l;
+                    df_add(th, tl, s1h, s1l);
+                    s_t1[(Z * N2 + Yp) * N2 + Xp] = df_norm(th, tl);
+                    if (excl && Z < K) s_u[(Z * K + Yp) * K + Xp] = df_norm(s1h, s1l);
+                }
+            }
+            __syncthreads();
+            if (active) {  // y and z passes, thread (Y' = Yp, X' = Xp)
+                float ayh[N2], ayl[N2];
+#pragma unroll
+                for (int Y = 0; Y < N2; Y++) {
+                    ayh[Y] = s_Ah[NC + Yp * N2 + Y];
+                    ayl[Y] = s_Al[NC + Yp * N2 + Y];
+                }
+                float2 t2[N2], t2x[K];
+#pragma unroll
+                for (int Z = 0; Z < N2; Z++) {
+                    float s0h = 0.0f, s0l = 0.0f, s1h = 0.0f, s1l = 0.0f;
+#pragma unroll
+                    for (int Y = 0; Y < K; Y++) {
+                        const float2 v = s_t1[(Z * N2 + Y) * N2 + Xp];
+                        df_fma(s0h, s0l, ayh[Y], ayl[Y], v.x, v.y);
+                    }
+#pragma unroll
+                    for (int Y = K; Y < N2; Y++) {
+                        const float2 v = s_t1[(Z * N2 + Y) * N2 + Xp];
+                        df_fma(s1h, s1l, ayh[Y], ayl[Y], v.x, v.y);
+                    }
+                    if (Z < K) {
+                        // t2x: u replaces T1 for Y < K (the scaling-scaling path in x and y left out)
+                        float xh = 0.0f, xl = 0.0f;
+                        if (excl) {
+#pragma unroll
+                            for (int Y = 0; Y < K; Y++) {
+                                const float2 v = s_u[(Z * K + Y) * K + Xp];
+                                df_fma(xh, xl, ayh[Y], ayl[Y], v.x, v.y);
+                            }
+                        }
+                        df_add(xh, xl, s1h, s1l);
+                        t2x[Z < K ? Z : 0] = df_norm(xh, xl);
+                    }
+                    df_add(s0h, s0l, s1h, s1l);
+                    t2[Z] = df_norm(s0h, s0l);
+                }
+#pragma unroll 2
+                for (int Zp = 0; Zp < N2; Zp++) {
+                    const float *azh = s_Ah + 2 * NC + Zp * N2, *azl = s_Al + 2 * NC + Zp * N2;
+                    float sh = 0.0f, sl = 0.0f;
+#pragma unroll
+                    for (int Z = 0; Z < N2; Z++) {
+                        float2 v = t2[Z];
+                        if (Zp < K && Z < K && excl) v = t2x[Z < K ? Z : 0];
+                        df_fma(sh, sl, azh[Z], azl[Z], v.x, v.y);
+                    }
+                    const float2 sn = df_norm(sh, sl);
+                    float2 &a = s_acc[(Zp * N2 + Yp) * N2 + Xp];
+                    float ah_ = a.x, al_ = a.y;
+                    df_fma(ah_, al_, cfh, cfl, sn.x, sn.y);
+                    a = df_norm(ah_, al_);
+                }
+            }
+        }
+        __syncthreads();
+        if (active) {
+            double *out = L.out[w];
+#pragma unroll 4
+            for (int Zp = 0; Zp < N2; Zp++) {
+                const int c = (Xp >= K ? 1 : 0) | (Yp >= K ? 2 : 0) | (Zp >= K ? 4 : 0);
+                const int gi = c * K3 + (Zp % K) * K * K + (Yp % K) * K + (Xp % K);
+                const float2 a = s_acc[(Zp * N2 + Yp) * N2 + Xp];
+                const double v = (double)a.x + (double)a.y;
+                if (L.set)
+                    out[gi] = v;
+                else
+                    out[gi] += v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int K>
+void launch_df(const ApplyLaunch &L, int nsm, cudaStream_t s) {
+    using G = DfGeo<K>;
+    MWG_CUDA(cudaFuncSetAttribute(apply_df_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
+    int per_sm = 0;
+    MWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, apply_df_kernel<K>, G::THREADS, G::SMEM));
+    if (per_sm < 1) per_sm = 1;
+    int grid = nsm * per_sm;
+    if (grid > L.nnodes) grid = L.nnodes;
+    if (grid < 1) return;
+    apply_df_kernel<K><<<grid, G::THREADS, G::SMEM, s>>>(L);
+    MWG_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+void k_apply_df(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s) {
+    if (L.nnodes <= 0) return;
+    MWG_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(int), s));
+    switch (b.K) {
+        case 4: launch_df<4>(L, nsm, s); break;
+        case 5: launch_df<5>(L, nsm, s); break;
+        case 6: launch_df<6>(L, nsm, s); break;
+        case 7: launch_df<7>(L, nsm, s); break;
+        case 8: launch_df<8>(L, nsm, s); break;
+        case 9: launch_df<9>(L, nsm, s); break;
+        case 10: launch_df<10>(L, nsm, s); break;
+        default: throw Error(MW_ERR_ARG, "no double-FP32 apply kernel for this order");
+    }
+}
+
+}  // namespace mwg

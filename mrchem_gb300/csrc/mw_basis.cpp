@@ -418,14 +418,21 @@ void Oper::build(const Basis &b) {
             if (q % 4 > 0) xmax[i] = std::max(xmax[i], ts[i].nrm[q]);
         }
     }
-    // device copies: FP64, and FP32 for the FP32 and TF32 tiers (the TF32 kernel rounds on load)
+    // device copies: FP64, and FP32 for the reduced tiers.  Each FP32 block is its high part (the
+    // value rounded to FP32, read by the FP32 and TF32 tiers) followed by its low part (the
+    // rounded remainder, read with the high part by the double-FP32 tier).
     size_t nel = blocks.size();
-    std::vector<float> b32(nel);
-    for (size_t i = 0; i < nel; i++) b32[i] = (float)blocks[i];
+    std::vector<float> b32(2 * nel);
+    for (size_t i = 0; i < nel; i++) {
+        const size_t blk = i / (size_t)bsz, r = i - blk * (size_t)bsz;
+        const float h = (float)blocks[i];
+        b32[2 * blk * bsz + r] = h;
+        b32[2 * blk * bsz + bsz + r] = (float)(blocks[i] - (double)h);
+    }
     MWG_CUDA(cudaMalloc(&d_blocks, sizeof(double) * nel));
-    MWG_CUDA(cudaMalloc(&d_blocks32, sizeof(float) * nel));
+    MWG_CUDA(cudaMalloc(&d_blocks32, sizeof(float) * 2 * nel));
     MWG_CUDA(cudaMemcpy(d_blocks, blocks.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
-    MWG_CUDA(cudaMemcpy(d_blocks32, b32.data(), sizeof(float) * nel, cudaMemcpyHostToDevice));
+    MWG_CUDA(cudaMemcpy(d_blocks32, b32.data(), sizeof(float) * 2 * nel, cudaMemcpyHostToDevice));
 }
 
 }  // namespace mwg

@@ -396,7 +396,7 @@ int mw_op_block(mw_op o, int term, int scale, int l, double *blk, double *norms4
 int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const mw_tree *prec_trees, int max_iter,
              int abs_prec, int precision_mode) {
     if (!out || !op || !inp || !(prec > 0.0) || nprec < 0 || (nprec > 0 && !prec_trees)) return MW_ERR_ARG;
-    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_MIXED_FP32) return MW_ERR_ARG;
+    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_DF) return MW_ERR_ARG;
     if (out == inp) return MW_ERR_ARG;
     mwg::Ctx *ctx = ctx_of(out);
     return guard(ctx, [&] {
@@ -415,7 +415,7 @@ int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const m
 int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *nprec,
                    const mw_tree *prec_trees, int max_iter, int abs_prec, int precision_mode) {
     if (n < 1 || !precs || !outs || !ops || !inps) return MW_ERR_ARG;
-    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_MIXED_FP32) return MW_ERR_ARG;
+    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_DF) return MW_ERR_ARG;
     for (int i = 0; i < n; i++)
         if (!outs[i] || !ops[i] || !inps[i] || !(precs[i] > 0.0) || outs[i] == inps[i]) return MW_ERR_ARG;
     mwg::Ctx *ctx = ctx_of(outs[0]);
@@ -439,7 +439,7 @@ int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tre
 
 int mw_apply_fixed(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec, int precision_mode) {
     if (!out || !op || !inp || !(prec > 0.0) || out == inp) return MW_ERR_ARG;
-    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_MIXED_FP32) return MW_ERR_ARG;
+    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_DF) return MW_ERR_ARG;
     mwg::Ctx *ctx = ctx_of(out);
     return guard(ctx, [&] {
         std::vector<mwg::ApplyJob> jobs(1);

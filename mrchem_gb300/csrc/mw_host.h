@@ -93,7 +93,7 @@ struct Tree {
     std::vector<double> cn;       // 8 component norms per node (host copy)
     double *d_coefs = nullptr;    // cap * bs
     double *d_cn = nullptr;       // cap * 8
-    float *d_coefs32 = nullptr;   // FP32 shadow (mixed-precision applies), cap32 blocks
+    float *d_coefs32 = nullptr;   // FP32 shadow (mixed-precision applies): cap32 x (high cube, low cube)
     size_t cap = 0, cap32 = 0;
     int nroots = 0;
 
@@ -125,7 +125,7 @@ struct Oper {
     std::vector<double> amax, xmax;  // per (t,s)
     long nblocks = 0;
     double *d_blocks = nullptr;  // (2K)^2 per block, FP64
-    float *d_blocks32 = nullptr; // FP32 copy
+    float *d_blocks32 = nullptr; // FP32 copy: per block the high part, then the low part (2 x (2K)^2)
     const double *norm(int t, int s, int l) const { return &norms[(size_t)(off[t * S + s] + l + band[t * S + s]) * 4]; }
     long block_index(int t, int s, int l) const { return off[t * S + s] + l + band[t * S + s]; }
     void build(const Basis &b);
@@ -248,6 +248,8 @@ void k_generate(const DevBasis &b, const GenTask *tasks, int n, cudaStream_t s);
 void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s);
 // TF32 tensor-core tier: FP32 cube-order input blocks and FP32 operator blocks, as the FP32 tier
 void k_apply_tc(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s);
+// double-FP32 tier: reads the high and low parts of the same shadows and operator blocks
+void k_apply_df(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s);
 void k_norms(const DevBasis &b, double *const *blocks, double *const *cn, int n, cudaStream_t s);
 void k_topdown(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s);
 void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s);
@@ -255,7 +257,8 @@ void k_multiply(const DevBasis &b, const MulTask *tasks, int n, cudaStream_t s);
 void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
            cudaStream_t s);
 void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);
-// FP32 copy of whole blocks, each written in cube order cube[Z][Y][X] (X = cx*K + ix)
+// FP32 shadow of whole blocks in cube order cube[Z][Y][X] (X = cx*K + ix): per block a high cube
+// and a low cube (2 * 8K^3 floats, the low one holds the rounded remainder)
 void k_to_fp32_cube(const double *in, float *out, size_t nblocks, int K, cudaStream_t s);
 void k_dot(const double *const *a, const double *const *b, const int *start, int n, int bs, double *partial,
            cudaStream_t s);

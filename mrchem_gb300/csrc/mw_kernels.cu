@@ -620,13 +620,18 @@ __global__ void to_fp32_kernel(const double *in, float *out, size_t n) {
         out[i] = (float)in[i];
 }
 
-// FP32 copy of nblocks blocks, each written in cube order cube[Z][Y][X]
+// FP32 shadow of nblocks blocks, each written in cube order cube[Z][Y][X] as a high cube
+// (the value rounded to FP32) followed by a low cube (the rounded remainder)
 __global__ void to_fp32_cube_kernel(const double *in, float *out, size_t nblocks, int K) {
     const size_t bs = 8 * (size_t)K * K * K, n = nblocks * bs;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         size_t b = i / bs;
         int gi = (int)(i - b * bs);
-        out[b * bs + cube_of_block(gi, K)] = (float)in[i];
+        const double x = in[i];
+        const float h = (float)x;
+        float *o = out + 2 * b * bs + cube_of_block(gi, K);
+        o[0] = h;
+        o[bs] = (float)(x - (double)h);
     }
 }
 
