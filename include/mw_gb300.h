@@ -99,10 +99,11 @@ const char *mw_last_error(mw_ctx ctx);
 int mw_ctx_basis(mw_ctx ctx, double *qx, double *qw, double *filter, double *c2v, double *v2c);
 int mw_ctx_last_stats(mw_ctx ctx, mw_stats *st);
 int mw_ctx_synchronize(mw_ctx ctx);
-/* Batched applies split their jobs into two groups on two streams and prepare one group's level
- * on the host while the GPU computes the other's (on = 1, the default).  With on = 0 the groups
- * are not formed: the tier kernels then run alone, so their CUDA-event times in mw_stats are
- * exclusive.  No counterpart in the reference (its applies are one per call). */
+/* Batched applies split their jobs into up to four groups on their own streams and prepare one
+ * group's level on the host while the GPU computes the others' (on = 1, the default).  With
+ * on = 0 the groups are not formed: the tier kernels then run alone, so their CUDA-event times in
+ * mw_stats are exclusive.  Results are bit-identical either way.  No counterpart in the reference
+ * (its applies are one per call). */
 int mw_ctx_set_overlap(mw_ctx ctx, int on);
 
 /* ---- trees (replaces FunctionTree<3>, src/qmfunctions/Orbital.h:51) ---- */

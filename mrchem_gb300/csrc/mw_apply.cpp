@@ -201,26 +201,35 @@ void enumerate_node(JobState &js, int w, int s, bool root, double thr, LookupCac
 }
 
 struct LevelItems {
-    // per tier: node list, begin offsets, item SoA
+    // per tier: node list, begin offsets, item SoA.  The arrays only grow; `nodes` and `items`
+    // are the level's counts, and the fill writes every entry below them.
+    long nodes = 0;
+    long long items = 0;
     std::vector<double *> out;
     std::vector<long long> begin;
     std::vector<const void *> in, ax, ay, az;
     std::vector<double> coef;
-    void resize(long nodes, long long items) {
-        out.assign(nodes, nullptr);
-        begin.assign(nodes + 1, 0);
-        in.assign(items, nullptr);
-        ax.assign(items, nullptr);
-        ay.assign(items, nullptr);
-        az.assign(items, nullptr);
-        coef.assign(items, 0.0);
+    void resize(long n, long long m) {
+        nodes = n;
+        items = m;
+        if ((long)out.size() < n) out.resize(n);
+        if ((long)begin.size() < n + 1) begin.resize(n + 1);
+        begin[0] = 0;
+        if ((long long)in.size() < m) {
+            in.resize(m);
+            ax.resize(m);
+            ay.resize(m);
+            az.resize(m);
+            coef.resize(m);
+        }
     }
 };
 
 // tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores, 3 double-FP32.  Returns the pinned host copy of the
 // launch's status word (read it after the stream has been synchronised), or nullptr.
 int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, int tier, mw_stats &st) {
-    int nn = (int)li.out.size();
+    const int nn = (int)li.nodes;
+    const size_t ni = (size_t)li.items;
     if (nn == 0) return nullptr;
     // nodes in decreasing item count (longest first) for the persistent grid's dynamic
     // scheduler; each node's own items keep their order, so results do not change
@@ -240,11 +249,11 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     pk.add(outp.data(), outp.size() * sizeof(double *));
     pk.add(beg.data(), beg.size() * sizeof(long long));
     pk.add(end.data(), end.size() * sizeof(long long));
-    pk.add(li.in.data(), li.in.size() * sizeof(void *));
-    pk.add(li.ax.data(), li.ax.size() * sizeof(void *));
-    pk.add(li.ay.data(), li.ay.size() * sizeof(void *));
-    pk.add(li.az.data(), li.az.size() * sizeof(void *));
-    pk.add(li.coef.data(), li.coef.size() * sizeof(double));
+    pk.add(li.in.data(), ni * sizeof(void *));
+    pk.add(li.ax.data(), ni * sizeof(void *));
+    pk.add(li.ay.data(), ni * sizeof(void *));
+    pk.add(li.az.data(), ni * sizeof(void *));
+    pk.add(li.coef.data(), ni * sizeof(double));
     pk.ship(ctx, arena);
     int *counter = (int *)arena.alloc(2 * sizeof(int));
     ApplyLaunch L;
@@ -334,10 +343,10 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             if (s.job->out->nodes[i].n == n) s.work.push_back(i);
     };
 
-    // The jobs are split into two groups that take turns: while the GPU runs one group's level,
-    // the host enumerates, screens and builds the items of the other group's level.  Group 0
-    // works on the context's stream and arena, group 1 on a second stream and arena of the
-    // context.  A single job runs as one group.
+    // The jobs are split into up to four groups that take turns: while the GPU runs the other
+    // groups' levels, the host enumerates, screens and builds the items of one group's level.
+    // Group 0 works on the context's stream and arena, the others on extra streams and arenas of
+    // the context.  A single job runs as one group.
     struct Group {
         std::vector<int> jobs;
         cudaStream_t stream = nullptr;
@@ -356,16 +365,16 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         StreamSwap(Ctx &c_, cudaStream_t s) : c(c_), saved(c_.stream) { c.stream = s; }
         ~StreamSwap() { c.stream = saved; }
     };
-    const int ngroups = (ctx.overlap && jobs.size() >= 2) ? 2 : 1;
+    const int ngroups = std::max(1, std::min<int>(ctx.groups, (int)jobs.size()));
     std::vector<Group> groups(ngroups);
     {
-        // balance the groups by input size, largest jobs first
+        // balance the groups by input size, largest jobs first into the lightest group
         std::vector<int> ord(jobs.size());
         for (size_t j = 0; j < jobs.size(); j++) ord[j] = (int)j;
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return jobs[a].inp->nn() > jobs[c].inp->nn(); });
-        long load[2] = {0, 0};
+        std::vector<long> load(ngroups, 0);
         for (int j : ord) {
-            int g = (ngroups == 2 && load[1] < load[0]) ? 1 : 0;
+            int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
             groups[g].jobs.push_back(j);
             load[g] += jobs[j].inp->nn();
         }
@@ -373,17 +382,21 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     }
     groups[0].stream = ctx.stream;
     groups[0].arena = &arena;
-    cudaEvent_t ev_start = nullptr, ev_g1 = nullptr;
-    if (ngroups == 2) {
-        if (!ctx.stream2) MWG_CUDA(cudaStreamCreateWithFlags(&ctx.stream2, cudaStreamNonBlocking));
-        ctx.arena2.reset();
-        groups[1].stream = ctx.stream2;
-        groups[1].arena = &ctx.arena2;
-        // group 1 starts after the set-up queued on the context's stream (FP32 shadows, zeroed roots)
+    cudaEvent_t ev_start = nullptr;
+    std::vector<cudaEvent_t> ev_end(ngroups, nullptr);
+    if (ngroups > 1) {
+        // groups 1.. start after the set-up queued on the context's stream (FP32 shadows, zeroed roots)
         MWG_CUDA(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
-        MWG_CUDA(cudaEventCreateWithFlags(&ev_g1, cudaEventDisableTiming));
         MWG_CUDA(cudaEventRecord(ev_start, ctx.stream));
-        MWG_CUDA(cudaStreamWaitEvent(ctx.stream2, ev_start, 0));
+        for (int g = 1; g < ngroups; g++) {
+            cudaStream_t &xs = ctx.xstream[g - 1];
+            if (!xs) MWG_CUDA(cudaStreamCreateWithFlags(&xs, cudaStreamNonBlocking));
+            ctx.xarena[g - 1].reset();
+            groups[g].stream = xs;
+            groups[g].arena = &ctx.xarena[g - 1];
+            MWG_CUDA(cudaStreamWaitEvent(xs, ev_start, 0));
+            MWG_CUDA(cudaEventCreateWithFlags(&ev_end[g], cudaEventDisableTiming));
+        }
     }
     for (auto &g : groups)
         for (auto &e : g.ev) MWG_CUDA(cudaEventCreate(&e));
@@ -686,15 +699,16 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         }
         if (!active) break;
     }
-    if (ngroups == 2) {
-        // the post-processing on the context's stream follows group 1's last work
-        MWG_CUDA(cudaEventRecord(ev_g1, ctx.stream2));
-        MWG_CUDA(cudaStreamWaitEvent(ctx.stream, ev_g1, 0));
+    // the post-processing on the context's stream follows every group's last work
+    for (int g = 1; g < ngroups; g++) {
+        MWG_CUDA(cudaEventRecord(ev_end[g], groups[g].stream));
+        MWG_CUDA(cudaStreamWaitEvent(ctx.stream, ev_end[g], 0));
     }
     for (auto &g : groups)
         for (auto &e : g.ev) cudaEventDestroy(e);
     if (ev_start) cudaEventDestroy(ev_start);
-    if (ev_g1) cudaEventDestroy(ev_g1);
+    for (auto &e : ev_end)
+        if (e) cudaEventDestroy(e);
     // input bytes: every distinct input block read once per apply (FP64 or FP32 shadow) + operator blocks
     for (auto &s : js) st.bytes += 8.0 * bs * (double)s.job->inp->nn();
 
@@ -1026,7 +1040,7 @@ void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats 
             }
         }
         std::stable_sort(items.begin(), items.end(), [](const TItem &a, const TItem &b2) { return a.target < b2.target; });
-        li.resize(0, 0);
+        li = LevelItems();
         li.begin.assign(1, 0);
         for (size_t q = 0; q < items.size(); q++) {
             const TItem &it = items[q];
@@ -1041,6 +1055,8 @@ void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats 
             li.coef.push_back(op.c[it.c->t]);
         }
         if (!items.empty()) li.begin.push_back((long long)items.size());
+        li.nodes = (long)li.out.size();
+        li.items = (long long)items.size();
         st.items += (long long)items.size();
         st.items_fp64 += (long long)items.size();
         st.out_nodes += (long long)li.out.size();

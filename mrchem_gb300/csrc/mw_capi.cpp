@@ -110,13 +110,15 @@ int mw_ctx_create(int device, int root_scale, const int corner[3], const int box
 static void ctx_free(mw_ctx c) {
     cudaSetDevice(c->ctx.device);
     cudaStreamSynchronize(c->ctx.stream);
-    if (c->ctx.stream2) cudaStreamSynchronize(c->ctx.stream2);
+    for (auto &xs : c->ctx.xstream)
+        if (xs) cudaStreamSynchronize(xs);
     c->ctx.arena.release();
-    c->ctx.arena2.release();
+    for (auto &xa : c->ctx.xarena) xa.release();
     if (c->ctx.h_pinned) cudaFreeHost(c->ctx.h_pinned);
     if (c->ctx.d_basis) cudaFree(c->ctx.d_basis);
     cudaStreamDestroy(c->ctx.stream);
-    if (c->ctx.stream2) cudaStreamDestroy(c->ctx.stream2);
+    for (auto &xs : c->ctx.xstream)
+        if (xs) cudaStreamDestroy(xs);
     delete c;
 }
 
@@ -158,7 +160,7 @@ int mw_ctx_synchronize(mw_ctx c) {
 
 int mw_ctx_set_overlap(mw_ctx c, int on) {
     if (!c || (on != 0 && on != 1)) return MW_ERR_ARG;
-    c->ctx.overlap = on != 0;
+    c->ctx.groups = on ? mwg::Ctx::XGROUPS + 1 : 1;
     return MW_OK;
 }
 

@@ -161,11 +161,13 @@ struct Ctx {
     int live = 0;           // trees and operators created through the C ABI and not yet destroyed
     bool closing = false;   // destroyed by the caller; released when live drops to 0
     Arena arena;
-    // second stream and arena: the batched apply runs half of its jobs there, so that the host
-    // prepares one half's level while the GPU computes the other half's
-    cudaStream_t stream2 = nullptr;
-    Arena arena2;
-    bool overlap = true;
+    // extra streams and arenas: the batched apply splits its jobs into up to XGROUPS + 1 groups
+    // (group 0 on `stream` / `arena`), so that the host prepares one group's level while the GPU
+    // computes the others'
+    static constexpr int XGROUPS = 3;
+    cudaStream_t xstream[XGROUPS] = {};
+    Arena xarena[XGROUPS];
+    int groups = XGROUPS + 1;  // job groups of a batched apply (1: no overlap)
     void *h_pinned = nullptr;
     size_t pinned_bytes = 0;
     void *pinned(size_t bytes);

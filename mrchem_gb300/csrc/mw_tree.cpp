@@ -121,8 +121,21 @@ void Packer::ship(Ctx &ctx, Arena &arena) {
     // staging lives in the arena's pinned chunks until the arena is reset, so packing never
     // waits for earlier copies or kernels
     char *h = (char *)arena.halloc(total);
-    for (size_t i = 0; i < srcs.size(); i++)
-        if (size[i]) std::memcpy(h + offs[i], srcs[i], size[i]);
+    if (total < ((size_t)1 << 20)) {
+        for (size_t i = 0; i < srcs.size(); i++)
+            if (size[i]) std::memcpy(h + offs[i], srcs[i], size[i]);
+    } else {
+        // large packs (the item lists of a level): 256 KiB pieces copied by all host threads
+        constexpr size_t PIECE = (size_t)1 << 18;
+        std::vector<std::pair<size_t, size_t>> pieces;  // (array, offset in it)
+        for (size_t i = 0; i < srcs.size(); i++)
+            for (size_t o = 0; o < size[i]; o += PIECE) pieces.push_back({i, o});
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long p = 0; p < (long)pieces.size(); p++) {
+            const size_t i = pieces[p].first, o = pieces[p].second;
+            std::memcpy(h + offs[i] + o, (const char *)srcs[i] + o, std::min(PIECE, size[i] - o));
+        }
+    }
     dev = (char *)arena.alloc(total);
     MWG_CUDA(cudaMemcpyAsync(dev, h, total, cudaMemcpyHostToDevice, ctx.stream));
 }
