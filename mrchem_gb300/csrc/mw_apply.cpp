@@ -50,33 +50,38 @@ constexpr double BOUND_PRUNE = 8.0 * 2.8285;  // (sum_f |in_f|) / |block| <= sqr
 
 double split_thr(double prec, double R, int n) { return prec * R * std::pow(2.0, -0.5 * (n + 1)); }
 
+// b = sum_ft |in_ft| s(ft), s(ft) = sum_gt prod_d |A_d^{g_d f_d}|.  For ft != 0 (and at the root)
+// the sum over gt factorises into prod_d (|A_d^{0 f_d}| + |A_d^{1 f_d}|); for ft = 0 below the root
+// the (0,0) pair is left out and the 7 other products are summed one by one (no cancellation).
 inline double item_bound(const double *nx, const double *ny, const double *nz, const double *cn, bool root) {
+    const double cx[2] = {nx[0] + nx[2], nx[1] + nx[3]}, cy[2] = {ny[0] + ny[2], ny[1] + ny[3]},
+                 cz[2] = {nz[0] + nz[2], nz[1] + nz[3]};
     double b = 0.0;
-    for (int ft = 0; ft < 8; ft++) {
-        if (cn[ft] == 0.0) continue;
-        int fx = ft & 1, fy = (ft >> 1) & 1, fz = (ft >> 2) & 1;
+    if (cn[0] != 0.0) {
         double s = 0.0;
-        for (int gt = 0; gt < 8; gt++) {
-            if (!root && ft == 0 && gt == 0) continue;
-            int gx = gt & 1, gy = (gt >> 1) & 1, gz = (gt >> 2) & 1;
-            s += nx[2 * gx + fx] * ny[2 * gy + fy] * nz[2 * gz + fz];
+        if (root) {
+            s = cx[0] * cy[0] * cz[0];
+        } else {
+            for (int gt = 1; gt < 8; gt++) s += nx[2 * (gt & 1)] * ny[2 * ((gt >> 1) & 1)] * nz[2 * (gt >> 2)];
         }
-        b += cn[ft] * s;
+        b += cn[0] * s;
     }
+    for (int ft = 1; ft < 8; ft++)
+        if (cn[ft] != 0.0) b += cn[ft] * (cx[ft & 1] * cy[(ft >> 1) & 1] * cz[ft >> 2]);
     return b;
 }
 
 // component pairs with a non-zero contraction (the algorithmic work unit, 6 K^4 flops each)
 inline int item_pairs(const double *nx, const double *ny, const double *nz, const double *cn, bool root) {
+    // non-zero sub-blocks per dimension and input half, multiplied over the dimensions
+    const int ex[2] = {(nx[0] != 0.0) + (nx[2] != 0.0), (nx[1] != 0.0) + (nx[3] != 0.0)},
+              ey[2] = {(ny[0] != 0.0) + (ny[2] != 0.0), (ny[1] != 0.0) + (ny[3] != 0.0)},
+              ez[2] = {(nz[0] != 0.0) + (nz[2] != 0.0), (nz[1] != 0.0) + (nz[3] != 0.0)};
     int p = 0;
     for (int ft = 0; ft < 8; ft++) {
         if (cn[ft] == 0.0) continue;
-        int fx = ft & 1, fy = (ft >> 1) & 1, fz = (ft >> 2) & 1;
-        for (int gt = 0; gt < 8; gt++) {
-            if (!root && ft == 0 && gt == 0) continue;
-            int gx = gt & 1, gy = (gt >> 1) & 1, gz = (gt >> 2) & 1;
-            if (nx[2 * gx + fx] != 0.0 && ny[2 * gy + fy] != 0.0 && nz[2 * gz + fz] != 0.0) p++;
-        }
+        p += ex[ft & 1] * ey[(ft >> 1) & 1] * ez[ft >> 2];
+        if (!root && ft == 0 && nx[0] != 0.0 && ny[0] != 0.0 && nz[0] != 0.0) p--;
     }
     return p;
 }
@@ -109,6 +114,7 @@ struct Cand {
     int src;   // input node index, or generated slot
     int gen;   // 1: src is a generated slot (ancestor index before generation)
     int tier;  // after screening: -1 skipped, 0 FP64, 1 FP32, 2 TF32 tensor cores, 3 double-FP32
+    double bd; // bound: exact for real inputs, from the ancestor's norm for generated ones
 };
 
 struct JobState {
@@ -193,7 +199,7 @@ void enumerate_node(JobState &js, int w, int s, bool root, double thr, LookupCac
                     }
                     double bd = item_bound(nx, ny, nz, cn, root);
                     if (!root && bd < thr) continue;
-                    out.push_back(Cand{t, lx, ly, lz, ce >= 0 ? ce : -(ce + 4), ce >= 0 ? 0 : 1, -1});
+                    out.push_back(Cand{t, lx, ly, lz, ce >= 0 ? ce : -(ce + 4), ce >= 0 ? 0 : 1, -1, bd});
                 }
             }
         }
@@ -448,9 +454,10 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         }
         auto tB = std::chrono::steady_clock::now();
         st.host_enum_ms += std::chrono::duration<double, std::milli>(tB - tA).count();
-        // phase B: generated input nodes
-        for (JobState *sp : jp) {
-            JobState &s = *sp;
+        // phase B: generated input nodes (each job has its own set: jobs in parallel, each in order)
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long j = 0; j < (long)jp.size(); j++) {
+            JobState &s = *jp[j];
             s.gens.clear();
             for (size_t w = 0; w < s.work.size(); w++) {
                 const NodeInfo &o = s.job->out->nodes[s.work[w]];
@@ -513,7 +520,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 const double *cn = cd.gen ? &s.gcn[8 * (size_t)cd.src] : &inp.cn[8 * (size_t)cd.src];
                 const double *nx = op.norm(cd.t, sidx, cd.lx), *ny = op.norm(cd.t, sidx, cd.ly),
                              *nz = op.norm(cd.t, sidx, cd.lz);
-                double bd = item_bound(nx, ny, nz, cn, root);
+                // real inputs keep their bound from the enumeration; generated ones get their own
+                const double bd = cd.gen ? item_bound(nx, ny, nz, cn, root) : cd.bd;
                 if (!root && bd < thr) {
                     cd.tier = -1;
                     continue;
