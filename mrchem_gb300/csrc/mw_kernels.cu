@@ -388,24 +388,31 @@ __device__ __forceinline__ void lds_row(float (&r)[N], const float *p) {
 }
 
 // FP32 tier of the NS-form apply.  Same contraction and exclusion as
-// apply_kernel, arranged so that every shared-memory read is a vector read of
-// a contiguous row: the x pass stores t1 transposed as t1T[Z][X'][Y], the
-// y pass reads rows of t1T, the z pass reads rows of A_z.  The FP32 partial
-// sum of the node is added once to its FP64 block.
+// apply_kernel, arranged so that shared-memory reads are vector reads that a
+// warp mostly shares: the x pass (thread (Y, X'), X' fastest) reads rows of the
+// input cube and stores t1 transposed as t1T[Z][X'][Y]; the y and z passes use
+// the mapping (Y', X') with Y' fastest, so that the lanes of a warp read the
+// same one or two rows of t1T, and hold their A_y row in registers; the node
+// accumulator acc[Z'][X'][Y'] (Y' fastest) lives in shared memory (two CTAs
+// per SM).  The FP32 partial sum of the node is added once to its FP64 block.
 template <int K>
 __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kernel(ApplyLaunch L) {
     constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K, U = ((K3 + 3) / 4) * 4;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *s_in = reinterpret_cast<float *>(smem_raw);
     float *s_t1 = s_in + C;   // t1T[Z][X'][Y]
-    float *s_acc = s_t1 + C;  // node accumulator acc[Z'][Y'][X'] (kept in shared memory: two CTAs per SM)
+    float *s_acc = s_t1 + C;  // node accumulator acc[Z'][X'][Y']
     float *s_u = s_acc + C;   // u[Z][X'][Y], Z, X', Y < K
     float *s_A = s_u + U;
     __shared__ int s_node;
     const int tid = threadIdx.x;
     const bool active = tid < NC;
+    // x pass: thread (Y = Yp, X' = Xp), X' fastest
     const int Yp = tid / N2, Xp = tid % N2;
     const bool excl = !L.root && active && (Yp < K) && (Xp < K);
+    // y and z passes, epilogue: thread (Y' = Yq, X' = Xq), Y' fastest
+    const int Xq = tid / N2, Yq = tid % N2;
+    const bool exq = !L.root && active && (Yq < K) && (Xq < K);
 
     while (true) {
         if (tid == 0) s_node = atomicAdd(L.counter, 1);
@@ -447,13 +454,13 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kerne
                 }
             }
             __syncthreads();
-            if (active) {  // y and z passes, thread (Y' = Yp, X' = Xp)
+            if (active) {  // y and z passes, thread (Y' = Yq, X' = Xq)
                 float ayr[N2], t2[N2], t2x[K];
-                lds_row<N2>(ayr, s_A + NC + Yp * N2);
+                lds_row<N2>(ayr, s_A + NC + Yq * N2);
 #pragma unroll
                 for (int Z = 0; Z < N2; Z++) {
                     float row[N2];
-                    lds_row<N2>(row, s_t1 + (Z * N2 + Xp) * N2);
+                    lds_row<N2>(row, s_t1 + (Z * N2 + Xq) * N2);
                     float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
                     for (int Y = 0; Y < K; Y++) s0 = fmaf(ayr[Y], row[Y], s0);
@@ -462,8 +469,8 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kerne
                     t2[Z] = s0 + s1;
                     if (Z < K) {
                         float su = 0.0f;
-                        if (excl) {
-                            const float *urow = s_u + (Z * K + Xp) * K;
+                        if (exq) {
+                            const float *urow = s_u + (Z * K + Xq) * K;
 #pragma unroll
                             for (int Y = 0; Y < K; Y++) su = fmaf(ayr[Y], urow[Y], su);
                         }
@@ -478,10 +485,10 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kerne
 #pragma unroll
                     for (int Z = 0; Z < N2; Z++) {
                         float v = t2[Z];
-                        if (Zp < K && Z < K) v = excl ? t2x[Z < K ? Z : 0] : v;
+                        if (Zp < K && Z < K) v = exq ? t2x[Z < K ? Z : 0] : v;
                         sacc = fmaf(azr[Z], v, sacc);
                     }
-                    float &a_ = s_acc[(Zp * N2 + Yp) * N2 + Xp];
+                    float &a_ = s_acc[(Zp * N2 + Xq) * N2 + Yq];
                     a_ = fmaf(cf, sacc, a_);
                 }
             }
@@ -491,9 +498,9 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kerne
             double *out = L.out[w];
 #pragma unroll
             for (int Zp = 0; Zp < N2; Zp++) {
-                int c = (Xp >= K ? 1 : 0) | (Yp >= K ? 2 : 0) | (Zp >= K ? 4 : 0);
-                int gi = c * K3 + (Zp % K) * K * K + (Yp % K) * K + (Xp % K);
-                double v = double(s_acc[(Zp * N2 + Yp) * N2 + Xp]);
+                int c = (Xq >= K ? 1 : 0) | (Yq >= K ? 2 : 0) | (Zp >= K ? 4 : 0);
+                int gi = c * K3 + (Zp % K) * K * K + (Yq % K) * K + (Xq % K);
+                double v = double(s_acc[(Zp * N2 + Xq) * N2 + Yq]);
                 if (L.set)
                     out[gi] = v;
                 else
