@@ -237,19 +237,55 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     const int nn = (int)li.nodes;
     const size_t ni = (size_t)li.items;
     if (nn == 0) return nullptr;
-    // nodes in decreasing item count (longest first) for the persistent grid's dynamic
-    // scheduler; each node's own items keep their order, so results do not change
-    std::vector<int> ord(nn);
-    for (int i = 0; i < nn; i++) ord[i] = i;
-    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
-        return li.begin[a + 1] - li.begin[a] > li.begin[b + 1] - li.begin[b];
-    });
-    std::vector<double *> outp(nn);
-    std::vector<long long> beg(nn), end(nn);
+    // A node with many items runs as several chunks of about CHUNK items, each a CTA task that
+    // writes a partial block; a second kernel sums every such node's partials in chunk order.
+    // The split depends only on the tier and the node's own item count, so results do not depend
+    // on which nodes share the launch.  CHUNK is about half a millisecond of one CTA's work:
+    // an item costs ~200 us (FP64), ~20 us (FP32), ~6 us (TF32) and ~70 us (double-FP32).
+    static constexpr long long CHUNKS[4] = {4, 32, 96, 8};
+    const long long CHUNK = CHUNKS[tier];
+    const int bs = ctx.basis.bs;
+    std::vector<double *> vout;
+    std::vector<long long> vbeg, vend;
+    std::vector<ReduceTask> red;
+    long nsplit = 0;
     for (int i = 0; i < nn; i++) {
-        outp[i] = li.out[ord[i]];
-        beg[i] = li.begin[ord[i]];
-        end[i] = li.begin[ord[i] + 1];
+        const long long m = li.begin[i + 1] - li.begin[i];
+        if (m > CHUNK + CHUNK / 2) nsplit += (m + CHUNK / 2) / CHUNK;
+    }
+    double *scratch = nsplit ? (double *)arena.alloc(sizeof(double) * (size_t)bs * nsplit) : nullptr;
+    if (scratch && !set) MWG_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double) * (size_t)bs * nsplit, ctx.stream));
+    long used = 0;
+    for (int i = 0; i < nn; i++) {
+        const long long b0 = li.begin[i], m = li.begin[i + 1] - b0;
+        const long long pieces = m > CHUNK + CHUNK / 2 ? (m + CHUNK / 2) / CHUNK : 1;
+        if (pieces == 1) {
+            vout.push_back(li.out[i]);
+            vbeg.push_back(b0);
+            vend.push_back(b0 + m);
+            continue;
+        }
+        red.push_back(ReduceTask{li.out[i], scratch + (size_t)used * bs, (int)pieces, set ? 1 : 0});
+        for (long long k = 0; k < pieces; k++) {
+            vout.push_back(scratch + (size_t)(used + k) * bs);
+            vbeg.push_back(b0 + m * k / pieces);
+            vend.push_back(b0 + m * (k + 1) / pieces);
+        }
+        used += (long)pieces;
+    }
+    // tasks in decreasing item count (longest first) for the persistent grid's dynamic
+    // scheduler; each task's own items keep their order, so results do not change
+    const int nv = (int)vout.size();
+    std::vector<int> ord(nv);
+    for (int i = 0; i < nv; i++) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(),
+                     [&](int a, int b) { return vend[a] - vbeg[a] > vend[b] - vbeg[b]; });
+    std::vector<double *> outp(nv);
+    std::vector<long long> beg(nv), end(nv);
+    for (int i = 0; i < nv; i++) {
+        outp[i] = vout[ord[i]];
+        beg[i] = vbeg[ord[i]];
+        end[i] = vend[ord[i]];
     }
     Packer pk;
     pk.add(outp.data(), outp.size() * sizeof(double *));
@@ -260,10 +296,11 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     pk.add(li.ay.data(), ni * sizeof(void *));
     pk.add(li.az.data(), ni * sizeof(void *));
     pk.add(li.coef.data(), ni * sizeof(double));
+    pk.add(red.data(), red.size() * sizeof(ReduceTask));
     pk.ship(ctx, arena);
     int *counter = (int *)arena.alloc(2 * sizeof(int));
     ApplyLaunch L;
-    L.nnodes = nn;
+    L.nnodes = nv;
     L.root = root ? 1 : 0;
     L.set = set ? 1 : 0;
     L.out = (double *const *)pk.ptr(0);
@@ -277,18 +314,21 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     L.counter = counter;
     L.status = counter + 1;
     st.launches++;
+    int *hs = nullptr;
     if (tier == 3) {
         k_apply_df(ctx.dbasis, L, ctx.nsm, ctx.stream);
-        return nullptr;
-    }
-    if (tier != 2) {
+    } else if (tier != 2) {
         k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
-        return nullptr;
+    } else {
+        k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
+        hs = (int *)arena.halloc(sizeof(int));
+        *hs = 0;
+        MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
     }
-    k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
-    int *hs = (int *)arena.halloc(sizeof(int));
-    *hs = 0;
-    MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+    if (!red.empty()) {
+        k_reduce_partials((const ReduceTask *)pk.ptr(8), (int)red.size(), bs, ctx.stream);
+        st.launches++;
+    }
     return hs;
 }
 

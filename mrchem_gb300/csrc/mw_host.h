@@ -265,6 +265,14 @@ void k_to_fp32_cube(const double *in, float *out, size_t nblocks, int K, cudaStr
 void k_dot(const double *const *a, const double *const *b, const int *start, int n, int bs, double *partial,
            cudaStream_t s);
 void k_scale(double *x, size_t n, double c, cudaStream_t s);
+// a node whose items ran as several chunks: out (=|+=) the sum of its chunks' partial blocks, in order
+struct ReduceTask {
+    double *out;
+    const double *part;  // count consecutive partial blocks
+    int count;
+    int set;
+};
+void k_reduce_partials(const ReduceTask *tasks, int n, int bs, cudaStream_t s);
 double probe_fma_tflops(int fp64, int nsm, cudaStream_t s);
 double probe_mma_tflops(int kind, int nsm, cudaStream_t s);
 void k_eval(const DevBasis &b, const double *const *blocks, const int *keys, const double *pts, int npts,

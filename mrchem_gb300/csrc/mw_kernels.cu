@@ -785,6 +785,23 @@ void k_to_fp32_cube(const double *in, float *out, size_t nblocks, int K, cudaStr
     MWG_CUDA(cudaGetLastError());
 }
 
+__global__ void reduce_partials_kernel(const ReduceTask *tasks, int n, int bs) {
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        const ReduceTask T = tasks[t];
+        for (int i = threadIdx.x; i < bs; i += blockDim.x) {
+            double v = T.set ? 0.0 : T.out[i];
+            for (int c = 0; c < T.count; c++) v += T.part[(size_t)c * bs + i];
+            T.out[i] = v;
+        }
+    }
+}
+
+void k_reduce_partials(const ReduceTask *tasks, int n, int bs, cudaStream_t s) {
+    if (n <= 0) return;
+    reduce_partials_kernel<<<std::min(n, 4096), 256, 0, s>>>(tasks, n, bs);
+    MWG_CUDA(cudaGetLastError());
+}
+
 void k_scale(double *x, size_t n, double c, cudaStream_t s) {
     if (n == 0) return;
     scale_kernel<<<4096, 256, 0, s>>>(x, n, c);
