@@ -80,13 +80,16 @@ typedef struct {
     double kernel_ms_fp64;   /* CUDA-event time of the FP64 contraction launches */
     double kernel_ms_fp32;   /* ... of the FP32 contraction launches */
     double host_enum_ms;     /* host: candidate enumeration (screening bounds, lookups) */
-    double host_items_ms;    /* host: generation requests, exact screening, tiers, item lists */
+    double host_items_ms;    /* host: exact screening, tiers, item lists */
     double host_wait_ms;     /* host: waiting for the level's kernels and norm downloads */
     double flops_tf32;       /* algorithmic flops of the TF32 tier */
     double kernel_ms_tf32;   /* CUDA-event time of the TF32 contraction launches */
     long long items_df;      /* contractions in double-FP32 (pairs of FP32 numbers) */
     double flops_df;         /* algorithmic flops of the double-FP32 tier */
     double kernel_ms_df;     /* CUDA-event time of the double-FP32 contraction launches */
+    double host_gen_ms;      /* host: generation requests and the generation of missing input nodes */
+    double host_launch_ms;   /* host: ordering, chunking and packing the item lists, launches */
+    double host_refine_ms;   /* host: refinement decisions after each level */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */

@@ -533,6 +533,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 s.gbase32 = (first32 && s.gbase) ? first32 + 2 * (s.gbase - first) : nullptr;
             }
         }
+        auto tC = std::chrono::steady_clock::now();
+        st.host_gen_ms += std::chrono::duration<double, std::milli>(tC - tB).count();
         // phase C: exact screening and tier per candidate (parallel), then the
         // per-tier item lists in node order (prefix sums + parallel fill)
         std::vector<std::pair<int, int>> nodes_flat;  // (job, work index) in launch order
@@ -652,7 +654,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         st.flops_fp32 += 6.0 * K4 * (double)pairs_t1;
         st.flops_tf32 += 6.0 * K4 * (double)pairs_t2;
         st.flops_df += 6.0 * K4 * (double)pairs_t3;
-        st.host_items_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tB).count();
+        auto tD = std::chrono::steady_clock::now();
+        st.host_items_ms += std::chrono::duration<double, std::milli>(tD - tC).count();
         MWG_CUDA(cudaEventRecord(G.ev[0], ctx.stream));
         G.tc_status = nullptr;
         for (int k = 0; k < NTIER; k++) {
@@ -682,6 +685,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             MWG_CUDA(cudaMemcpyAsync(G.h_cn[j], out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
                                      ctx.stream));
         }
+        st.host_launch_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tD).count();
         return true;
     };
 
@@ -692,7 +696,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         const bool root = (G.level == 0);
         auto tW = std::chrono::steady_clock::now();
         ctx.sync();
-        st.host_wait_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tW).count();
+        auto tR = std::chrono::steady_clock::now();
+        st.host_wait_ms += std::chrono::duration<double, std::milli>(tR - tW).count();
         check_status(G.tc_status);
         float ms_t[NTIER];
         for (int k = 0; k < NTIER; k++) MWG_CUDA(cudaEventElapsedTime(&ms_t[k], G.ev[k], G.ev[k + 1]));
@@ -730,6 +735,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         st.levels++;
         G.arena->reset();
         G.level++;
+        st.host_refine_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tR).count();
     };
 
     while (true) {
