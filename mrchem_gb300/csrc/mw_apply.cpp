@@ -428,12 +428,20 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     }
     groups[0].stream = ctx.stream;
     groups[0].arena = &arena;
+    if (!ctx.fast) {
+        int least = 0, greatest = 0;
+        MWG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        MWG_CUDA(cudaStreamCreateWithPriority(&ctx.fast, cudaStreamNonBlocking, greatest));
+        MWG_CUDA(cudaEventCreateWithFlags(&ctx.fast_done, cudaEventDisableTiming));
+    }
     cudaEvent_t ev_start = nullptr;
     std::vector<cudaEvent_t> ev_end(ngroups, nullptr);
+    // the generation stream and groups 1.. start after everything queued on the context's stream
+    // so far (input uploads, FP32 shadows, zeroed roots)
+    MWG_CUDA(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
+    MWG_CUDA(cudaEventRecord(ev_start, ctx.stream));
+    MWG_CUDA(cudaStreamWaitEvent(ctx.fast, ev_start, 0));
     if (ngroups > 1) {
-        // groups 1.. start after the set-up queued on the context's stream (FP32 shadows, zeroed roots)
-        MWG_CUDA(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
-        MWG_CUDA(cudaEventRecord(ev_start, ctx.stream));
         for (int g = 1; g < ngroups; g++) {
             cudaStream_t &xs = ctx.xstream[g - 1];
             if (!xs) MWG_CUDA(cudaStreamCreateWithFlags(&xs, cudaStreamNonBlocking));
@@ -516,7 +524,15 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 sets.push_back({&sp->gens, sp->job->inp});
                 total += sp->gens.keys.size();
             }
-            generate_all(sets, ar, &st);
+            {
+                // generation on the high-priority stream: its kernel and norm download are what
+                // the host waits for before the exact screening; the group's stream then waits
+                // for the generated blocks with an event
+                StreamSwap fast(ctx, ctx.fast);
+                generate_all(sets, ar, &st);
+                MWG_CUDA(cudaEventRecord(ctx.fast_done, ctx.fast));
+            }
+            MWG_CUDA(cudaStreamWaitEvent(ctx.stream, ctx.fast_done, 0));
             double *first = nullptr;
             for (JobState *sp : jp)
                 if (sp->gens.base && !first) first = sp->gens.base;

@@ -485,8 +485,10 @@ void launch_tc(const ApplyLaunch &L, int nsm, cudaStream_t s) {
     int per_sm = 0;
     MWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, apply_tc_kernel<K>, threads, smem));
     if (per_sm < 1) per_sm = 1;
-    int grid = nsm * per_sm;
-    if (grid > L.nnodes) grid = L.nnodes;
+    // one CTA per task (tasks are ordered longest first and taken in that order): CTAs end
+    // throughout the launch, so kernels of other streams get SM slots without waiting for it
+    (void)nsm;
+    const int grid = L.nnodes;
     if (grid < 1) return;
     apply_tc_kernel<K><<<grid, threads, smem, s>>>(L);
     MWG_CUDA(cudaGetLastError());

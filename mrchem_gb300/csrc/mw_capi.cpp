@@ -112,6 +112,7 @@ static void ctx_free(mw_ctx c) {
     cudaStreamSynchronize(c->ctx.stream);
     for (auto &xs : c->ctx.xstream)
         if (xs) cudaStreamSynchronize(xs);
+    if (c->ctx.fast) cudaStreamSynchronize(c->ctx.fast);
     c->ctx.arena.release();
     for (auto &xa : c->ctx.xarena) xa.release();
     if (c->ctx.h_pinned) cudaFreeHost(c->ctx.h_pinned);
@@ -119,6 +120,8 @@ static void ctx_free(mw_ctx c) {
     cudaStreamDestroy(c->ctx.stream);
     for (auto &xs : c->ctx.xstream)
         if (xs) cudaStreamDestroy(xs);
+    if (c->ctx.fast) cudaStreamDestroy(c->ctx.fast);
+    if (c->ctx.fast_done) cudaEventDestroy(c->ctx.fast_done);
     delete c;
 }
 

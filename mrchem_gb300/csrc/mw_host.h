@@ -168,6 +168,11 @@ struct Ctx {
     cudaStream_t xstream[XGROUPS] = {};
     Arena xarena[XGROUPS];
     int groups = XGROUPS + 1;  // job groups of a batched apply (1: no overlap)
+    // high-priority stream for the generation of missing input nodes, which the host waits for
+    // in the middle of preparing a level; the contraction kernels run one CTA per task, so the
+    // generation gets the next free slot instead of waiting for whole kernels of other groups
+    cudaStream_t fast = nullptr;
+    cudaEvent_t fast_done = nullptr;
     void *h_pinned = nullptr;
     size_t pinned_bytes = 0;
     void *pinned(size_t bytes);
