@@ -120,6 +120,29 @@ struct Cand {
 struct JobState {
     ApplyJob *job = nullptr;
     double R = 1.0, fmax = 0.0;
+    // per level (scale - root scale): the largest block norm an input candidate at that scale can
+    // have, i.e. of the input nodes at that scale and of the coarser leaves (generated inputs)
+    std::vector<double> fmax_lv;
+    double fmax_at(int lv) const { return lv < (int)fmax_lv.size() ? fmax_lv[lv] : fmax; }
+    void set_fmax(const Tree &t, int n0) {
+        fmax = 0.0;
+        int nl = 1;
+        for (const NodeInfo &ni : t.nodes) nl = std::max(nl, ni.n - n0 + 2);
+        std::vector<double> at(nl, 0.0), leaf(nl, 0.0);
+        for (int i = 0; i < t.nn(); i++) {
+            const int lv = t.nodes[i].n - n0;
+            const double v = block_norm8(&t.cn[8 * (size_t)i]);
+            fmax = std::max(fmax, v);
+            at[lv] = std::max(at[lv], v);
+            if (t.nodes[i].child0 < 0) leaf[lv] = std::max(leaf[lv], v);
+        }
+        fmax_lv.assign(nl, 0.0);
+        double coarser_leaf = 0.0;
+        for (int lv = 0; lv < nl; lv++) {
+            fmax_lv[lv] = std::max(at[lv], coarser_leaf);
+            coarser_leaf = std::max(coarser_leaf, leaf[lv]);
+        }
+    }
     std::vector<int> work;
     std::vector<double> wgt;
     int iter = 0;
@@ -132,13 +155,27 @@ struct JobState {
 
 struct LookupCache {
     int L = -1, side = 0;
+    unsigned stamp = 0;          // entries whose stamp differs are unknown (reset in O(1))
+    std::vector<unsigned> st;
     std::vector<int> idx;      // -3 unknown, -2 outside, >= 0 node, <= -4 generated with ancestor -(v+4)
     std::vector<double> anorm;
     void reset(int Lm) {
-        L = Lm;
-        side = 2 * Lm + 1;
-        idx.assign((size_t)side * side * side, -3);
-        anorm.assign((size_t)side * side * side, 0.0);
+        if (Lm != L || ++stamp == 0) {
+            L = Lm;
+            side = 2 * Lm + 1;
+            const size_t n = (size_t)side * side * side;
+            st.assign(n, 0u);
+            idx.assign(n, -3);
+            anorm.assign(n, 0.0);
+            stamp = 1;
+        }
+    }
+    int &entry(size_t ci) {
+        if (st[ci] != stamp) {
+            st[ci] = stamp;
+            idx[ci] = -3;
+        }
+        return idx[ci];
     }
 };
 
@@ -150,7 +187,7 @@ void enumerate_node(JobState &js, int w, int s, bool root, double thr, LookupCac
     const NodeInfo &o = js.job->out->nodes[js.work[w]];
     std::vector<Cand> &out = js.cand[w];
     out.clear();
-    const double fm = BOUND_PRUNE * js.fmax;
+    const double fm = BOUND_PRUNE * js.fmax_at(s);
     int Lm = 0;
     for (int t = 0; t < op.T; t++) Lm = std::max(Lm, op.band[t * op.S + s]);
     cache.reset(Lm);
@@ -171,7 +208,7 @@ void enumerate_node(JobState &js, int w, int s, bool root, double thr, LookupCac
                 if (!root && fm * (xz * ay * A + az * xy * A + az * ay * X) < thr) continue;
                 for (int lx = -L; lx <= L; lx++) {
                     size_t ci = ((size_t)(lz + Lm) * cache.side + (ly + Lm)) * cache.side + (lx + Lm);
-                    int &ce = cache.idx[ci];
+                    int &ce = cache.entry(ci);
                     if (ce == -3) {
                         int p[3] = {o.l[0] - lx, o.l[1] - ly, o.l[2] - lz};
                         if (!b.in_world(o.n, p)) {
@@ -363,7 +400,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         s.job = &job;
         if (job.inp->ctx != &ctx || job.out->ctx != &ctx || job.op->ctx != &ctx)
             throw Error(MW_ERR_ARG, "apply: trees and operator must belong to one context");
-        for (int i = 0; i < job.inp->nn(); i++) s.fmax = std::max(s.fmax, block_norm8(&job.inp->cn[8 * (size_t)i]));
+        s.set_fmax(*job.inp, b.n0);
         if (!fixed_grid) {
             if (job.out->nn() != job.out->nroots) throw Error(MW_ERR_STATE, "apply: output tree must be empty");
             tree_zero(*job.out, 0, job.out->nn());
