@@ -316,6 +316,7 @@ def run(args):
         "kernel_ms_per_step": st_ser["kernel_ms"], "host_ms_per_step": st["host_ms"],
         "host_breakdown_ms": {"enumerate": st["host_enum_ms"], "generate": st["host_gen_ms"], "items": st["host_items_ms"],
                               "launch": st["host_launch_ms"], "refine": st["host_refine_ms"],
+                              "gpu_levels_span": st["gpu_levels_ms"], "gpu_post": st["gpu_post_ms"],
                               "wait_level": st["host_wait_ms"], "kernel_fp64": st_ser["kernel_ms_fp64"],
                               "kernel_fp32": st_ser["kernel_ms_fp32"], "kernel_tf32": st_ser["kernel_ms_tf32"],
                               "kernel_df32": st_ser["kernel_ms_df"],

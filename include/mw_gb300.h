@@ -90,6 +90,8 @@ typedef struct {
     double host_gen_ms;      /* host: generation requests and the generation of missing input nodes */
     double host_launch_ms;   /* host: ordering, chunking and packing the item lists, launches */
     double host_refine_ms;   /* host: refinement decisions after each level */
+    double gpu_levels_ms;    /* GPU time from the call's first queued work to the end of its last level */
+    double gpu_post_ms;      /* GPU time of the post-processing (sum over scales, compression, norms) */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */

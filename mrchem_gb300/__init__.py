@@ -58,7 +58,7 @@ class Stats(C.Structure):
                 ("host_items_ms", C.c_double), ("host_wait_ms", C.c_double), ("flops_tf32", C.c_double),
                 ("kernel_ms_tf32", C.c_double), ("items_df", C.c_longlong), ("flops_df", C.c_double),
                 ("kernel_ms_df", C.c_double), ("host_gen_ms", C.c_double), ("host_launch_ms", C.c_double),
-                ("host_refine_ms", C.c_double)]
+                ("host_refine_ms", C.c_double), ("gpu_levels_ms", C.c_double), ("gpu_post_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

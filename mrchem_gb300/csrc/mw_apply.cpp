@@ -354,13 +354,16 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     int *hs = nullptr;
     if (tier == 3) {
         k_apply_df(ctx.dbasis, L, ctx.nsm, ctx.stream);
-    } else if (tier != 2) {
-        k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
     } else {
-        k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
-        hs = (int *)arena.halloc(sizeof(int));
-        *hs = 0;
-        MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+        if (tier == 2)
+            k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
+        else
+            k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
+        if (tier == 2) {  // the TF32 kernel waits for bulk copies with a bound
+            hs = (int *)arena.halloc(sizeof(int));
+            *hs = 0;
+            MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+        }
     }
     if (!red.empty()) {
         k_reduce_partials((const ReduceTask *)pk.ptr(8), (int)red.size(), bs, ctx.stream);
@@ -371,7 +374,7 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
 
 void check_status(const int *hs) {
     if (hs && *hs != 0)
-        throw Error(MW_ERR_TIMEOUT, "apply: a bounded wait for an asynchronous copy ran out (tensor-core tier)");
+        throw Error(MW_ERR_TIMEOUT, "apply: a bounded wait for an asynchronous copy ran out");
 }
 
 }  // namespace
@@ -391,6 +394,10 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     Arena &arena = ctx.arena;
     arena.reset();
     float kernel_ms = 0.0f;
+    // GPU spans: set-up + levels, and the post-processing after them
+    cudaEvent_t ev_span[3];
+    for (auto &e : ev_span) MWG_CUDA(cudaEventCreate(&e));
+    MWG_CUDA(cudaEventRecord(ev_span[0], ctx.stream));
 
     std::vector<JobState> js(jobs.size());
     int max_levels = 0;
@@ -438,7 +445,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         bool pending = false, done = false;
         LevelItems lt[NTIER];
         cudaEvent_t ev[NTIER + 1];
-        int *tc_status = nullptr;
+        std::vector<int *> status;  // pinned copies of the launches' status words
         std::vector<double *> h_cn;  // pinned staging of each job's component norms
     };
     // runs the host side with the context's stream pointing at the group's stream
@@ -710,10 +717,10 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         auto tD = std::chrono::steady_clock::now();
         st.host_items_ms += std::chrono::duration<double, std::milli>(tD - tC).count();
         MWG_CUDA(cudaEventRecord(G.ev[0], ctx.stream));
-        G.tc_status = nullptr;
+        G.status.clear();
         for (int k = 0; k < NTIER; k++) {
             int *hs = launch_tier(ctx, ar, lt[k], root, k == 0, k, st);
-            if (hs) G.tc_status = hs;
+            if (hs) G.status.push_back(hs);
             MWG_CUDA(cudaEventRecord(G.ev[k + 1], ctx.stream));
         }
         // norms of the level's output nodes, downloaded into pinned staging
@@ -751,7 +758,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         ctx.sync();
         auto tR = std::chrono::steady_clock::now();
         st.host_wait_ms += std::chrono::duration<double, std::milli>(tR - tW).count();
-        check_status(G.tc_status);
+        for (const int *hs : G.status) check_status(hs);
         float ms_t[NTIER];
         for (int k = 0; k < NTIER; k++) MWG_CUDA(cudaEventElapsedTime(&ms_t[k], G.ev[k], G.ev[k + 1]));
         kernel_ms += ms_t[0] + ms_t[1] + ms_t[2] + ms_t[3];
@@ -819,6 +826,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     // input bytes: every distinct input block read once per apply (FP64 or FP32 shadow) + operator blocks
     for (auto &s : js) st.bytes += 8.0 * bs * (double)s.job->inp->nn();
 
+    MWG_CUDA(cudaEventRecord(ev_span[1], ctx.stream));
     // post-processing: top-down sum over scales, then bottom-up compression
     int maxn = b.n0;
     for (auto &s : js) maxn = std::max(maxn, s.job->out->max_scale());
@@ -879,8 +887,17 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
                                  ctx.stream));
     }
+    MWG_CUDA(cudaEventRecord(ev_span[2], ctx.stream));
     ctx.sync();
     arena.reset();
+    {
+        float a = 0.0f, c = 0.0f;
+        MWG_CUDA(cudaEventElapsedTime(&a, ev_span[0], ev_span[1]));
+        MWG_CUDA(cudaEventElapsedTime(&c, ev_span[1], ev_span[2]));
+        st.gpu_levels_ms += a;
+        st.gpu_post_ms += c;
+    }
+    for (auto &e : ev_span) cudaEventDestroy(e);
     st.kernel_ms += kernel_ms;
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }

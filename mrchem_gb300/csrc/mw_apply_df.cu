@@ -59,8 +59,9 @@ template <int K>
 struct DfGeo {
     static constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K;
     static constexpr int THREADS = ((NC + 31) / 32) * 32;
-    // float2 units: IN, T1, ACC (C each), U (K^3); then floats: A hi (3 NC), A lo (3 NC)
-    static constexpr size_t SMEM = sizeof(float2) * (3 * (size_t)C + K3) + sizeof(float) * 6 * (size_t)NC;
+    // float2 units: IN (later T2), T1, ACC (C each), U and T2X (K^3 each); then floats: A hi (3 NC),
+    // A lo (3 NC)
+    static constexpr size_t SMEM = sizeof(float2) * (3 * (size_t)C + 2 * K3) + sizeof(float) * 6 * (size_t)NC;
 };
 
 template <int K>
@@ -72,7 +73,9 @@ __global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLau
     float2 *s_t1 = s_in + C;       // T1[Z][Y][X']
     float2 *s_acc = s_t1 + C;      // node accumulator acc[Z'][Y'][X']
     float2 *s_u = s_acc + C;       // u[Z][Y][X'], Z, Y, X' < K
-    float *s_Ah = reinterpret_cast<float *>(s_u + K3);  // A_x, A_y, A_z high parts
+    float2 *s_t2 = s_in;           // T2[Z][Y'][X'] (the input is dead after the x pass)
+    float2 *s_t2x = s_u + K3;      // t2x[Z][Y'][X'], Z, Y', X' < K
+    float *s_Ah = reinterpret_cast<float *>(s_t2x + K3);  // A_x, A_y, A_z high parts
     float *s_Al = s_Ah + 3 * NC;                        // low parts
     __shared__ int s_node;
     const int tid = threadIdx.x;
@@ -147,8 +150,9 @@ __global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLau
                     ayh[Y] = s_Ah[NC + Yp * N2 + Y];
                     ayl[Y] = s_Al[NC + Yp * N2 + Y];
                 }
-                float2 t2[N2], t2x[K];
-#pragma unroll
+                // rolled over Z (a fully unrolled pass overflows the instruction cache): each
+                // thread parks its own T2 column in shared memory and reads it back for the z pass
+#pragma unroll 2
                 for (int Z = 0; Z < N2; Z++) {
                     float s0h = 0.0f, s0l = 0.0f, s1h = 0.0f, s1l = 0.0f;
 #pragma unroll
@@ -172,11 +176,16 @@ __global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLau
                             }
                         }
                         df_add(xh, xl, s1h, s1l);
-                        t2x[Z < K ? Z : 0] = df_norm(xh, xl);
+                        if (excl) s_t2x[(Z * K + Yp) * K + Xp] = df_norm(xh, xl);
                     }
                     df_add(s0h, s0l, s1h, s1l);
-                    t2[Z] = df_norm(s0h, s0l);
+                    s_t2[(Z * N2 + Yp) * N2 + Xp] = df_norm(s0h, s0l);
                 }
+                float2 t2[N2], t2x[K];
+#pragma unroll
+                for (int Z = 0; Z < N2; Z++) t2[Z] = s_t2[(Z * N2 + Yp) * N2 + Xp];
+#pragma unroll
+                for (int Z = 0; Z < K; Z++) t2x[Z] = excl ? s_t2x[(Z * K + Yp) * K + Xp] : make_float2(0.0f, 0.0f);
 #pragma unroll 2
                 for (int Zp = 0; Zp < N2; Zp++) {
                     const float *azh = s_Ah + 2 * NC + Zp * N2, *azl = s_Al + 2 * NC + Zp * N2;

@@ -229,7 +229,7 @@ struct ApplyLaunch {
     const void *const *az;
     const double *coef;           // per item
     int *counter;                 // dynamic node counter (persistent grid)
-    int *status;                  // 0, or 1 when a bounded wait of the launch ran out (tensor-core tier)
+    int *status;                  // 0, or 1 when a bounded wait of the launch ran out (TF32 tier)
 };
 
 struct PairTask {  // parent -> children (8 consecutive blocks)
@@ -251,7 +251,11 @@ struct AddTask {
 };
 
 void k_project(const DevBasis &b, const ProjFunc &f, const ProjTask *tasks, int n, cudaStream_t s);
-void k_generate(const DevBasis &b, const GenTask *tasks, int n, cudaStream_t s);
+// scratch: grid x generate_scratch_doubles(K) doubles (one slice per CTA)
+void k_generate(const DevBasis &b, const GenTask *tasks, int n, double *scratch, int grid, cudaStream_t s);
+inline size_t generate_scratch_doubles(int K) {
+    return (size_t)4 * K * K * K + (size_t)2 * K * K * K + (size_t)K * K * K;
+}
 void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s);
 // TF32 tensor-core tier: FP32 cube-order input blocks and FP32 operator blocks, as the FP32 tier
 void k_apply_tc(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s);

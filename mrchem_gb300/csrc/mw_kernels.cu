@@ -202,47 +202,91 @@ __global__ void project_kernel(DevBasis b, ProjFunc f, const ProjTask *tasks, in
 }
 
 // ----------------------------------------------------------------- generated nodes
-__global__ void generate_kernel(DevBasis b, const GenTask *tasks, int n) {
-    extern __shared__ double sm[];
-    int K = b.K, N2 = 2 * K, C = N2 * N2 * N2, K3 = K * K * K;
-    double *cube = sm, *tmp = sm + C, *red = sm + 2 * C;
+// Missing input nodes: a leaf's block reconstructed down a path of child steps
+// to the requested node.  Each step keeps only the child's scaling part, so
+// after the first step the block's wavelet parts are zero and the three passes
+// contract over K instead of 2K.  The intermediates live in per-CTA scratch in
+// global memory (L2-resident), so that the kernel needs no shared memory and
+// fits on SMs beside the contraction CTAs: the host waits for it while
+// preparing a level.  Every task writes the full block (wavelet parts zero)
+// and its 8 component norms.
+__global__ void __launch_bounds__(128) generate_kernel(DevBasis b, const GenTask *tasks, int n, double *scratch) {
+    __shared__ double s_red[4];
+    const int K = b.K, N2 = 2 * K, K3 = K * K * K, KK = K * K;
+    const size_t per = (size_t)N2 * N2 * K + (size_t)N2 * K * K + K3;
+    double *t1 = scratch + (size_t)blockIdx.x * per, *t2 = t1 + (size_t)N2 * N2 * K, *sc = t2 + (size_t)N2 * K * K;
     for (int t = blockIdx.x; t < n; t += gridDim.x) {
-        GenTask task = tasks[t];
-        load_block(cube, task.anc, K);
+        const GenTask task = tasks[t];
         for (int s = 0; s < task.steps; s++) {
-            int c = (int)((task.path >> (3 * s)) & 7);
-            int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
-            // child c's scaling part: rows b*K.. of W^T in each dimension
-            for (int i = threadIdx.x; i < N2 * N2 * K; i += blockDim.x) {
-                int x = i % K, YZ = i / K;
-                double acc = 0.0;
-                for (int k = 0; k < N2; k++) acc += b.WT[(bx * K + x) * N2 + k] * cube[YZ * N2 + k];
-                tmp[YZ * K + x] = acc;  // tmp[Z][Y][x]
-            }
-            __syncthreads();
-            for (int i = threadIdx.x; i < N2 * K * K; i += blockDim.x) {
-                int x = i % K, y = (i / K) % K, Z = i / (K * K);
-                double acc = 0.0;
-                for (int k = 0; k < N2; k++) acc += b.WT[(by * K + y) * N2 + k] * tmp[(Z * N2 + k) * K + x];
-                cube[i] = acc;  // cube[Z][y][x] (compact)
-            }
-            __syncthreads();
-            for (int i = threadIdx.x; i < K3; i += blockDim.x) {
-                int xy = i % (K * K), z = i / (K * K);
-                double acc = 0.0;
-                for (int k = 0; k < N2; k++) acc += b.WT[(bz * K + z) * N2 + k] * cube[k * K * K + xy];
-                tmp[i] = acc;  // s[z][y][x]
-            }
-            __syncthreads();
-            for (int i = threadIdx.x; i < C; i += blockDim.x) {
-                int X = i % N2, Y = (i / N2) % N2, Z = i / (N2 * N2);
-                cube[i] = (X < K && Y < K && Z < K) ? tmp[(Z * K + Y) * K + X] : 0.0;
+            const int c = (int)((task.path >> (3 * s)) & 7);
+            const int bx = c & 1, by = (c >> 1) & 1, bz = (c >> 2) & 1;
+            if (s == 0) {
+                // from the ancestor's full block (component-major, components cx|cy<<1|cz<<2)
+                for (int i = threadIdx.x; i < N2 * N2 * K; i += blockDim.x) {
+                    const int x = i % K, YZ = i / K, Y = YZ % N2, Z = YZ / N2;
+                    const int cyz = ((Y >= K) ? 2 : 0) | ((Z >= K) ? 4 : 0);
+                    const double *row = task.anc + (Z % K) * KK + (Y % K) * K;
+                    double acc = 0.0;
+                    for (int X = 0; X < N2; X++)
+                        acc += b.WT[(bx * K + x) * N2 + X] * row[(cyz | (X >= K ? 1 : 0)) * K3 + (X % K)];
+                    t1[YZ * K + x] = acc;  // t1[Z][Y][x]
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < N2 * KK; i += blockDim.x) {
+                    const int x = i % K, y = (i / K) % K, Z = i / KK;
+                    double acc = 0.0;
+                    for (int Y = 0; Y < N2; Y++) acc += b.WT[(by * K + y) * N2 + Y] * t1[(Z * N2 + Y) * K + x];
+                    t2[i] = acc;  // t2[Z][y][x]
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                    const int xy = i % KK, z = i / KK;
+                    double acc = 0.0;
+                    for (int Z = 0; Z < N2; Z++) acc += b.WT[(bz * K + z) * N2 + Z] * t2[Z * KK + xy];
+                    sc[i] = acc;  // s[z][y][x]
+                }
+            } else {
+                // from the previous step's scaling part (its wavelet parts are zero)
+                for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                    const int x = i % K, zy = i / K;
+                    double acc = 0.0;
+                    for (int X = 0; X < K; X++) acc += b.WT[(bx * K + x) * N2 + X] * sc[zy * K + X];
+                    t1[i] = acc;  // t1[z][y][x']
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                    const int x = i % K, y = (i / K) % K, z = i / KK;
+                    double acc = 0.0;
+                    for (int Y = 0; Y < K; Y++) acc += b.WT[(by * K + y) * N2 + Y] * t1[(z * K + Y) * K + x];
+                    t2[i] = acc;  // t2[z][y'][x]
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                    const int xy = i % KK, z = i / KK;
+                    double acc = 0.0;
+                    for (int Z = 0; Z < K; Z++) acc += b.WT[(bz * K + z) * N2 + Z] * t2[Z * KK + xy];
+                    sc[i] = acc;  // s[z'][y][x]
+                }
             }
             __syncthreads();
         }
-        store_block(task.out, cube, K);
+        // the block: component 0 = s, components 1..7 = 0; norms likewise
+        double ss = 0.0;
+        for (int i = threadIdx.x; i < 8 * K3; i += blockDim.x) {
+            const double v = i < K3 ? sc[i] : 0.0;
+            task.out[i] = v;
+            ss += v * v;
+        }
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = ss;
         __syncthreads();
-        block_norms(task.out, task.cn, K, red);
+        if (threadIdx.x < 8) {
+            double tot = 0.0;
+            if (threadIdx.x == 0)
+                for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += s_red[w];
+            task.cn[threadIdx.x] = threadIdx.x == 0 ? sqrt(tot) : 0.0;
+        }
+        __syncthreads();
     }
 }
 
@@ -721,11 +765,9 @@ void k_project(const DevBasis &b, const ProjFunc &f, const ProjTask *tasks, int 
     MWG_CUDA(cudaGetLastError());
 }
 
-void k_generate(const DevBasis &b, const GenTask *tasks, int n, cudaStream_t s) {
+void k_generate(const DevBasis &b, const GenTask *tasks, int n, double *scratch, int grid, cudaStream_t s) {
     if (n <= 0) return;
-    size_t smem = 2 * cube_bytes(b.K) + 8 * 256 * sizeof(double);
-    MWG_CUDA(cudaFuncSetAttribute(generate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    generate_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, n);
+    generate_kernel<<<grid, 128, 0, s>>>(b, tasks, n, scratch);
     MWG_CUDA(cudaGetLastError());
 }
 
