@@ -298,12 +298,20 @@ class FunctionTree:
     def crop(self, prec, abs_prec=False):
         _check(_lib.mw_crop(self.ptr, prec, int(abs_prec)), self.mra.ptr)
 
-    def download(self):
-        """(keys[n,4] int32, coefs[n, 8K^3] float64, is_leaf[n] uint8) in canonical order."""
+    def download(self, out=None):
+        """(keys[n,4] int32, coefs[n, 8K^3] float64, is_leaf[n] uint8) in canonical order.
+
+        out: optional (keys, coefs, is_leaf) arrays of exactly these shapes and types to fill
+        instead of new ones (saves allocating and first-touching tens of MB per tree).
+        """
         n = self.nnodes
-        keys = np.zeros((n, 4), dtype=np.int32)
-        coefs = np.zeros((n, 8 * self.mra.K ** 3))
-        leaf = np.zeros(n, dtype=np.uint8)
+        shapes = ((n, 4), (n, 8 * self.mra.K ** 3), (n,))
+        dtypes = (np.int32, np.float64, np.uint8)
+        if out is not None and all(a.shape == s and a.dtype == d and a.flags.c_contiguous
+                                   for a, s, d in zip(out, shapes, dtypes)):
+            keys, coefs, leaf = out
+        else:
+            keys, coefs, leaf = (np.empty(s, dtype=d) for s, d in zip(shapes, dtypes))
         _check(_lib.mw_tree_download(self.ptr, _ip(keys), _dp(coefs), leaf.ctypes.data_as(C.POINTER(C.c_ubyte))),
                self.mra.ptr)
         return keys, coefs, leaf

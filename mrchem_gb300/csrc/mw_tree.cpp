@@ -592,6 +592,8 @@ void tree_upload(Tree &t, int nnodes, const int *keys, const double *coefs, Aren
     if (t.nn() != nnodes) throw Error(MW_ERR_ARG, "upload: keys do not form a complete tree");
     ctx.sync();
     double *h = (double *)ctx.pinned(sizeof(double) * (size_t)bs * nnodes);
+    // gather into tree order with all host threads (the blocks are tens of MB per tree)
+#pragma omp parallel for schedule(static)
     for (int i = 0; i < nnodes; i++) std::memcpy(h + (size_t)i * bs, coefs + (size_t)from[i] * bs, sizeof(double) * bs);
     MWG_CUDA(cudaMemcpyAsync(t.d_coefs, h, sizeof(double) * (size_t)bs * nnodes, cudaMemcpyHostToDevice, ctx.stream));
     arena.reset();
@@ -606,6 +608,7 @@ void tree_download(Tree &t, int *keys, double *coefs, unsigned char *leaf) {
         double *h = (double *)ctx.pinned(sizeof(double) * (size_t)bs * n);
         MWG_CUDA(cudaMemcpyAsync(h, t.d_coefs, sizeof(double) * (size_t)bs * n, cudaMemcpyDeviceToHost, ctx.stream));
         ctx.sync();
+#pragma omp parallel for schedule(static)
         for (int j = 0; j < n; j++) std::memcpy(coefs + (size_t)j * bs, h + (size_t)idx[j] * bs, sizeof(double) * bs);
     }
     for (int j = 0; j < n; j++) {
