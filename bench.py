@@ -252,18 +252,20 @@ def run(args):
     host_outputs = [None] * NORB
 
     def e2e_step():
-        for f, (k, c, _) in zip(e2e_phis, host_inputs):
-            f.upload(k, c)
+        mw.upload_batch(e2e_phis, host_inputs)
         for o in outs:
             o.clear()
         mw.apply_batch([PREC] * NORB, outs, ops, e2e_phis, abs_prec=True, precision="mixed")
-        nbytes = 0
-        for i, o in enumerate(outs):
-            host_outputs[i] = o.download(out=host_outputs[i])
-            nbytes += sum(a.nbytes for a in host_outputs[i])
-        return nbytes
+        host_outputs[:] = mw.download_batch(outs, outs=host_outputs if host_outputs[0] is not None else None)
+        return sum(a.nbytes for r in host_outputs for a in r)
 
     e2e_step()
+    # the host buffers live in pinned memory (mw_pin_host), as a caller that keeps orbitals on the
+    # host between steps would hold them: the copy engines then move them directly
+    for _, c, _ in host_inputs:
+        mw.pin_host(mra, c)
+    for r in host_outputs:
+        mw.pin_host(mra, r[1])
     barrier()
     t0 = time.perf_counter()
     d2h = 0

@@ -22,6 +22,8 @@
 #ifndef MW_GB300_H
 #define MW_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -119,6 +121,19 @@ int mw_tree_nleaves(mw_tree t, int *n);
 int mw_tree_depth(mw_tree t, int *d);
 int mw_tree_upload(mw_tree t, int nnodes, const int *keys, const double *coefs);
 int mw_tree_download(mw_tree t, int *keys, double *coefs, unsigned char *is_leaf);
+/* mw_tree_upload / mw_tree_download for n trees of one context with one synchronisation in all
+ * (the reference moves orbitals one at a time, src/qmfunctions/orbital_utils.cpp:1218-1240).
+ * Arrays of n per-tree pointers; a null keys / coefs / is_leaf entry skips that output. */
+int mw_tree_upload_batch(int n, mw_tree *trees, const int *nnodes, const int *const *keys,
+                         const double *const *coefs);
+int mw_tree_download_batch(int n, mw_tree *trees, int *const *keys, double *const *coefs,
+                           unsigned char *const *is_leaf);
+/* Page-locks (pins) a host buffer for the context's GPU, or releases it.  When every coefficient
+ * buffer of a batched upload or download is pinned, the GPU's copy engines move it directly and
+ * the reordering into tree or canonical order runs on the device; otherwise the library stages
+ * the blocks through its own pinned buffer.  No counterpart in the reference. */
+int mw_pin_host(mw_ctx ctx, void *p, size_t bytes);
+int mw_unpin_host(mw_ctx ctx, void *p);
 int mw_tree_squared_norm(mw_tree t, double *out);
 int mw_tree_integrate(mw_tree t, double *out);
 int mw_tree_rescale(mw_tree t, double c);

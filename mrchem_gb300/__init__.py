@@ -75,6 +75,7 @@ EXPORTS = [
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
     "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
     "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap",
+    "mw_tree_upload_batch", "mw_tree_download_batch", "mw_pin_host", "mw_unpin_host",
 ]
 
 
@@ -103,6 +104,10 @@ def load_library(path=None):
         "mw_tree_depth": [P, ip],
         "mw_tree_upload": [P, I, ip, dp],
         "mw_tree_download": [P, ip, dp, C.POINTER(C.c_ubyte)],
+        "mw_tree_upload_batch": [I, pp, ip, pp, pp],
+        "mw_pin_host": [P, P, C.c_size_t],
+        "mw_unpin_host": [P, P],
+        "mw_tree_download_batch": [I, pp, pp, pp, pp],
         "mw_tree_squared_norm": [P, dp],
         "mw_tree_integrate": [P, dp],
         "mw_tree_rescale": [P, D],
@@ -321,6 +326,49 @@ class FunctionTree:
         coefs = np.ascontiguousarray(coefs, dtype=np.float64)
         _check(_lib.mw_tree_upload(self.ptr, keys.shape[0], _ip(keys), _dp(coefs)), self.mra.ptr)
         return self
+
+
+def pin_host(mra, arr):
+    """Page-locks a NumPy array for the GPU (mw_pin_host); batched transfers then copy it directly."""
+    _check(_lib.mw_pin_host(mra.ptr, arr.ctypes.data, arr.nbytes), mra.ptr)
+    return arr
+
+
+def unpin_host(mra, arr):
+    _check(_lib.mw_unpin_host(mra.ptr, arr.ctypes.data), mra.ptr)
+
+
+def upload_batch(trees, inputs):
+    """tree.upload(keys, coefs) for every (tree, (keys, coefs, ...)) pair with one synchronisation."""
+    n = len(trees)
+    ks = [np.ascontiguousarray(x[0], dtype=np.int32) for x in inputs]
+    cs = [np.ascontiguousarray(x[1], dtype=np.float64) for x in inputs]
+    nn = np.ascontiguousarray([k.shape[0] for k in ks], dtype=np.int32)
+    kp = (C.c_void_p * n)(*[k.ctypes.data for k in ks])
+    cp = (C.c_void_p * n)(*[c.ctypes.data for c in cs])
+    _check(_lib.mw_tree_upload_batch(n, _ptrs(trees), _ip(nn), kp, cp), trees[0].mra.ptr)
+    return trees
+
+
+def download_batch(trees, outs=None):
+    """[tree.download() for tree in trees] with one synchronisation; outs as in download(out=)."""
+    n = len(trees)
+    res = []
+    for i, t in enumerate(trees):
+        m = t.nnodes
+        shapes = ((m, 4), (m, 8 * t.mra.K ** 3), (m,))
+        dtypes = (np.int32, np.float64, np.uint8)
+        o = outs[i] if outs is not None else None
+        if o is not None and all(a.shape == s and a.dtype == d and a.flags.c_contiguous
+                                 for a, s, d in zip(o, shapes, dtypes)):
+            res.append(tuple(o))
+        else:
+            res.append(tuple(np.empty(s, dtype=d) for s, d in zip(shapes, dtypes)))
+    kp = (C.c_void_p * n)(*[r[0].ctypes.data for r in res])
+    cp = (C.c_void_p * n)(*[r[1].ctypes.data for r in res])
+    lp = (C.c_void_p * n)(*[r[2].ctypes.data for r in res])
+    _check(_lib.mw_tree_download_batch(n, _ptrs(trees), kp, cp, lp), trees[0].mra.ptr)
+    return res
 
 
 def _gterms(terms):

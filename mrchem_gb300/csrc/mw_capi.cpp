@@ -225,6 +225,52 @@ int mw_tree_download(mw_tree t, int *keys, double *coefs, unsigned char *is_leaf
     return guard(ctx_of(t), [&] { mwg::tree_download(t->tree, keys, coefs, is_leaf); });
 }
 
+int mw_tree_upload_batch(int n, mw_tree *trees, const int *nnodes, const int *const *keys,
+                         const double *const *coefs) {
+    if (n < 1 || !trees || !nnodes || !keys || !coefs) return MW_ERR_ARG;
+    for (int i = 0; i < n; i++) {
+        if (!trees[i] || nnodes[i] < 1 || !keys[i] || !coefs[i]) return MW_ERR_ARG;
+        if (ctx_of(trees[i]) != ctx_of(trees[0])) return MW_ERR_ARG;
+        for (int k = 0; k < i; k++)
+            if (trees[k] == trees[i]) return MW_ERR_ARG;
+    }
+    mwg::Ctx *ctx = ctx_of(trees[0]);
+    return guard(ctx, [&] {
+        std::vector<mwg::Tree *> ts(n);
+        for (int i = 0; i < n; i++) ts[i] = &trees[i]->tree;
+        mwg::tree_upload_batch(ts, nnodes, keys, coefs, ctx->arena);
+    });
+}
+
+int mw_tree_download_batch(int n, mw_tree *trees, int *const *keys, double *const *coefs,
+                           unsigned char *const *is_leaf) {
+    if (n < 1 || !trees || !keys || !coefs || !is_leaf) return MW_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (!trees[i] || ctx_of(trees[i]) != ctx_of(trees[0])) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(trees[0]);
+    return guard(ctx, [&] {
+        std::vector<mwg::Tree *> ts(n);
+        for (int i = 0; i < n; i++) ts[i] = &trees[i]->tree;
+        mwg::tree_download_batch(ts, keys, coefs, is_leaf);
+    });
+}
+
+int mw_pin_host(mw_ctx c, void *p, size_t bytes) {
+    if (!c || !p || bytes == 0) return MW_ERR_ARG;
+    return guard(&c->ctx, [&] {
+        MWG_CUDA(cudaSetDevice(c->ctx.device));
+        MWG_CUDA(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+    });
+}
+
+int mw_unpin_host(mw_ctx c, void *p) {
+    if (!c || !p) return MW_ERR_ARG;
+    return guard(&c->ctx, [&] {
+        MWG_CUDA(cudaSetDevice(c->ctx.device));
+        MWG_CUDA(cudaHostUnregister(p));
+    });
+}
+
 int mw_tree_squared_norm(mw_tree t, double *out) {
     if (!t || !out) return MW_ERR_ARG;
     *out = t->tree.sqnorm_leaves();

@@ -282,6 +282,10 @@ struct ReduceTask {
     int set;
 };
 void k_reduce_partials(const ReduceTask *tasks, int n, int bs, cudaStream_t s);
+// dst block j = src block map[j]; bs even
+void k_permute_blocks(double *dst, const double *src, const int *map, int n, int bs, cudaStream_t s);
+// true when the GPU's DMA engines can read / write the host buffer directly (pinned memory)
+bool host_is_pinned(const void *p);
 double probe_fma_tflops(int fp64, int nsm, cudaStream_t s);
 double probe_mma_tflops(int kind, int nsm, cudaStream_t s);
 void k_eval(const DevBasis &b, const double *const *blocks, const int *keys, const double *pts, int npts,

@@ -30,6 +30,11 @@ void tree_compress(Tree &t, Arena &arena, mw_stats *st);
 void tree_norms_all(Tree &t, Arena &arena);
 void tree_upload(Tree &t, int nnodes, const int *keys, const double *coefs, Arena &arena);
 void tree_download(Tree &t, int *keys, double *coefs, unsigned char *leaf);
+void tree_upload_batch(const std::vector<Tree *> &trees, const int *nnodes, const int *const *keys,
+                       const double *const *coefs, Arena &arena);
+void tree_norms_batch(const std::vector<Tree *> &trees, const int *nnodes, Arena &arena);
+void tree_download_batch(const std::vector<Tree *> &trees, int *const *keys, double *const *coefs,
+                         unsigned char *const *leaf);
 
 void project_gauss(double prec, Tree &t, int nterms, const mw_gterm *terms, bool abs_prec, Arena &arena);
 void project_hydrogen(double prec, Tree &t, int n, int l, int m, double Z, const double *origin, bool abs_prec,

@@ -846,6 +846,21 @@ void k_reduce_partials(const ReduceTask *tasks, int n, int bs, cudaStream_t s) {
     MWG_CUDA(cudaGetLastError());
 }
 
+// dst block j = src block map[j] (blocks of bs doubles)
+__global__ void permute_blocks_kernel(double *dst, const double *src, const int *map, int n, int bs) {
+    for (int j = blockIdx.x; j < n; j += gridDim.x) {
+        const double2 *s2 = reinterpret_cast<const double2 *>(src + (size_t)map[j] * bs);
+        double2 *d2 = reinterpret_cast<double2 *>(dst + (size_t)j * bs);
+        for (int i = threadIdx.x; i < bs / 2; i += blockDim.x) d2[i] = s2[i];
+    }
+}
+
+void k_permute_blocks(double *dst, const double *src, const int *map, int n, int bs, cudaStream_t s) {
+    if (n <= 0) return;
+    permute_blocks_kernel<<<std::min(n, 4096), 256, 0, s>>>(dst, src, map, n, bs);
+    MWG_CUDA(cudaGetLastError());
+}
+
 void k_scale(double *x, size_t n, double c, cudaStream_t s) {
     if (n == 0) return;
     scale_kernel<<<4096, 256, 0, s>>>(x, n, c);

@@ -573,9 +573,8 @@ void project_hydrogen(double prec, Tree &t, int n, int l, int m, double Z, const
 }
 
 // ------------------------------------------------------------------ transfers
-void tree_upload(Tree &t, int nnodes, const int *keys, const double *coefs, Arena &arena) {
-    Ctx &ctx = *t.ctx;
-    int bs = ctx.basis.bs;
+// the tree structure of a key list; returns, per tree node, its position in the list
+static std::vector<int> upload_structure(Tree &t, int nnodes, const int *keys) {
     std::unordered_map<Key, int, KeyHash> src;
     src.reserve(nnodes * 2);
     for (int i = 0; i < nnodes; i++) src[Key{keys[4 * i], {keys[4 * i + 1], keys[4 * i + 2], keys[4 * i + 3]}}] = i;
@@ -590,6 +589,13 @@ void tree_upload(Tree &t, int nnodes, const int *keys, const double *coefs, Aren
         if (src.count(Key{nd.n + 1, {cl[0], cl[1], cl[2]}})) t.split(i);
     }
     if (t.nn() != nnodes) throw Error(MW_ERR_ARG, "upload: keys do not form a complete tree");
+    return from;
+}
+
+void tree_upload(Tree &t, int nnodes, const int *keys, const double *coefs, Arena &arena) {
+    Ctx &ctx = *t.ctx;
+    int bs = ctx.basis.bs;
+    std::vector<int> from = upload_structure(t, nnodes, keys);
     ctx.sync();
     double *h = (double *)ctx.pinned(sizeof(double) * (size_t)bs * nnodes);
     // gather into tree order with all host threads (the blocks are tens of MB per tree)
@@ -598,6 +604,157 @@ void tree_upload(Tree &t, int nnodes, const int *keys, const double *coefs, Aren
     MWG_CUDA(cudaMemcpyAsync(t.d_coefs, h, sizeof(double) * (size_t)bs * nnodes, cudaMemcpyHostToDevice, ctx.stream));
     arena.reset();
     tree_norms_all(t, arena);
+}
+
+// Several trees of one context in one pass: all structures first, then one gather of every
+// block into pinned staging with all host threads, the copies, one norms launch and one
+// synchronisation (instead of one per tree).
+bool host_is_pinned(const void *p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+void tree_upload_batch(const std::vector<Tree *> &trees, const int *nnodes, const int *const *keys,
+                       const double *const *coefs, Arena &arena) {
+    if (trees.empty()) return;
+    Ctx &ctx = *trees[0]->ctx;
+    const int bs = ctx.basis.bs, n = (int)trees.size();
+    std::vector<std::vector<int>> from(n);
+    std::vector<size_t> first(n + 1, 0);
+    for (int i = 0; i < n; i++) {
+        from[i] = upload_structure(*trees[i], nnodes[i], keys[i]);
+        first[i + 1] = first[i] + (size_t)nnodes[i];
+    }
+    ctx.sync();
+    bool pinned = true;
+    for (int i = 0; i < n && pinned; i++) pinned = host_is_pinned(coefs[i]);
+    if (pinned) {
+        // the caller's blocks go straight to device scratch; the permutation into tree order
+        // runs on the device
+        arena.reset();
+        double *scratch = (double *)arena.alloc(sizeof(double) * (size_t)bs * first[n]);
+        std::vector<int> maps;
+        maps.reserve(first[n]);
+        for (int i = 0; i < n; i++) maps.insert(maps.end(), from[i].begin(), from[i].end());
+        Packer pk;
+        pk.add(maps.data(), maps.size() * sizeof(int));
+        pk.ship(ctx, arena);
+        const int *dmap = (const int *)pk.ptr(0);
+        for (int i = 0; i < n; i++) {
+            MWG_CUDA(cudaMemcpyAsync(scratch + first[i] * bs, coefs[i], sizeof(double) * (size_t)bs * nnodes[i],
+                                     cudaMemcpyHostToDevice, ctx.stream));
+            k_permute_blocks(trees[i]->d_coefs, scratch + first[i] * bs, dmap + first[i], nnodes[i], bs, ctx.stream);
+        }
+        tree_norms_batch(trees, nnodes, arena);
+        return;
+    }
+    double *h = (double *)ctx.pinned(sizeof(double) * (size_t)bs * first[n]);
+    std::vector<std::pair<int, int>> all;  // (tree, node)
+    all.reserve(first[n]);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < nnodes[i]; j++) all.push_back({i, j});
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < (long)all.size(); q++) {
+        const int i = all[q].first, j = all[q].second;
+        std::memcpy(h + (first[i] + j) * bs, coefs[i] + (size_t)from[i][j] * bs, sizeof(double) * bs);
+    }
+    arena.reset();
+    for (int i = 0; i < n; i++)
+        MWG_CUDA(cudaMemcpyAsync(trees[i]->d_coefs, h + first[i] * bs, sizeof(double) * (size_t)bs * nnodes[i],
+                                 cudaMemcpyHostToDevice, ctx.stream));
+    tree_norms_batch(trees, nnodes, arena);
+}
+
+// component norms of every node of several trees: one launch, one download, one synchronisation
+void tree_norms_batch(const std::vector<Tree *> &trees, const int *nnodes, Arena &arena) {
+    Ctx &ctx = *trees[0]->ctx;
+    const int n = (int)trees.size();
+    std::vector<double *> bl, cnp;
+    for (int i = 0; i < n; i++) {
+        Tree &t = *trees[i];
+        for (int j = 0; j < t.nn(); j++) {
+            bl.push_back(t.block(j));
+            cnp.push_back(t.d_cn + (size_t)j * 8);
+        }
+    }
+    Packer pk;
+    pk.add(bl.data(), bl.size() * sizeof(double *));
+    pk.add(cnp.data(), cnp.size() * sizeof(double *));
+    pk.ship(ctx, arena);
+    k_norms(ctx.dbasis, (double *const *)pk.ptr(0), (double *const *)pk.ptr(1), (int)bl.size(), ctx.stream);
+    std::vector<double *> hcn(n);
+    for (int i = 0; i < n; i++) {
+        hcn[i] = (double *)arena.halloc(sizeof(double) * 8 * nnodes[i]);
+        MWG_CUDA(cudaMemcpyAsync(hcn[i], trees[i]->d_cn, sizeof(double) * 8 * nnodes[i], cudaMemcpyDeviceToHost,
+                                 ctx.stream));
+    }
+    ctx.sync();
+    for (int i = 0; i < n; i++) std::copy(hcn[i], hcn[i] + (size_t)8 * nnodes[i], trees[i]->cn.begin());
+    arena.reset();
+}
+
+void tree_download_batch(const std::vector<Tree *> &trees, int *const *keys, double *const *coefs,
+                         unsigned char *const *leaf) {
+    if (trees.empty()) return;
+    Ctx &ctx = *trees[0]->ctx;
+    const int bs = ctx.basis.bs, n = (int)trees.size();
+    std::vector<std::vector<int>> idx(n);
+    std::vector<size_t> first(n + 1, 0);
+    for (int i = 0; i < n; i++) first[i + 1] = first[i] + (size_t)trees[i]->nn();
+    for (int i = 0; i < n; i++) idx[i] = canonical_order(*trees[i]);
+    bool pinned = true;
+    for (int i = 0; i < n && pinned; i++) pinned = !coefs[i] || host_is_pinned(coefs[i]);
+    double *h = nullptr;
+    if (pinned) {
+        // permutation into canonical order on the device, then straight into the caller's buffers
+        Arena &arena = ctx.arena;
+        ctx.sync();
+        arena.reset();
+        double *scratch = (double *)arena.alloc(sizeof(double) * (size_t)bs * first[n]);
+        std::vector<int> maps;
+        maps.reserve(first[n]);
+        for (int i = 0; i < n; i++) maps.insert(maps.end(), idx[i].begin(), idx[i].end());
+        Packer pk;
+        pk.add(maps.data(), maps.size() * sizeof(int));
+        pk.ship(ctx, arena);
+        const int *dmap = (const int *)pk.ptr(0);
+        for (int i = 0; i < n; i++) {
+            if (!coefs[i]) continue;
+            k_permute_blocks(scratch + first[i] * bs, trees[i]->d_coefs, dmap + first[i], trees[i]->nn(), bs,
+                             ctx.stream);
+            MWG_CUDA(cudaMemcpyAsync(coefs[i], scratch + first[i] * bs, sizeof(double) * (size_t)bs * trees[i]->nn(),
+                                     cudaMemcpyDeviceToHost, ctx.stream));
+        }
+    } else {
+        h = (double *)ctx.pinned(sizeof(double) * (size_t)bs * first[n]);
+        for (int i = 0; i < n; i++)
+            if (coefs[i])
+                MWG_CUDA(cudaMemcpyAsync(h + first[i] * bs, trees[i]->d_coefs,
+                                         sizeof(double) * (size_t)bs * trees[i]->nn(), cudaMemcpyDeviceToHost,
+                                         ctx.stream));
+    }
+    ctx.sync();
+    if (pinned) ctx.arena.reset();
+    std::vector<std::pair<int, int>> all;
+    all.reserve(first[n]);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < trees[i]->nn(); j++) all.push_back({i, j});
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < (long)all.size(); q++) {
+        const int i = all[q].first, j = all[q].second;
+        const int src = idx[i][j];
+        if (coefs[i] && h) std::memcpy(coefs[i] + (size_t)j * bs, h + (first[i] + src) * bs, sizeof(double) * bs);
+        const NodeInfo &nd = trees[i]->nodes[src];
+        if (keys[i]) {
+            keys[i][4 * j] = nd.n;
+            for (int d = 0; d < 3; d++) keys[i][4 * j + 1 + d] = nd.l[d];
+        }
+        if (leaf[i]) leaf[i][j] = nd.child0 < 0;
+    }
 }
 
 void tree_download(Tree &t, int *keys, double *coefs, unsigned char *leaf) {

@@ -118,3 +118,42 @@ def test_tree_file_roundtrip(engine, tmp_path):
         fh.truncate(100)
     with pytest.raises(engine.MWError):
         engine.load_tree(engine.FunctionTree(mra), path)
+
+
+def test_batched_upload_download_match_single(engine):
+    # mw_tree_upload_batch / mw_tree_download_batch: the same trees, blocks and norms as one call
+    # per tree, with keys given in a shuffled order
+    mra = engine.MultiResolutionAnalysis(7)
+    srcs = [engine.project(1e-5, engine.FunctionTree(mra), [(1.0, a, (0.1 * i, -0.2, 0.3), (i % 2, 0, 0))],
+                           abs_prec=True) for i, a in enumerate((1.5, 6.0, 20.0))]
+    data = [s.download() for s in srcs]
+    rng = np.random.default_rng(3)
+    shuffled = []
+    for k, c, _ in data:
+        p = rng.permutation(k.shape[0])
+        shuffled.append((k[p], c[p]))
+    single = [engine.FunctionTree(mra).upload(k, c) for k, c in shuffled]
+    batch = engine.upload_batch([engine.FunctionTree(mra) for _ in shuffled], shuffled)
+    got = engine.download_batch(batch)
+    again = engine.download_batch(batch, outs=got)  # into the same buffers
+    for s, b, (k0, c0, l0), (k1, c1, l1), (k2, c2, l2) in zip(single, batch, data, got, again):
+        ks, cs, ls = s.download()
+        assert np.array_equal(ks, k0) and np.array_equal(k1, k0) and np.array_equal(k2, k0)
+        assert np.array_equal(cs, c0) and np.array_equal(c1, c0) and np.array_equal(c2, c0)
+        assert np.array_equal(l1, l0) and s.norm() == b.norm()
+    # pinned buffers: direct copies, with the reordering done on the device
+    pinned_in = [(k.copy(), c.copy()) for k, c in shuffled]
+    for _, c in pinned_in:
+        engine.pin_host(mra, c)
+    outs = [(np.empty_like(k), np.empty_like(c), np.empty_like(l)) for k, c, l in data]
+    for o in outs:
+        engine.pin_host(mra, o[1])
+    pb = engine.upload_batch([engine.FunctionTree(mra) for _ in pinned_in], pinned_in)
+    res = engine.download_batch(pb, outs=outs)
+    for (k0, c0, l0), (k1, c1, l1), o, s, t in zip(data, res, outs, single, pb):
+        assert c1 is o[1] and np.array_equal(k1, k0) and np.array_equal(c1, c0) and np.array_equal(l1, l0)
+        assert s.norm() == t.norm()
+    for _, c in pinned_in:
+        engine.unpin_host(mra, c)
+    for o in outs:
+        engine.unpin_host(mra, o[1])
