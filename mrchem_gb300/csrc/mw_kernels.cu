@@ -432,16 +432,19 @@ __device__ __forceinline__ void lds_row(float (&r)[N], const float *p) {
 }
 
 // FP32 tier of the NS-form apply.  Same contraction and exclusion as
-// apply_kernel, arranged so that shared-memory reads are vector reads that a
-// warp mostly shares: the x pass (thread (Y, X'), X' fastest) reads rows of the
+// apply_kernel; each thread computes two outputs of every pass (indices i and
+// i + K of one dimension), so that every row it reads from shared memory feeds
+// twice the FMAs.  The x pass (thread (Y, X'), X' in [0, K)) reads rows of the
 // input cube and stores t1 transposed as t1T[Z][X'][Y]; the y and z passes use
-// the mapping (Y', X') with Y' fastest, so that the lanes of a warp read the
-// same one or two rows of t1T, and hold their A_y row in registers; the node
-// accumulator acc[Z'][X'][Y'] (Y' fastest) lives in shared memory (two CTAs
-// per SM).  The FP32 partial sum of the node is added once to its FP64 block.
+// (Y', X') with Y' in [0, K) fastest, so that the lanes of a warp read the same
+// few rows of t1T, and hold their two A_y rows in registers; the node
+// accumulator acc[Z'][X'][Y'] lives in shared memory (two CTAs per SM).  Each
+// output's sums run in the same order as in the one-output form.  The FP32
+// partial sum of the node is added once to its FP64 block.
 template <int K>
-__global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kernel(ApplyLaunch L) {
+__global__ void __launch_bounds__(((2 * K * K + 31) / 32) * 32, 2) apply32_kernel(ApplyLaunch L) {
     constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K, U = ((K3 + 3) / 4) * 4;
+    constexpr int NH = NC / 2;  // threads with work: (2K) x K
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *s_in = reinterpret_cast<float *>(smem_raw);
     float *s_t1 = s_in + C;   // t1T[Z][X'][Y]
@@ -450,13 +453,13 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kerne
     float *s_A = s_u + U;
     __shared__ int s_node;
     const int tid = threadIdx.x;
-    const bool active = tid < NC;
-    // x pass: thread (Y = Yp, X' = Xp), X' fastest
-    const int Yp = tid / N2, Xp = tid % N2;
-    const bool excl = !L.root && active && (Yp < K) && (Xp < K);
-    // y and z passes, epilogue: thread (Y' = Yq, X' = Xq), Y' fastest
-    const int Xq = tid / N2, Yq = tid % N2;
-    const bool exq = !L.root && active && (Yq < K) && (Xq < K);
+    const bool active = tid < NH;
+    // x pass: thread (Y = Yp, X' = Xh and Xh + K), Xh fastest
+    const int Yp = tid / K, Xh = tid % K;
+    const bool excl = !L.root && active && (Yp < K);  // u for X' = Xh (< K) on the scaling octant
+    // y and z passes, epilogue: thread (Y' = Yh and Yh + K, X' = Xq), Yh fastest
+    const int Xq = tid / K, Yh = tid % K;
+    const bool exq = !L.root && active && (Xq < K);  // t2x for Y' = Yh (< K)
 
     while (true) {
         if (tid == 0) s_node = atomicAdd(L.counter, 1);
@@ -481,74 +484,97 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kerne
             }
             const float cf = float(L.coef[j]);
             __syncthreads();
-            if (active) {  // x pass, thread (Y = Yp, X' = Xp)
-                float a[N2];
-                lds_row<N2>(a, s_A + Xp * N2);
+            if (active) {  // x pass
+                float a0[N2], a1[N2];
+                lds_row<N2>(a0, s_A + Xh * N2);
+                lds_row<N2>(a1, s_A + (Xh + K) * N2);
 #pragma unroll 2
                 for (int Z = 0; Z < N2; Z++) {
                     float row[N2];
                     lds_row<N2>(row, s_in + (Z * N2 + Yp) * N2);
-                    float s0 = 0.0f, s1 = 0.0f;
+                    float p0 = 0.0f, p1 = 0.0f, q0 = 0.0f, q1 = 0.0f;
 #pragma unroll
-                    for (int X = 0; X < K; X++) s0 = fmaf(a[X], row[X], s0);
+                    for (int X = 0; X < K; X++) {
+                        p0 = fmaf(a0[X], row[X], p0);
+                        q0 = fmaf(a1[X], row[X], q0);
+                    }
 #pragma unroll
-                    for (int X = K; X < N2; X++) s1 = fmaf(a[X], row[X], s1);
-                    s_t1[(Z * N2 + Xp) * N2 + Yp] = s0 + s1;
-                    if (excl && Z < K) s_u[(Z * K + Xp) * K + Yp] = s1;
+                    for (int X = K; X < N2; X++) {
+                        p1 = fmaf(a0[X], row[X], p1);
+                        q1 = fmaf(a1[X], row[X], q1);
+                    }
+                    s_t1[(Z * N2 + Xh) * N2 + Yp] = p0 + p1;
+                    s_t1[(Z * N2 + Xh + K) * N2 + Yp] = q0 + q1;
+                    if (excl && Z < K) s_u[(Z * K + Xh) * K + Yp] = p1;
                 }
             }
             __syncthreads();
-            if (active) {  // y and z passes, thread (Y' = Yq, X' = Xq)
-                float ayr[N2], t2[N2], t2x[K];
-                lds_row<N2>(ayr, s_A + NC + Yq * N2);
+            if (active) {  // y and z passes
+                float ay0[N2], ay1[N2], t20[N2], t21[N2], t2x[K];
+                lds_row<N2>(ay0, s_A + NC + Yh * N2);
+                lds_row<N2>(ay1, s_A + NC + (Yh + K) * N2);
 #pragma unroll
                 for (int Z = 0; Z < N2; Z++) {
                     float row[N2];
                     lds_row<N2>(row, s_t1 + (Z * N2 + Xq) * N2);
-                    float s0 = 0.0f, s1 = 0.0f;
+                    float p0 = 0.0f, p1 = 0.0f, q0 = 0.0f, q1 = 0.0f;
 #pragma unroll
-                    for (int Y = 0; Y < K; Y++) s0 = fmaf(ayr[Y], row[Y], s0);
+                    for (int Y = 0; Y < K; Y++) {
+                        p0 = fmaf(ay0[Y], row[Y], p0);
+                        q0 = fmaf(ay1[Y], row[Y], q0);
+                    }
 #pragma unroll
-                    for (int Y = K; Y < N2; Y++) s1 = fmaf(ayr[Y], row[Y], s1);
-                    t2[Z] = s0 + s1;
+                    for (int Y = K; Y < N2; Y++) {
+                        p1 = fmaf(ay0[Y], row[Y], p1);
+                        q1 = fmaf(ay1[Y], row[Y], q1);
+                    }
+                    t20[Z] = p0 + p1;
+                    t21[Z] = q0 + q1;
                     if (Z < K) {
                         float su = 0.0f;
                         if (exq) {
                             const float *urow = s_u + (Z * K + Xq) * K;
 #pragma unroll
-                            for (int Y = 0; Y < K; Y++) su = fmaf(ayr[Y], urow[Y], su);
+                            for (int Y = 0; Y < K; Y++) su = fmaf(ay0[Y], urow[Y], su);
                         }
-                        t2x[Z < K ? Z : 0] = su + s1;
+                        t2x[Z < K ? Z : 0] = su + p1;
                     }
                 }
 #pragma unroll
                 for (int Zp = 0; Zp < N2; Zp++) {
                     float azr[N2];
                     lds_row<N2>(azr, s_A + 2 * NC + Zp * N2);
-                    float sacc = 0.0f;
+                    float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
                     for (int Z = 0; Z < N2; Z++) {
-                        float v = t2[Z];
+                        float v = t20[Z];
                         if (Zp < K && Z < K) v = exq ? t2x[Z < K ? Z : 0] : v;
-                        sacc = fmaf(azr[Z], v, sacc);
+                        s0 = fmaf(azr[Z], v, s0);
+                        s1 = fmaf(azr[Z], t21[Z], s1);
                     }
-                    float &a_ = s_acc[(Zp * N2 + Xq) * N2 + Yq];
-                    a_ = fmaf(cf, sacc, a_);
+                    float &a0_ = s_acc[(Zp * N2 + Xq) * N2 + Yh];
+                    float &a1_ = s_acc[(Zp * N2 + Xq) * N2 + Yh + K];
+                    a0_ = fmaf(cf, s0, a0_);
+                    a1_ = fmaf(cf, s1, a1_);
                 }
             }
         }
         __syncthreads();
         if (active) {
             double *out = L.out[w];
-#pragma unroll
+#pragma unroll 4
             for (int Zp = 0; Zp < N2; Zp++) {
-                int c = (Xq >= K ? 1 : 0) | (Yq >= K ? 2 : 0) | (Zp >= K ? 4 : 0);
-                int gi = c * K3 + (Zp % K) * K * K + (Yq % K) * K + (Xq % K);
-                double v = double(s_acc[(Zp * N2 + Xq) * N2 + Yq]);
-                if (L.set)
-                    out[gi] = v;
-                else
-                    out[gi] += v;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int Yq = Yh + h * K;
+                    const int c = (Xq >= K ? 1 : 0) | (Yq >= K ? 2 : 0) | (Zp >= K ? 4 : 0);
+                    const int gi = c * K3 + (Zp % K) * K * K + (Yq % K) * K + (Xq % K);
+                    const double v = double(s_acc[(Zp * N2 + Xq) * N2 + Yq]);
+                    if (L.set)
+                        out[gi] = v;
+                    else
+                        out[gi] += v;
+                }
             }
         }
         __syncthreads();
@@ -558,8 +584,8 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32, 2) apply32_kerne
 template <typename T, int K>
 void launch_apply_t(const ApplyLaunch &L, int nsm, cudaStream_t s) {
     constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K;
-    const int threads = ((NC + 31) / 32) * 32;
     const bool f32 = sizeof(T) == 4;
+    const int threads = f32 ? ((NC / 2 + 31) / 32) * 32 : ((NC + 31) / 32) * 32;
     const size_t smem = f32 ? sizeof(float) * (3 * C + ((K3 + 3) / 4) * 4 + 3 * NC) : sizeof(T) * (2 * C + K3 + 3 * NC);
     auto fn = f32 ? apply32_kernel<K> : apply_kernel<T, K>;
     MWG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
