@@ -285,22 +285,32 @@ def run(args):
     fp32_tf = mra.probe_fma_peak(False)
     tf32_tf = mra.probe_mma_peak("tf32")
 
-    def roof(flops, ms, peak, kernel, bound, source):
+    # DRAM read bytes per item of each tier kernel, from an ncu capture of the 4-orbital case of this
+    # batch (dram__bytes_read.sum + dram__bytes_write.sum over all launches of one step / items);
+    # traffic per step = that x the tier's items in this step
+    dram_per_item = {"fp32": 2.79e3, "tf32": 1.34e3, "df32": 10.1e3}
+    tier_items = {"fp64": st_ser["items_fp64"], "fp32": st_ser["items_fp32"], "tf32": st_ser["items_tf32"],
+                  "df32": st_ser["items_df"]}
+
+    def roof(flops, ms, peak, kernel, bound, source, tier=None):
         ach = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
+        traffic = dram_per_item[tier] * tier_items[tier] if tier in dram_per_item else None
         return {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak if peak else None,
-                "traffic": None, "kernel": kernel, "kernel_ms_per_step": ms, "peak_source": source}
+                "traffic": traffic, "traffic_unit": "bytes per step (all launches of the kernel)" if traffic else None,
+                "traffic_source": "ncu dram bytes per item on the 4-orbital case, scaled by items" if traffic else None,
+                "kernel": kernel, "kernel_ms_per_step": ms, "peak_source": source}
 
     fma_src = "probed FMA throughput of this GPU (mw_probe_fma_peak); MEASURED_PEAKS.json holds no FP64/FP32 figure"
     mma_src = ("probed dense m16n8k8 TF32 warp-MMA throughput of this GPU (mw_probe_mma_peak); "
                "MEASURED_PEAKS.json holds no TF32 figure")
     roofs = {
         "fp64": roof(st_ser["flops_fp64"], st_ser["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
-        "fp32": roof(st_ser["flops_fp32"], st_ser["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src),
-        "tf32": roof(st_ser["flops_tf32"], st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc_kernel<10>", "tensor", mma_src),
+        "fp32": roof(st_ser["flops_fp32"], st_ser["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src, tier="fp32"),
+        "tf32": roof(st_ser["flops_tf32"], st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc_kernel<10>", "tensor", mma_src, tier="tf32"),
         # a double-FP32 multiply-add costs 12 FP32 instructions: peak = FP32 FMA peak * 2 / 24
         "df32": roof(st_ser["flops_df"], st_ser["kernel_ms_df"], fp32_tf / 12.0, "apply_df_kernel<10>",
                      "fp32-pipe (double-FP32)", fma_src + "; divided by 12 FP32 instructions per double-FP32 "
-                     "multiply-add"),
+                     "multiply-add", tier="df32"),
     }
     dominant = max(roofs, key=lambda k: roofs[k]["kernel_ms_per_step"])
     line = {

@@ -408,10 +408,11 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         if (job.inp->ctx != &ctx || job.out->ctx != &ctx || job.op->ctx != &ctx)
             throw Error(MW_ERR_ARG, "apply: trees and operator must belong to one context");
         s.set_fmax(*job.inp, b.n0);
-        if (!fixed_grid) {
-            if (job.out->nn() != job.out->nroots) throw Error(MW_ERR_STATE, "apply: output tree must be empty");
-            tree_zero(*job.out, 0, job.out->nn());
-        }
+        if (!fixed_grid && job.out->nn() != job.out->nroots)
+            throw Error(MW_ERR_STATE, "apply: output tree must be empty");
+        // every tier adds into the output blocks: they start at zero (on a fixed grid too, whose
+        // coefficients the apply replaces)
+        tree_zero(*job.out, 0, job.out->nn());
         if (mixed) {
             Tree &in = *job.inp;
             if (in.cap32 < (size_t)in.nn()) {
@@ -648,14 +649,14 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             }
             for (int k = 0; k < NTIER; k++) cnt[k][q + 1] = c[k];
         }
-        // FP64 launch: every node (it writes the block); other tiers: nodes that have items there
+        // every tier adds to the output blocks (zeroed when their nodes were created), so each
+        // tier launches only the nodes that have items in it
         LevelItems *lt = G.lt;
         std::vector<long> slot[NTIER];
-        long nnt[NTIER] = {NN, 0, 0, 0};
+        long nnt[NTIER] = {0, 0, 0, 0};
         for (int k = 0; k < NTIER; k++) slot[k].assign(NN, -1);
         for (long q = 0; q < NN; q++) {
-            slot[0][q] = q;
-            for (int k = 1; k < NTIER; k++)
+            for (int k = 0; k < NTIER; k++)
                 if (cnt[k][q + 1] > 0) slot[k][q] = nnt[k]++;
             for (int k = 0; k < NTIER; k++) cnt[k][q + 1] += cnt[k][q];
         }
@@ -719,7 +720,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         MWG_CUDA(cudaEventRecord(G.ev[0], ctx.stream));
         G.status.clear();
         for (int k = 0; k < NTIER; k++) {
-            int *hs = launch_tier(ctx, ar, lt[k], root, k == 0, k, st);
+            int *hs = launch_tier(ctx, ar, lt[k], root, false, k, st);
             if (hs) G.status.push_back(hs);
             MWG_CUDA(cudaEventRecord(G.ev[k + 1], ctx.stream));
         }
