@@ -143,6 +143,22 @@ def run_reference(args):
                       "e2e": {"value": v, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def max_over_ranks(ms, device):
+    """The slowest rank's time: every rank's timed region ends at a barrier, the job at its last rank."""
+    import torch
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+        return float(ms)
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, t_max_ms):
+    """Units processed by all ranks (each rank runs the same workload, weak scaling) per second."""
+    return units_per_rank * world / (t_max_ms / 1e3)
+
+
 def run(args):
     import torch
 
@@ -235,13 +251,8 @@ def run(args):
     ms = start.elapsed_time(end) / args.steps
     nodes = stats[-1]["out_nodes"]
     errs = [rel_err(o, r) for o, r in zip(outs, ref)]
-    local_v = nodes / (ms / 1e3)
-    t_max = ms
-    if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
-    value = nodes * world / (t_max / 1e3)
+    t_max = max_over_ranks(ms, "cuda")
+    value = whole_job_rate(nodes, world, t_max)
 
     # end-to-end through the C ABI: host input buffers -> device, apply, device -> host output.
     # One untimed step sizes the device trees and the host output buffers; every timed step then
@@ -272,8 +283,8 @@ def run(args):
     for _ in range(args.e2e_steps):
         d2h = e2e_step()
     barrier()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    e2e_v = nodes * world / e2e_s
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps * 1e3, "cuda")
+    e2e_v = whole_job_rate(nodes, world, e2e_ms)
 
     st = stats[-1]
     # one step with the job groups not overlapped: its tier kernels run alone, so their
