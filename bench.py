@@ -55,6 +55,7 @@ class ClockSampler:
 
     def __init__(self):
         self.samples, self.proc = [], None
+        self.t0 = self.t1 = None  # the timed region (perf_counter seconds)
 
     def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -62,7 +63,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", "0"], stdout=subprocess.PIPE, text=True)
+                                          "-lms", "50", "-i", "0"], stdout=subprocess.PIPE, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except (OSError, FileNotFoundError):
@@ -73,22 +74,30 @@ class ClockSampler:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) == 7:
-                self.samples.append(parts)
+                self.samples.append((time.perf_counter(), parts))
 
     def __exit__(self, *a):
         if self.proc:
             self.proc.terminate()
             self.proc.wait()
 
+    def mark(self, start):
+        if start:
+            self.t0 = time.perf_counter()
+        else:
+            self.t1 = time.perf_counter()
+
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        inside = [p for t, p in self.samples
+                  if (self.t0 is None or t >= self.t0) and (self.t1 is None or t <= self.t1)]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(s[0]) for s in inside if s[0].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        reasons = sorted({names[i] for s in inside for i in range(4) if s[3 + i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": float(self.samples[0][1]) if self.samples[0][1].replace(".", "").isdigit() else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "sm_max_mhz": float(inside[0][1]) if inside[0][1].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(inside)}
 
 
 def measured_peaks():
@@ -98,23 +107,31 @@ def measured_peaks():
         return {}
 
 
-def cpu_sample(terms, mus, max_iter):
-    """Oracle (OpenMP FP64) Helmholtz apply of orbital 0 (max_iter = -1: the complete adaptive apply)."""
+def cpu_sample(terms, mus, max_iter, budget_s):
+    """Oracle (OpenMP FP64) Helmholtz applies of the batch's orbitals 0, 1, ... in turn, until
+    budget_s seconds of apply time have passed or the batch is done (max_iter = -1: the complete
+    adaptive apply of each).  Projection and operator setup are outside the timed part."""
     from oracle import pyoracle as po
     po.build()
     threads = os.cpu_count() or 1
     po.set_threads(threads)
     mra = po.MRA(ORDER)
-    phi = po.project_gauss(PREC, po.Tree(mra), terms[0], abs_prec=True)
-    phi.rescale(1.0 / phi.norm())
-    op = po.helmholtz(mra, float(mus[0]), PREC)
-    out = po.Tree(mra)
-    t0 = time.perf_counter()
-    st = po.apply(PREC, out, op, phi, max_iter=max_iter, abs_prec=True)
-    dt = time.perf_counter() - t0
-    return {"value": st["out_nodes"] / dt, "unit": "nodes/s", "cores": threads, "kind": "port",
-            "sample": "orbital 0 of the batch, %s adaptive apply (%d output nodes, %.1f s)"
-                      % ("complete" if max_iter < 0 else "levels 0..%d of the" % max_iter, st["out_nodes"], dt)}
+    nodes, dt, done = 0, 0.0, 0
+    for i in range(len(terms)):
+        phi = po.project_gauss(PREC, po.Tree(mra), terms[i], abs_prec=True)
+        phi.rescale(1.0 / phi.norm())
+        op = po.helmholtz(mra, float(mus[i]), PREC)
+        out = po.Tree(mra)
+        t0 = time.perf_counter()
+        st = po.apply(PREC, out, op, phi, max_iter=max_iter, abs_prec=True)
+        dt += time.perf_counter() - t0
+        nodes += st["out_nodes"]
+        done += 1
+        if dt >= budget_s:
+            break
+    return {"value": nodes / dt, "unit": "nodes/s", "cores": threads, "kind": "port",
+            "sample": "orbitals 0..%d of the batch, %s adaptive apply each (%d output nodes, %.1f s)"
+                      % (done - 1, "complete" if max_iter < 0 else "levels 0..%d of the" % max_iter, nodes, dt)}
 
 
 def run_reference(args):
@@ -125,10 +142,10 @@ def run_reference(args):
     terms, mus = orbital_terms(rng)
     vals = []
     for _ in range(args.warmup):
-        cpu_sample(terms, mus, args.cpu_levels)
+        cpu_sample(terms, mus, args.cpu_levels, args.ref_step_s)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        s = cpu_sample(terms, mus, args.cpu_levels)
+        s = cpu_sample(terms, mus, args.cpu_levels, args.ref_step_s)
         vals.append(s["value"])
     wall = time.perf_counter() - t0
     v = float(np.mean(vals))
@@ -237,17 +254,21 @@ def run(args):
     f32_ms, st_f32 = timed("mixed-fp32", 1)
     f32_err = max(rel_err(o, r) for o, r in zip(outs, ref))
 
-    for _ in range(args.warmup):
-        step("mixed", outs)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stats = []
+    # the sampler starts before the warm-up steps (nvidia-smi takes a while to print its first
+    # line); only the samples taken between the two marks are reported
     with ClockSampler() as clk:
+        for _ in range(args.warmup):
+            step("mixed", outs)
         barrier()
+        clk.mark(True)
         start.record()
         for _ in range(args.steps):
             stats.append(step("mixed", outs))
         end.record()
         barrier()
+        clk.mark(False)
     ms = start.elapsed_time(end) / args.steps
     nodes = stats[-1]["out_nodes"]
     errs = [rel_err(o, r) for o, r in zip(outs, ref)]
@@ -364,7 +385,7 @@ def run(args):
     }
     line["speedup_mixed_vs_fp64"] = (nodes / (ms / 1e3)) / (st64["out_nodes"] / fp64_s)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_sample(terms, mus, args.cpu_levels)
+        line["cpu_baseline"] = cpu_sample(terms, mus, args.cpu_levels, args.cpu_s)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -374,11 +395,15 @@ def run(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-levels", type=int, default=-1)
+    ap.add_argument("--cpu-s", type=float, default=12.0,
+                    help="seconds of oracle apply time for the cpu_baseline sample")
+    ap.add_argument("--ref-step-s", type=float, default=4.0,
+                    help="seconds of oracle apply time per step of --impl reference")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--orbitals", type=int, default=16)
     ap.add_argument("--fp64-steps", type=int, default=1)

@@ -843,7 +843,10 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         Packer pk;
         pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
         pk.ship(ctx, arena);
-        k_topdown(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
+        if (mixed)
+            k_topdown_df(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
+        else
+            k_topdown(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
         st.launches++;
     }
     for (int n = maxn - 1; n >= b.n0; n--) {
@@ -862,7 +865,12 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
         pk.add(cnp.data(), cnp.size() * sizeof(double *));
         pk.ship(ctx, arena);
-        k_compress(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(), ctx.stream);
+        if (mixed)
+            k_compress_df(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(),
+                          ctx.stream);
+        else
+            k_compress(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(),
+                       ctx.stream);
         st.launches++;
     }
     // leaf norms after the top-down pass

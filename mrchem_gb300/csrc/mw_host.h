@@ -264,6 +264,9 @@ void k_apply_df(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s
 void k_norms(const DevBasis &b, double *const *blocks, double *const *cn, int n, cudaStream_t s);
 void k_topdown(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s);
 void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s);
+// the same two passes with double-FP32 arithmetic on the FP32 pipe (mw_post_df.cu); FP64 blocks and norms
+void k_topdown_df(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s);
+void k_compress_df(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s);
 void k_multiply(const DevBasis &b, const MulTask *tasks, int n, cudaStream_t s);
 void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
            cudaStream_t s);
