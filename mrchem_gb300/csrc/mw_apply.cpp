@@ -23,6 +23,7 @@
 #include <cstring>
 
 #include "mw_internal.h"
+#include "mw_tc05_layout.h"
 
 namespace mwg {
 
@@ -149,6 +150,7 @@ struct JobState {
     GenSet gens;
     double *gbase = nullptr;
     float *gbase32 = nullptr;
+    float *gbase_tc = nullptr;  // generated blocks in the tensor-core tier's x-pass layout
     std::vector<double> gcn;
     std::vector<std::vector<Cand>> cand;
 };
@@ -356,7 +358,7 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
         k_apply_df(ctx.dbasis, L, ctx.nsm, ctx.stream);
     } else {
         if (tier == 2)
-            k_apply_tc(ctx.dbasis, L, ctx.nsm, ctx.stream);
+            k_apply_tc05(ctx.dbasis, L, ctx.stream);
         else
             k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
         if (tier == 2) {  // the TF32 kernel waits for bulk copies with a bound
@@ -374,7 +376,8 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
 
 void check_status(const int *hs) {
     if (hs && *hs != 0)
-        throw Error(MW_ERR_TIMEOUT, "apply: a bounded wait for an asynchronous copy ran out");
+        throw Error(MW_ERR_TIMEOUT,
+                    "apply: a bounded wait for an asynchronous copy or MMA ran out (status " + std::to_string(*hs) + ")");
 }
 
 }  // namespace
@@ -422,6 +425,15 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             }
             k_to_fp32_cube(in.d_coefs, in.d_coefs32, (size_t)in.nn(), b.K, ctx.stream);
             st.launches++;
+            if (tensor) {
+                if (in.cap_tc < (size_t)in.nn()) {
+                    if (in.d_coefs_tc) cudaFree(in.d_coefs_tc);
+                    MWG_CUDA(cudaMalloc(&in.d_coefs_tc, sizeof(float) * tc5_x_floats(b.K) * in.cap));
+                    in.cap_tc = in.cap;
+                }
+                k_to_tc_x(in.d_coefs32, in.d_coefs_tc, (size_t)in.nn(), b.K, ctx.stream);
+                st.launches++;
+            }
         }
         for (int i = 0; i < job.out->nroots; i++) s.work.push_back(i);
         if (fixed_grid) max_levels = std::max(max_levels, job.out->max_scale() - b.n0 + 1);
@@ -581,17 +593,23 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             double *first = nullptr;
             for (JobState *sp : jp)
                 if (sp->gens.base && !first) first = sp->gens.base;
-            float *first32 = nullptr;
+            float *first32 = nullptr, *firsttc = nullptr;
             if (mixed && total > 0) {
                 first32 = (float *)ar.alloc(sizeof(float) * 2 * (size_t)bs * total);
                 k_to_fp32_cube(first, first32, total, b.K, ctx.stream);
                 st.launches++;
+                if (tensor) {
+                    firsttc = (float *)ar.alloc(sizeof(float) * tc5_x_floats(b.K) * total);
+                    k_to_tc_x(first32, firsttc, total, b.K, ctx.stream);
+                    st.launches++;
+                }
             }
             for (JobState *sp : jp) {
                 JobState &s = *sp;
                 s.gbase = s.gens.base;
                 s.gcn.swap(s.gens.cn);
                 s.gbase32 = (first32 && s.gbase) ? first32 + 2 * (s.gbase - first) : nullptr;
+                s.gbase_tc = (firsttc && s.gbase) ? firsttc + tc5_x_floats(b.K) * (size_t)((s.gbase - first) / bs) : nullptr;
             }
         }
         auto tC = std::chrono::steady_clock::now();
@@ -691,6 +709,14 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     T.ax[pi] = op.d_blocks + (size_t)bxi * bsz;
                     T.ay[pi] = op.d_blocks + (size_t)byi * bsz;
                     T.az[pi] = op.d_blocks + (size_t)bzi * bsz;
+                } else if (cd.tier == 2) {
+                    // the tensor-core tier reads its own operand layouts (mw_tc05_layout.h)
+                    const size_t tx = tc5_x_floats(b.K), tb = tc5_b_floats(b.K);
+                    T.in[pi] = cd.gen ? (const void *)(s.gbase_tc + tx * (size_t)cd.src)
+                                      : (const void *)(inp.d_coefs_tc + tx * (size_t)cd.src);
+                    T.ax[pi] = op.d_blocks_tc + tb * (size_t)bxi;
+                    T.ay[pi] = op.d_blocks_tc + tb * (size_t)byi;
+                    T.az[pi] = op.d_blocks_tc + tb * (size_t)bzi;
                 } else {
                     // the reduced tiers read the FP32 cube-order shadows and the FP32 operator blocks
                     // (high part first, low part after it)

@@ -1,0 +1,434 @@
+// mw_apply_tc05.cu -- TF32 tier of the NS-form apply on the 5th-generation tensor cores
+// (tcgen05.mma, accumulators in tensor memory).
+//
+// The item contraction of the other tiers (mw_kernels.cu),
+//
+//   x pass  T1[(Z,Y)][X']  = sum_X IN[Z][Y][X]  A_x[X'][X]
+//   y pass  T2[(X',Z)][Y'] = sum_Y T1[Z][Y][X'] A_y[Y'][Y]
+//   z pass  OUT[(Y',X')][Z'] += sum_Z T2[Z][Y'][X'] c A_z[Z'][Z],
+//
+// as three GEMMs D[M x N] = A[M x 8k] B[N x 8k]^T of tcgen05.mma.kind::tf32 with M = 128,
+// N = 32 (16 for K <= 5) and FP32 accumulation in tensor memory (TMEM).  The rows of a pass are
+// its (2K)^2 index pairs, padded to whole tiles of 128; the columns are the 2K output indices.
+// One thread issues the MMAs of a pass and commits them to an mbarrier; eight warps then read
+// the result out of TMEM (tcgen05.ld, one row per thread), round it to TF32 (cvt.rna) and store
+// it as the A operand of the next pass.  The z pass accumulates into a second TMEM region that
+// holds the output node for all of its items and is written to the FP64 block once.
+//
+// The scaling-scaling path is left out exactly below the root scale, as in the other tiers
+// (no subtraction):
+//   u   = the wavelet-in-x part of T1 on the scaling octant: K spare columns of the x pass get
+//         the first K rows of A_x with the scaling columns zeroed (prepared with the operator
+//         blocks), so one set of x MMAs yields T1 and u;
+//   t2x = the y pass in which u replaces T1 for Y < K: K^2 extra rows (X', Z < K) of the y pass
+//         (the row padding of the last tile has room for them);
+//   the z pass takes t2x for Z < K in K^2 extra rows (Y', X' < K), whose columns Z' < K replace
+//         those of the ordinary rows in the node epilogue.
+//
+// Operands in shared memory use the canonical K-major layout without swizzling: k-groups of 4
+// columns, row r of a group at byte 16 r (8-row core matrices of 128 bytes, M-direction stride
+// SBO = 128), groups LBO bytes apart.  The x pass's A (the input block) and every B (operator
+// block) arrive in that layout, already rounded to TF32, by one bulk copy (TMA engine) each:
+// the host prepares them once per input tree and per operator (mw_tc05_layout.h).  A_y and A_z
+// are written by the epilogues into region R, whose LBO is padded to 80 mod 128 bytes so that
+// the stores of a warp (one k per lane, rows shifted by one between the warp's runs of lanes)
+// fall into distinct banks.  The coefficient c_t scales A_z (written by the y epilogue), so the
+// operator blocks need no per-item scaling.
+//
+// Buffers: S (the input block, x pass), R (A_y, then A_z), a zero pad, and two sets of the
+// three B operands.  The next item's copies (into S and the other B set) start as soon as the
+// x MMAs have read S, so they run during this item's epilogues and y and z MMAs.
+//
+// Synchronisation: only the issuing thread waits for the copies (no other thread reads S or the
+// B operands), so it cannot start the next item's copies while another thread still waits for
+// the current ones.  A commit tracks every earlier MMA of the issuing thread, so the x pass's
+// barrier also says that the previous item's z MMAs are done with R and their B set; the z MMAs
+// get a commit of their own only at the end of a node.  The last k-step of a pass may read one k-group past
+// its operand (2K is not a multiple of 8): the B operands are zero there, and the bytes read
+// (S runs into R, R into the zero pad) are finite and not written while those MMAs run.  With
+// about 97 KB of shared memory and 256 TMEM columns per CTA, two CTAs share an SM, so one CTA's
+// MMAs run while the other's warps move data.
+//
+// Rounding: every operand is rounded to TF32 (unit roundoff 2^-11) as in the warp-level MMA
+// version, so an item is off by at most about 6 * 2^-11 * b (b = its screening bound).
+//
+// Every wait on an mbarrier is bounded; one that runs out marks the launch failed (status word,
+// reported by the host as MW_ERR_TIMEOUT) and the kernel ends normally, freeing its TMEM.
+#include "mw_async.cuh"
+#include "mw_host.h"
+#include "mw_tc05_layout.h"
+
+#include <algorithm>
+
+namespace mwg {
+
+namespace {
+
+template <int K>
+struct T5Geo {
+    static constexpr int N2 = 2 * K, NN = N2 * N2, KK = K * K, K3 = K * K * K;
+    static constexpr int RE = NN + KK;                 // rows of the y and z passes (ordinary + extra)
+    static constexpr int MT = (RE + 127) / 128;        // M tiles of the y and z passes
+    static constexpr int MTX = (NN + 127) / 128;       // M tiles of the x pass
+    static constexpr int N = tc5_n(K);                 // MMA N: 2K outputs + K columns of u
+    static constexpr int KG = tc5_kg(K);               // k-groups holding data
+    static constexpr int KS = tc5_ks(K);               // MMA k-steps of 8
+    static constexpr int LBO_S = NN * 16;              // the input block as staged (x pass A)
+    static constexpr int SX = KG * LBO_S;
+    static constexpr int LBO_R = ((RE * 16 - 80 + 127) / 128) * 128 + 80;  // >= RE rows, 80 mod 128
+    static constexpr int LBO_B = N * 16;
+    static constexpr int BSZ = 2 * KS * LBO_B;         // bytes of one B operand (all k-steps)
+    static constexpr int OR = SX, RSZ = KG * LBO_R;
+    // bytes an MMA pass reads from the start of its A operand
+    static constexpr int READ_S = (2 * KS - 1) * LBO_S + MTX * 2048;
+    static constexpr int READ_R = (2 * KS - 1) * LBO_R + MT * 2048;
+    static constexpr int ZPAD = READ_R > RSZ ? READ_R - RSZ : 0;
+    static constexpr int OB = OR + RSZ + ZPAD;         // two sets of (B_x, B_y, B_z)
+    static constexpr int SMEM = OB + 6 * BSZ;
+    static constexpr int TMEM_COLS = 2 * MT * N <= 32 ? 32 : (2 * MT * N <= 64 ? 64 : (2 * MT * N <= 128 ? 128 : 256));
+    static constexpr uint32_t STAGE_BYTES = (uint32_t)(SX + 3 * BSZ);
+    static constexpr int THREADS = 256;
+    // dynamic shared memory requested at launch: at least enough that no more CTAs share an SM
+    // than its 512 TMEM columns serve (an allocation beyond them would wait for another CTA)
+    static constexpr int MAX_CTAS = 512 / TMEM_COLS;
+    static constexpr int SMEM_FLOOR = 228 * 1024 / (MAX_CTAS + 1);
+    static constexpr int SMEM_LAUNCH = MAX_CTAS >= 8 || SMEM >= SMEM_FLOOR ? SMEM : SMEM_FLOOR;
+    static_assert(N2 + K <= N, "u columns do not fit");
+    static_assert(2 * MT * N <= 256, "TMEM budget");
+    static_assert((size_t)SX == tc5_x_floats(K) * 4 && (size_t)BSZ == tc5_b_floats(K) * 4, "layouts");
+    static_assert(LBO_R >= RE * 16 && LBO_R % 128 == 80, "R layout");
+    static_assert(READ_S <= SX + RSZ, "the x pass reads past R");
+    static_assert(SX % 16 == 0 && OB % 16 == 0 && BSZ % 16 == 0, "alignment");
+    static_assert(SMEM <= 113 * 1024, "two CTAs per SM");
+};
+
+__device__ __forceinline__ float tf32r(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// shared-memory matrix descriptor: canonical K-major layout without swizzling
+__device__ __forceinline__ uint64_t t5_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ void t5_mma(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void t5_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void t5_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void t5_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void async_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 32 consecutive TMEM columns of this warp's 32 lanes: v[j] = column j of lane (row) base + lane
+__device__ __forceinline__ void t5_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%"
+        "19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void t5_ld16(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
+#pragma unroll
+    for (int j = 16; j < 32; j++) v[j] = 0.0f;
+}
+
+template <int K>
+__device__ __forceinline__ void t5_ld(uint32_t taddr, float (&v)[32]) {
+    if (T5Geo<K>::N == 32)
+        t5_ld32(taddr, v);
+    else
+        t5_ld16(taddr, v);
+}
+
+// element (row r, column k) of region R (k-group stride LBO_R, 16 bytes per row)
+template <int K>
+__device__ __forceinline__ float *r_at(uint8_t *R, int r, int k) {
+    return reinterpret_cast<float *>(R + (k >> 2) * T5Geo<K>::LBO_R + 16 * r + 4 * (k & 3));
+}
+
+template <int K>
+__global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyLaunch L) {
+    using G = T5Geo<K>;
+    constexpr int N2 = G::N2, NN = G::NN, KK = G::KK, K3 = G::K3, N = G::N;
+    extern __shared__ __align__(1024) uint8_t smem5[];
+    uint8_t *sS = smem5, *sR = smem5 + G::OR, *sB = smem5 + G::OB;
+    __shared__ __align__(8) uint64_t bar[4];  // 0 staging copies, 1 x MMAs, 2 y MMAs, 3 end of a node
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_node;
+    __shared__ volatile int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int q = warp & 3, half = warp >> 2;  // TMEM lane quarter, tile parity of this warp
+    const bool excl = !L.root;
+
+    // zero everything once: padding rows, columns and k-groups are read by the MMAs
+    for (int i = tid; i < G::SMEM / 16; i += blockDim.x) reinterpret_cast<float4 *>(smem5)[i] = make_float4(0, 0, 0, 0);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
+                     "r"(G::TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int b = 0; b < 4; b++) mbar_init(&bar[b]);
+        s_fail = 0;
+    }
+    async_fence();
+    t5_before_sync();
+    __syncthreads();
+    t5_after_sync();
+    const uint32_t tmem = s_tmem;
+    const uint32_t tD = tmem, tACC = tmem + (uint32_t)(G::MT * N);  // column offsets
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    // descriptors of the operands' first core matrices; a tile / k-step adds its byte offset >> 4
+    const uint64_t dS = t5_desc(smem_addr(sS), G::LBO_S, 128), dR = t5_desc(smem_addr(sR), G::LBO_R, 128);
+    const uint64_t dB = t5_desc(smem_addr(sB), G::LBO_B, 128);
+    uint32_t ph[4] = {0, 0, 0, 0};  // bar[0]'s parity is tracked by thread 0 alone
+    uint32_t nitem = 0;  // items this CTA has started: B set nitem & 1
+
+    auto stage = [&](const void *in, const void *ax, const void *ay, const void *az, uint32_t set) {
+        if (s_fail) return;  // thread 0: the item's input block and B operands
+        async_fence();
+        mbar_expect_tx(&bar[0], G::STAGE_BYTES);
+        uint8_t *B = sB + set * 3 * G::BSZ;
+        bulk_copy(sS, in, G::SX, &bar[0]);
+        bulk_copy(B, ax, G::BSZ, &bar[0]);
+        bulk_copy(B + G::BSZ, ay, G::BSZ, &bar[0]);
+        bulk_copy(B + 2 * G::BSZ, az, G::BSZ, &bar[0]);
+    };
+    // status on a wait that runs out: 1 + barrier + 4 * (parity) + 8 * (items this CTA had started)
+    auto wait = [&](int b) {
+        mbar_wait(&bar[b], ph[b], &s_fail, L.status, 1 + b + 4 * (int)ph[b] + 8 * (int)(nitem < 65535u ? nitem : 65535u));
+        ph[b] ^= 1u;
+    };
+    // all threads: the MMAs may read what was stored; the issuing thread then orders after the sync
+    auto publish = [&]() {
+        async_fence();
+        t5_before_sync();
+        __syncthreads();
+        t5_after_sync();
+    };
+    // thread 0: tiles x k-steps of one pass, then a commit to barrier b (none if b < 0)
+    auto issue_pass = [&](uint64_t da, int lbo_a, uint64_t db, int tiles, uint32_t dcol, bool accumulate, int b) {
+        if (s_fail) return;
+        for (int i = 0; i < tiles; i++)
+#pragma unroll
+            for (int s = 0; s < G::KS; s++)
+                t5_mma(dcol + (uint32_t)(i * N), da + (uint64_t)((2 * s * lbo_a + i * 2048) >> 4),
+                       db + (uint64_t)((2 * s * G::LBO_B) >> 4), idesc, (accumulate || s > 0) ? 1u : 0u);
+        if (b >= 0) t5_commit(&bar[b]);
+    };
+
+    while (true) {
+        if (tid == 0) s_node = atomicAdd(L.counter, 1);
+        __syncthreads();
+        const int w = s_node;
+        if (w >= L.nnodes) break;
+        const long long b0 = L.begin[w], b1 = L.end[w];
+        if (tid == 0 && b0 < b1) stage(L.in[b0], L.ax[b0], L.ay[b0], L.az[b0], nitem & 1u);
+        for (long long j = b0; j < b1; j++, nitem++) {
+            const uint32_t set = nitem & 1u;
+            const uint64_t dBs = dB + (uint64_t)((set * 3 * G::BSZ) >> 4);
+            const float cf = float(L.coef[j]);
+            // item j+1's pointers, read early (thread 0 copies its blocks after the x MMAs)
+            const bool more = j + 1 < b1;
+            const void *nin = nullptr, *nax = nullptr, *nay = nullptr, *naz = nullptr;
+            if (tid == 0 && more) {
+                nin = L.in[j + 1];
+                nax = L.ax[j + 1];
+                nay = L.ay[j + 1];
+                naz = L.az[j + 1];
+            }
+            if (tid == 0) {
+                wait(0);  // item j's input block and B operands are in S and B set `set`
+                issue_pass(dS, G::LBO_S, dBs, G::MTX, tD, false, 1);
+            }
+            wait(1);  // the x MMAs, and every earlier MMA (the previous item's z pass), are done
+            t5_after_sync();
+            if (tid == 0 && more) stage(nin, nax, nay, naz, set ^ 1u);
+            // ---- x epilogue: D row (Z, Y) -> A_y rows (X', Z) and extra rows (X' < K, Z < K), k = Y
+            for (int i = half; i < G::MTX; i += 2) {
+                float v[32];
+                t5_ld<K>(tD + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * N), v);
+                const int r = i * 128 + 32 * q + lane;
+                if (r < NN) {
+                    const int Z = r / N2, Y = r - Z * N2;
+                    float *base = r_at<K>(sR, 0, Y);
+#pragma unroll
+                    for (int xp = 0; xp < N2; xp++) base[4 * (xp * N2 + Z)] = tf32r(v[xp]);
+                    if (Z < K) {
+#pragma unroll
+                        for (int xp = 0; xp < K; xp++)
+                            base[4 * (NN + xp * K + Z)] = tf32r(Y < K ? v[N2 + xp] : v[xp]);
+                    }
+                }
+            }
+            publish();
+            if (tid == 0) issue_pass(dR, G::LBO_R, dBs + (uint64_t)(G::BSZ >> 4), G::MT, tD, false, 2);
+            wait(2);
+            t5_after_sync();
+            // ---- y epilogue: D row (X', Z) -> c * A_z rows (Y', X') with k = Z; extra rows (Y', X' < K)
+            for (int i = half; i < G::MT; i += 2) {
+                float v[32];
+                t5_ld<K>(tD + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * N), v);
+                const int r = i * 128 + 32 * q + lane;
+                if (r < NN) {
+                    const int xp = r / N2, Z = r - xp * N2;
+                    float *base = r_at<K>(sR, 0, Z);
+#pragma unroll
+                    for (int yp = 0; yp < N2; yp++) base[4 * (yp * N2 + xp)] = tf32r(cf * v[yp]);
+                    if (Z >= K && xp < K) {
+#pragma unroll
+                        for (int yp = 0; yp < K; yp++) base[4 * (NN + yp * K + xp)] = tf32r(cf * v[yp]);
+                    }
+                } else if (r < G::RE) {
+                    const int e = r - NN, xp = e / K, Z = e - xp * K;
+                    float *base = r_at<K>(sR, 0, Z);
+#pragma unroll
+                    for (int yp = 0; yp < K; yp++) base[4 * (NN + yp * K + xp)] = tf32r(cf * v[yp]);
+                }
+            }
+            publish();
+            if (tid == 0) issue_pass(dR, G::LBO_R, dBs + (uint64_t)((2 * G::BSZ) >> 4), G::MT, tACC, j != b0, -1);
+        }
+        // ---- node epilogue: accumulator rows (Y', X'), columns Z' -> component-major FP64 block
+        if (b0 < b1) {
+            if (tid == 0 && !s_fail) t5_commit(&bar[3]);
+            wait(3);
+        }
+        t5_after_sync();
+        double *out = L.out[w];
+        for (int i = half; i < G::MT; i += 2) {
+            float v[32];
+            if (b0 < b1) {
+                t5_ld<K>(tACC + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * N), v);
+            } else {
+#pragma unroll
+                for (int c = 0; c < 32; c++) v[c] = 0.0f;
+            }
+            const int r = i * 128 + 32 * q + lane;
+            int yp = -1, xp = 0, zmax = 0, zmin = 0;
+            if (r < NN) {
+                yp = r / N2;
+                xp = r - yp * N2;
+                zmax = N2;
+                zmin = (excl && yp < K && xp < K) ? K : 0;  // Z' < K from the extra row
+            } else if (r < G::RE && excl) {
+                const int e = r - NN;
+                yp = e / K;
+                xp = e - yp * K;
+                zmax = K;
+            }
+            if (yp >= 0) {
+                const int cxy = (xp >= K ? 1 : 0) | (yp >= K ? 2 : 0);
+                const int off = (yp % K) * K + (xp % K);
+#pragma unroll
+                for (int zp = 0; zp < N2; zp++) {
+                    if (zp < zmin || zp >= zmax) continue;
+                    const int gi = (cxy | (zp >= K ? 4 : 0)) * K3 + (zp % K) * KK + off;
+                    if (L.set)
+                        out[gi] = double(v[zp]);
+                    else
+                        out[gi] += double(v[zp]);
+                }
+            }
+        }
+        t5_before_sync();
+        __syncthreads();
+        t5_after_sync();
+    }
+    if (s_fail && tid == 0) {
+        // a wait ran out: let whatever this CTA still has in flight end (bounded) before TMEM is freed
+        t5_commit(&bar[3]);
+        for (int b = 0; b < 4; b++)
+            for (int it = 0; it < TMA_WAIT_LIMIT; it++)
+                if (mbar_try_wait(&bar[b], ph[b])) break;
+    }
+    t5_before_sync();
+    __syncthreads();
+    t5_after_sync();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(G::TMEM_COLS));
+}
+
+template <int K>
+void launch_tc05(const ApplyLaunch &L, cudaStream_t s) {
+    using G = T5Geo<K>;
+    MWG_CUDA(cudaFuncSetAttribute(apply_tc05_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_LAUNCH));
+    const int grid = L.nnodes;
+    if (grid < 1) return;
+    apply_tc05_kernel<K><<<grid, G::THREADS, G::SMEM_LAUNCH, s>>>(L);
+    MWG_CUDA(cudaGetLastError());
+}
+
+// FP32 cube-order shadow (high cube) -> x-pass operand: float4 (g, r) = row r = Z * 2K + Y, X = 4g .. 4g+3
+__global__ void to_tc_x_kernel(const float *cube32, float *out, size_t nblocks, int K) {
+    const int N2 = 2 * K, NN = N2 * N2, KG = tc5_kg(K), C = NN * N2;
+    const size_t per = (size_t)KG * NN, total = nblocks * per;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t blk = i / per;
+        const int rem = (int)(i - blk * per), g = rem / NN, r = rem - g * NN;
+        const float *src = cube32 + blk * 2 * (size_t)C + (size_t)r * N2 + 4 * g;
+        float4 v;
+        v.x = 4 * g + 0 < N2 ? tf32r(src[0]) : 0.0f;
+        v.y = 4 * g + 1 < N2 ? tf32r(src[1]) : 0.0f;
+        v.z = 4 * g + 2 < N2 ? tf32r(src[2]) : 0.0f;
+        v.w = 4 * g + 3 < N2 ? tf32r(src[3]) : 0.0f;
+        reinterpret_cast<float4 *>(out)[i] = v;
+    }
+}
+
+}  // namespace
+
+void k_to_tc_x(const float *cube32, float *out, size_t nblocks, int K, cudaStream_t s) {
+    if (nblocks == 0) return;
+    const size_t total = nblocks * (size_t)tc5_kg(K) * (size_t)(4 * K * K);
+    const int grid = (int)std::min<size_t>((total + 255) / 256, 4096);
+    to_tc_x_kernel<<<grid, 256, 0, s>>>(cube32, out, nblocks, K);
+    MWG_CUDA(cudaGetLastError());
+}
+
+void k_apply_tc05(const DevBasis &b, const ApplyLaunch &L, cudaStream_t s) {
+    if (L.nnodes <= 0) return;
+    MWG_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(int), s));
+    MWG_CUDA(cudaMemsetAsync(L.status, 0, sizeof(int), s));
+    switch (b.K) {
+        case 4: launch_tc05<4>(L, s); break;
+        case 5: launch_tc05<5>(L, s); break;
+        case 6: launch_tc05<6>(L, s); break;
+        case 7: launch_tc05<7>(L, s); break;
+        case 8: launch_tc05<8>(L, s); break;
+        case 9: launch_tc05<9>(L, s); break;
+        case 10: launch_tc05<10>(L, s); break;
+        default: throw Error(MW_ERR_ARG, "no tensor-core apply kernel for this order");
+    }
+}
+
+}  // namespace mwg

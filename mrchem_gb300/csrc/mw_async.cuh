@@ -43,12 +43,14 @@ __device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t b
 // wait of the CTA returns at once, so the kernel still ends with all threads on the same path.
 constexpr int TMA_WAIT_LIMIT = 1 << 20;
 
-__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, volatile int *fail, int *status) {
+// `code` (non-zero) is what the status word receives: it tells which wait of the kernel ran out.
+__device__ __forceinline__ void mbar_wait(uint64_t *bar, uint32_t parity, volatile int *fail, int *status,
+                                          int code = 1) {
     if (*fail) return;
     for (int it = 0; it < TMA_WAIT_LIMIT; it++)
         if (mbar_try_wait(bar, parity)) return;
     *fail = 1;
-    atomicExch(status, 1);
+    atomicExch(status, code);
 }
 
 }  // namespace

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "mw_host.h"
+#include "mw_tc05_layout.h"
 
 namespace mwg {
 
@@ -433,6 +434,28 @@ void Oper::build(const Basis &b) {
     MWG_CUDA(cudaMalloc(&d_blocks32, sizeof(float) * 2 * nel));
     MWG_CUDA(cudaMemcpy(d_blocks, blocks.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
     MWG_CUDA(cudaMemcpy(d_blocks32, b32.data(), sizeof(float) * 2 * nel, cudaMemcpyHostToDevice));
+    // the tensor-core tier's B operand of every block (mw_tc05_layout.h): k-groups of 4 columns,
+    // rows n < 2K = A[n][k], rows 2K + i (i < K) = A[i][k] for k >= K (zero for k < K), TF32
+    if (K >= 4 && K <= KMAX) {
+        const int N2 = 2 * K, NB = tc5_n(K);
+        const size_t per = tc5_b_floats(K), nb = nel / (size_t)bsz;
+        std::vector<float> tc(per * nb, 0.0f);
+        for (size_t blk = 0; blk < nb; blk++) {
+            const float *h = &b32[2 * blk * bsz];
+            float *o = &tc[blk * per];
+            for (int n = 0; n < NB; n++)
+                for (int k = 0; k < N2; k++) {
+                    float v = 0.0f;
+                    if (n < N2)
+                        v = h[n * N2 + k];
+                    else if (n < N2 + K && k >= K)
+                        v = h[(n - N2) * N2 + k];
+                    o[((size_t)(k / 4) * NB + n) * 4 + (k % 4)] = tf32_round_host(v);
+                }
+        }
+        MWG_CUDA(cudaMalloc(&d_blocks_tc, sizeof(float) * tc.size()));
+        MWG_CUDA(cudaMemcpy(d_blocks_tc, tc.data(), sizeof(float) * tc.size(), cudaMemcpyHostToDevice));
+    }
 }
 
 }  // namespace mwg

@@ -398,6 +398,7 @@ int mw_op_destroy(mw_op o) {
     cudaStreamSynchronize(o->op.ctx->stream);
     if (o->op.d_blocks) cudaFree(o->op.d_blocks);
     if (o->op.d_blocks32) cudaFree(o->op.d_blocks32);
+    if (o->op.d_blocks_tc) cudaFree(o->op.d_blocks_tc);
     mwg::Ctx *ctx = o->op.ctx;
     delete o;
     ctx_child_gone(ctx);

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <stdexcept>
 #include <string>
 #include <unordered_map>
@@ -94,7 +95,8 @@ struct Tree {
     double *d_coefs = nullptr;    // cap * bs
     double *d_cn = nullptr;       // cap * 8
     float *d_coefs32 = nullptr;   // FP32 shadow (mixed-precision applies): cap32 x (high cube, low cube)
-    size_t cap = 0, cap32 = 0;
+    float *d_coefs_tc = nullptr;  // TF32 x-pass operand of the tensor-core tier (mw_tc05_layout.h), cap_tc blocks
+    size_t cap = 0, cap32 = 0, cap_tc = 0;
     int nroots = 0;
 
     int find(int n, const int *l) const {
@@ -126,6 +128,7 @@ struct Oper {
     long nblocks = 0;
     double *d_blocks = nullptr;  // (2K)^2 per block, FP64
     float *d_blocks32 = nullptr; // FP32 copy: per block the high part, then the low part (2 x (2K)^2)
+    float *d_blocks_tc = nullptr; // TF32 B operand of the tensor-core tier per block (mw_tc05_layout.h)
     const double *norm(int t, int s, int l) const { return &norms[(size_t)(off[t * S + s] + l + band[t * S + s]) * 4]; }
     long block_index(int t, int s, int l) const { return off[t * S + s] + l + band[t * S + s]; }
     void build(const Basis &b);
@@ -259,6 +262,19 @@ inline size_t generate_scratch_doubles(int K) {
 void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s);
 // TF32 tensor-core tier: FP32 cube-order input blocks and FP32 operator blocks, as the FP32 tier
 void k_apply_tc(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s);
+// the same tier on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor memory)
+void k_apply_tc05(const DevBasis &b, const ApplyLaunch &L, cudaStream_t s);
+// FP32 cube-order shadows (high cube read) -> the tensor-core tier's x-pass operand layout
+void k_to_tc_x(const float *cube32, float *out, size_t nblocks, int K, cudaStream_t s);
+// round to TF32: nearest, ties away from zero (as cvt.rna.tf32.f32)
+inline float tf32_round_host(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & ~0x1fffu;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
 // double-FP32 tier: reads the high and low parts of the same shadows and operator blocks
 void k_apply_df(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s);
 void k_norms(const DevBasis &b, double *const *blocks, double *const *cn, int n, cudaStream_t s);

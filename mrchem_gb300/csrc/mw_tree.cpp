@@ -231,10 +231,12 @@ void Tree::free_device() {
     if (d_coefs) cudaFree(d_coefs);
     if (d_cn) cudaFree(d_cn);
     if (d_coefs32) cudaFree(d_coefs32);
+    if (d_coefs_tc) cudaFree(d_coefs_tc);
     d_coefs = nullptr;
     d_cn = nullptr;
     d_coefs32 = nullptr;
-    cap = cap32 = 0;
+    d_coefs_tc = nullptr;
+    cap = cap32 = cap_tc = 0;
 }
 
 void tree_zero(Tree &t, int first, int count) {
