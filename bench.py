@@ -315,12 +315,14 @@ def run(args):
     mra.set_overlap(True)
     fp64_tf = mra.probe_fma_peak(True)
     fp32_tf = mra.probe_fma_peak(False)
-    tf32_tf = mra.probe_mma_peak("tf32")
+    tf32_tf = mra.probe_mma_peak("tc05")          # tcgen05 TF32, M128 N256 K8: the device's dense rate
+    tf32_n32_tf = mra.probe_mma_peak("tc05_n32")  # the same at the tier's own MMA shape, N = 32
+    tf32_sync_tf = mra.probe_mma_peak("tf32")     # warp-level mma.sync m16n8k8 TF32, for comparison
 
     # DRAM read bytes per item of each tier kernel, from an ncu capture of the 4-orbital case of this
     # batch (dram__bytes_read.sum + dram__bytes_write.sum over all launches of one step / items);
     # traffic per step = that x the tier's items in this step
-    dram_per_item = {"fp32": 2.79e3, "tf32": 1.34e3, "df32": 10.1e3}
+    dram_per_item = {"fp32": 2.79e3, "tf32": 1.36e3, "df32": 10.1e3}
     tier_items = {"fp64": st_ser["items_fp64"], "fp32": st_ser["items_fp32"], "tf32": st_ser["items_tf32"],
                   "df32": st_ser["items_df"]}
 
@@ -333,17 +335,19 @@ def run(args):
                 "kernel": kernel, "kernel_ms_per_step": ms, "peak_source": source}
 
     fma_src = "probed FMA throughput of this GPU (mw_probe_fma_peak); MEASURED_PEAKS.json holds no FP64/FP32 figure"
-    mma_src = ("probed dense m16n8k8 TF32 warp-MMA throughput of this GPU (mw_probe_mma_peak); "
+    mma_src = ("probed dense tcgen05.mma TF32 throughput of this GPU at M128 N256 K8 (mw_probe_mma_peak kind 2); "
                "MEASURED_PEAKS.json holds no TF32 figure")
     roofs = {
         "fp64": roof(st_ser["flops_fp64"], st_ser["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
         "fp32": roof(st_ser["flops_fp32"], st_ser["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src, tier="fp32"),
-        "tf32": roof(st_ser["flops_tf32"], st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc_kernel<10>", "tensor", mma_src, tier="tf32"),
+        "tf32": roof(st_ser["flops_tf32"], st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc05_kernel<10>", "tensor", mma_src, tier="tf32"),
         # a double-FP32 multiply-add costs 12 FP32 instructions: peak = FP32 FMA peak * 2 / 24
         "df32": roof(st_ser["flops_df"], st_ser["kernel_ms_df"], fp32_tf / 12.0, "apply_df_kernel<10>",
                      "fp32-pipe (double-FP32)", fma_src + "; divided by 12 FP32 instructions per double-FP32 "
                      "multiply-add", tier="df32"),
     }
+    roofs["tf32"]["peak_tc05_n32"] = tf32_n32_tf
+    roofs["tf32"]["peak_mma_sync_tf32"] = tf32_sync_tf
     dominant = max(roofs, key=lambda k: roofs[k]["kernel_ms_per_step"])
     line = {
         "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": args.steps,

@@ -221,7 +221,9 @@ int mw_tree_load(mw_tree t, const char *path);
 /* measured FMA throughput of this GPU (TFLOP/s) in FP64 (fp64 = 1) or FP32 (fp64 = 0):
  * the denominator of the CUDA-core roofline of the contraction kernels */
 int mw_probe_fma_peak(mw_ctx ctx, int fp64, double *tflops);
-/* measured dense warp-MMA throughput (TFLOP/s): kind 0 = TF32 m16n8k8, kind 1 = BF16 m16n8k16 */
+/* measured dense tensor-core throughput (TFLOP/s): kind 0 = warp-level mma.sync TF32 m16n8k8,
+ * kind 1 = mma.sync BF16 m16n8k16, kind 2 = tcgen05.mma TF32 M128 N256 K8 (the device's dense TF32
+ * rate), kind 3 = tcgen05.mma TF32 M128 N32 K8 (the shape of the TF32 apply tier) */
 int mw_probe_mma_peak(mw_ctx ctx, int kind, double *tflops);
 
 #ifdef __cplusplus

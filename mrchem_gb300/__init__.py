@@ -228,9 +228,12 @@ class MultiResolutionAnalysis:
         return v.value
 
     def probe_mma_peak(self, kind="tf32"):
-        """Measured dense warp-MMA throughput in TFLOP/s ("tf32": m16n8k8, "bf16": m16n8k16)."""
+        """Measured dense tensor-core throughput in TFLOP/s: "tf32" / "bf16" = warp-level mma.sync
+        (m16n8k8 / m16n8k16), "tc05" = tcgen05.mma TF32 M128 N256 K8 (the dense TF32 rate),
+        "tc05_n32" = tcgen05.mma TF32 M128 N32 K8 (the TF32 apply tier's shape)."""
         v = C.c_double()
-        _check(_lib.mw_probe_mma_peak(self.ptr, {"tf32": 0, "bf16": 1}[kind], C.byref(v)), self.ptr)
+        code = {"tf32": 0, "bf16": 1, "tc05": 2, "tc05_n32": 3}[kind]
+        _check(_lib.mw_probe_mma_peak(self.ptr, code, C.byref(v)), self.ptr)
         return v.value
 
 

@@ -405,7 +405,77 @@ __global__ void to_tc_x_kernel(const float *cube32, float *out, size_t nblocks, 
     }
 }
 
+// throughput probe: one thread per CTA issues `iters` dense TF32 MMAs (M = 128, N = n, K = 8) on
+// zeroed operands into one TMEM accumulator, then waits (bounded) for their commit
+__global__ void __launch_bounds__(128) tc05_probe_kernel(int iters, int n, int *status) {
+    extern __shared__ __align__(1024) uint8_t smp[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t s_tmem;
+    __shared__ volatile int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int bytes_a = 128 * 32, bytes_b = n * 32;
+    for (int i = tid; i < (bytes_a + bytes_b) / 16; i += blockDim.x)
+        reinterpret_cast<float4 *>(smp)[i] = make_float4(0, 0, 0, 0);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_addr(&s_tmem)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        mbar_init(&bar);
+        s_fail = 0;
+    }
+    async_fence();
+    t5_before_sync();
+    __syncthreads();
+    t5_after_sync();
+    const uint32_t tmem = s_tmem;
+    if (tid == 0) {
+        const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | (8u << 24);
+        const uint64_t da = t5_desc(smem_addr(smp), 128, 256), db = t5_desc(smem_addr(smp + bytes_a), 128, 256);
+        for (int i = 0; i < iters; i++) t5_mma(tmem, da, db, idesc, i > 0 ? 1u : 0u);
+        t5_commit(&bar);
+        mbar_wait(&bar, 0, &s_fail, status);
+    }
+    t5_before_sync();
+    __syncthreads();
+    t5_after_sync();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+}
+
 }  // namespace
+
+// Dense tcgen05 TF32 throughput (TFLOP/s, 2 flops per MAC) for MMAs of shape M = 128, N = n, K = 8.
+double probe_tc05_tflops(int n, int nsm, cudaStream_t s) {
+    if (n < 16 || n > 256 || n % 16) throw Error(MW_ERR_ARG, "probe: N must be a multiple of 16 in [16, 256]");
+    // at most two CTAs per SM (512 TMEM columns): the shared memory asked for keeps a third out
+    const int blocks = 2 * nsm, iters = 1 << 12, smem = 80 * 1024;
+    MWG_CUDA(cudaFuncSetAttribute(tc05_probe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int *status = nullptr;
+    MWG_CUDA(cudaMalloc(&status, sizeof(int)));
+    MWG_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+    cudaEvent_t e0, e1;
+    MWG_CUDA(cudaEventCreate(&e0));
+    MWG_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        MWG_CUDA(cudaEventRecord(e0, s));
+        tc05_probe_kernel<<<blocks, 128, smem, s>>>(iters, n, status);
+        MWG_CUDA(cudaGetLastError());
+        MWG_CUDA(cudaEventRecord(e1, s));
+        MWG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        MWG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0 && ms < best) best = ms;
+    }
+    int hs = 0;
+    MWG_CUDA(cudaMemcpy(&hs, status, sizeof(int), cudaMemcpyDeviceToHost));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(status);
+    if (hs) throw Error(MW_ERR_TIMEOUT, "probe: a bounded wait for the MMAs ran out");
+    const double flops = 2.0 * 128.0 * n * 8.0 * (double)iters * blocks;
+    return flops / (best * 1e-3) / 1e12;
+}
 
 void k_to_tc_x(const float *cube32, float *out, size_t nblocks, int K, cudaStream_t s) {
     if (nblocks == 0) return;

@@ -617,7 +617,7 @@ int mw_tree_load(mw_tree t, const char *path) {
 }
 
 int mw_probe_mma_peak(mw_ctx c, int kind, double *tflops) {
-    if (!c || !tflops || kind < 0 || kind > 1) return MW_ERR_ARG;
+    if (!c || !tflops || kind < 0 || kind > 3) return MW_ERR_ARG;
     return guard(&c->ctx, [&] { *tflops = mwg::probe_mma_tflops(kind, c->ctx.nsm, c->ctx.stream); });
 }
 

@@ -260,9 +260,8 @@ inline size_t generate_scratch_doubles(int K) {
     return (size_t)4 * K * K * K + (size_t)2 * K * K * K + (size_t)K * K * K;
 }
 void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s);
-// TF32 tensor-core tier: FP32 cube-order input blocks and FP32 operator blocks, as the FP32 tier
-void k_apply_tc(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s);
-// the same tier on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor memory)
+// TF32 tensor-core tier on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
+// memory); items point at the operand layouts of mw_tc05_layout.h
 void k_apply_tc05(const DevBasis &b, const ApplyLaunch &L, cudaStream_t s);
 // FP32 cube-order shadows (high cube read) -> the tensor-core tier's x-pass operand layout
 void k_to_tc_x(const float *cube32, float *out, size_t nblocks, int K, cudaStream_t s);
@@ -307,6 +306,7 @@ void k_permute_blocks(double *dst, const double *src, const int *map, int n, int
 bool host_is_pinned(const void *p);
 double probe_fma_tflops(int fp64, int nsm, cudaStream_t s);
 double probe_mma_tflops(int kind, int nsm, cudaStream_t s);
+double probe_tc05_tflops(int n, int nsm, cudaStream_t s);
 void k_eval(const DevBasis &b, const double *const *blocks, const int *keys, const double *pts, int npts,
             double *out, cudaStream_t s);
 

@@ -965,6 +965,8 @@ __global__ void mma_probe_kernel(float *out, int iters, int kind) {
 
 // Dense warp-MMA throughput (TFLOP/s, 2 flops per MAC) of the legacy mma.sync path.
 double probe_mma_tflops(int kind, int nsm, cudaStream_t s) {
+    if (kind == 2) return probe_tc05_tflops(256, nsm, s);
+    if (kind == 3) return probe_tc05_tflops(32, nsm, s);
     const int threads = 256, blocks = nsm * 8, iters = 1 << 12;
     float *out = nullptr;
     MWG_CUDA(cudaMalloc(&out, sizeof(float) * blocks));
