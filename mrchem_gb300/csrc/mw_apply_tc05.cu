@@ -87,7 +87,8 @@ struct T5Geo {
     static constexpr int SMEM = OB + 6 * BSZ;
     static constexpr int TMEM_COLS = 2 * MT * N <= 32 ? 32 : (2 * MT * N <= 64 ? 64 : (2 * MT * N <= 128 ? 128 : 256));
     static constexpr uint32_t STAGE_BYTES = (uint32_t)(SX + 3 * BSZ);
-    static constexpr int THREADS = 256;
+    static constexpr int EPI_WARPS = 8;                 // warps that read TMEM and store operands
+    static constexpr int THREADS = 32 * EPI_WARPS + 32; // + one warp that issues copies and MMAs
     // dynamic shared memory requested at launch: at least enough that no more CTAs share an SM
     // than its 512 TMEM columns serve (an allocation beyond them would wait for another CTA)
     static constexpr int MAX_CTAS = 512 / TMEM_COLS;
@@ -131,9 +132,17 @@ __device__ __forceinline__ void t5_before_sync() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ void t5_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void async_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// 32 consecutive TMEM columns of this warp's 32 lanes: v[j] = column j of lane (row) base + lane
-__device__ __forceinline__ void t5_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
+// Loads of TMEM into registers.  tcgen05.ld is asynchronous: t5_ld* only start a load of 32
+// (N = 32) or 16 (N = 16) consecutive columns of this warp's 32 lanes (r[j] = column j of lane
+// base + lane); t5_wait ends every load of the thread and takes the registers of the load as
+// in-out operands, so that no use of them is scheduled before it.
+#define T5_R32(r)                                                                                          \
+    "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), \
+        "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]),   \
+        "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]),  \
+        "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+
+__device__ __forceinline__ void t5_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%"
         "19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -142,37 +151,47 @@ __device__ __forceinline__ void t5_ld32(uint32_t taddr, float (&v)[32]) {
           "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
           "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ void t5_ld16(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[16];
+__device__ __forceinline__ void t5_ld16(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
-#pragma unroll
-    for (int j = 16; j < 32; j++) v[j] = 0.0f;
+    for (int j = 16; j < 32; j++) r[j] = 0u;
 }
 
 template <int K>
-__device__ __forceinline__ void t5_ld(uint32_t taddr, float (&v)[32]) {
+__device__ __forceinline__ void t5_ld(uint32_t taddr, uint32_t (&r)[32]) {
     if (T5Geo<K>::N == 32)
-        t5_ld32(taddr, v);
+        t5_ld32(taddr, r);
     else
-        t5_ld16(taddr, v);
+        t5_ld16(taddr, r);
 }
+
+__device__ __forceinline__ void t5_wait(uint32_t (&r)[32]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" : T5_R32(r) : : "memory");
+}
+
 
 // element (row r, column k) of region R (k-group stride LBO_R, 16 bytes per row)
 template <int K>
 __device__ __forceinline__ float *r_at(uint8_t *R, int r, int k) {
     return reinterpret_cast<float *>(R + (k >> 2) * T5Geo<K>::LBO_R + 16 * r + 4 * (k & 3));
+}
+
+// the epilogue of one pass for the TMEM tiles of this warp (tiles half, half + 2, ... < tiles)
+template <int K, class Row>
+__device__ __forceinline__ void t5_epilogue(uint32_t tcol, int tiles, int q, int half, int lane, Row row) {
+    constexpr int N = T5Geo<K>::N;
+    for (int i = half; i < tiles; i += 2) {
+        uint32_t a[32];
+        t5_ld<K>(tcol + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * N), a);
+        t5_wait(a);
+        row(i * 128 + 32 * q + lane, a);
+    }
 }
 
 template <int K>
@@ -181,12 +200,15 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
     constexpr int N2 = G::N2, NN = G::NN, KK = G::KK, K3 = G::K3, N = G::N;
     extern __shared__ __align__(1024) uint8_t smem5[];
     uint8_t *sS = smem5, *sR = smem5 + G::OR, *sB = smem5 + G::OB;
-    __shared__ __align__(8) uint64_t bar[4];  // 0 staging copies, 1 x MMAs, 2 y MMAs, 3 end of a node
+    // barriers: 0 staging copies, 1 x MMAs, 2 y MMAs, 3 end of a node, 4 draining after a failed wait
+    __shared__ __align__(8) uint64_t bar[5];
     __shared__ uint32_t s_tmem;
     __shared__ int s_node;
     __shared__ volatile int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int q = warp & 3, half = warp >> 2;  // TMEM lane quarter, tile parity of this warp
+    const bool producer = warp == G::EPI_WARPS;  // copies and MMAs (lane 0)
+    const bool issuer = producer && lane == 0;
+    const int q = warp & 3, half = warp >> 2;  // epilogue warps: TMEM lane quarter, tile parity
     const bool excl = !L.root;
 
     // zero everything once: padding rows, columns and k-groups are read by the MMAs
@@ -197,7 +219,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int b = 0; b < 4; b++) mbar_init(&bar[b]);
+        for (int b = 0; b < 5; b++) mbar_init(&bar[b]);
         s_fail = 0;
     }
     async_fence();
@@ -210,11 +232,11 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
     // descriptors of the operands' first core matrices; a tile / k-step adds its byte offset >> 4
     const uint64_t dS = t5_desc(smem_addr(sS), G::LBO_S, 128), dR = t5_desc(smem_addr(sR), G::LBO_R, 128);
     const uint64_t dB = t5_desc(smem_addr(sB), G::LBO_B, 128);
-    uint32_t ph[4] = {0, 0, 0, 0};  // bar[0]'s parity is tracked by thread 0 alone
+    uint32_t ph = 0;     // bit b: the parity of barrier b's next phase (a thread tracks the ones it waits on)
     uint32_t nitem = 0;  // items this CTA has started: B set nitem & 1
 
     auto stage = [&](const void *in, const void *ax, const void *ay, const void *az, uint32_t set) {
-        if (s_fail) return;  // thread 0: the item's input block and B operands
+        if (s_fail) return;  // the issuing thread: the item's input block and B operands
         async_fence();
         mbar_expect_tx(&bar[0], G::STAGE_BYTES);
         uint8_t *B = sB + set * 3 * G::BSZ;
@@ -223,10 +245,11 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
         bulk_copy(B + G::BSZ, ay, G::BSZ, &bar[0]);
         bulk_copy(B + 2 * G::BSZ, az, G::BSZ, &bar[0]);
     };
-    // status on a wait that runs out: 1 + barrier + 4 * (parity) + 8 * (items this CTA had started)
+    // status on a wait that runs out: 1 + barrier + 8 * (parity) + 16 * (items this CTA had started)
     auto wait = [&](int b) {
-        mbar_wait(&bar[b], ph[b], &s_fail, L.status, 1 + b + 4 * (int)ph[b] + 8 * (int)(nitem < 65535u ? nitem : 65535u));
-        ph[b] ^= 1u;
+        const uint32_t p = (ph >> b) & 1u;
+        mbar_wait(&bar[b], p, &s_fail, L.status, 1 + b + 8 * (int)p + 16 * (int)(nitem < 65535u ? nitem : 65535u));
+        ph ^= 1u << b;
     };
     // all threads: the MMAs may read what was stored; the issuing thread then orders after the sync
     auto publish = [&]() {
@@ -235,7 +258,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
         __syncthreads();
         t5_after_sync();
     };
-    // thread 0: tiles x k-steps of one pass, then a commit to barrier b (none if b < 0)
+    // the issuing thread: tiles x k-steps of one pass, then a commit to barrier b (none if b < 0)
     auto issue_pass = [&](uint64_t da, int lbo_a, uint64_t db, int tiles, uint32_t dcol, bool accumulate, int b) {
         if (s_fail) return;
         for (int i = 0; i < tiles; i++)
@@ -252,124 +275,125 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
         const int w = s_node;
         if (w >= L.nnodes) break;
         const long long b0 = L.begin[w], b1 = L.end[w];
-        if (tid == 0 && b0 < b1) stage(L.in[b0], L.ax[b0], L.ay[b0], L.az[b0], nitem & 1u);
+        if (issuer && b0 < b1) stage(L.in[b0], L.ax[b0], L.ay[b0], L.az[b0], nitem & 1u);
         for (long long j = b0; j < b1; j++, nitem++) {
             const uint32_t set = nitem & 1u;
             const uint64_t dBs = dB + (uint64_t)((set * 3 * G::BSZ) >> 4);
-            const float cf = float(L.coef[j]);
-            // item j+1's pointers, read early (thread 0 copies its blocks after the x MMAs)
-            const bool more = j + 1 < b1;
-            const void *nin = nullptr, *nax = nullptr, *nay = nullptr, *naz = nullptr;
-            if (tid == 0 && more) {
-                nin = L.in[j + 1];
-                nax = L.ax[j + 1];
-                nay = L.ay[j + 1];
-                naz = L.az[j + 1];
-            }
-            if (tid == 0) {
-                wait(0);  // item j's input block and B operands are in S and B set `set`
-                issue_pass(dS, G::LBO_S, dBs, G::MTX, tD, false, 1);
-            }
-            wait(1);  // the x MMAs, and every earlier MMA (the previous item's z pass), are done
-            t5_after_sync();
-            if (tid == 0 && more) stage(nin, nax, nay, naz, set ^ 1u);
-            // ---- x epilogue: D row (Z, Y) -> A_y rows (X', Z) and extra rows (X' < K, Z < K), k = Y
-            for (int i = half; i < G::MTX; i += 2) {
-                float v[32];
-                t5_ld<K>(tD + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * N), v);
-                const int r = i * 128 + 32 * q + lane;
-                if (r < NN) {
+            if (producer) {
+                if (lane == 0) {
+                    const bool more = j + 1 < b1;
+                    const void *nin = nullptr, *nax = nullptr, *nay = nullptr, *naz = nullptr;
+                    if (more) {  // item j+1's pointers, read while item j's copies land
+                        nin = L.in[j + 1];
+                        nax = L.ax[j + 1];
+                        nay = L.ay[j + 1];
+                        naz = L.az[j + 1];
+                    }
+                    wait(0);  // item j's input block and B operands are in S and B set `set`
+                    issue_pass(dS, G::LBO_S, dBs, G::MTX, tD, false, 1);
+                    // the x MMAs, and every earlier MMA (the previous item's z pass), are done:
+                    // S and the other B set are free for item j+1
+                    wait(1);
+                    if (more) stage(nin, nax, nay, naz, set ^ 1u);
+                }
+                __syncwarp();
+            } else {
+                // ---- x epilogue: D row (Z, Y) -> A_y rows (X', Z) and extra rows (X' < K, Z < K), k = Y
+                wait(1);
+                t5_after_sync();
+                t5_epilogue<K>(tD, G::MTX, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
+                    if (r >= NN) return;
                     const int Z = r / N2, Y = r - Z * N2;
                     float *base = r_at<K>(sR, 0, Y);
 #pragma unroll
-                    for (int xp = 0; xp < N2; xp++) base[4 * (xp * N2 + Z)] = tf32r(v[xp]);
+                    for (int xp = 0; xp < N2; xp++) base[4 * (xp * N2 + Z)] = tf32r(__uint_as_float(v[xp]));
                     if (Z < K) {
 #pragma unroll
                         for (int xp = 0; xp < K; xp++)
-                            base[4 * (NN + xp * K + Z)] = tf32r(Y < K ? v[N2 + xp] : v[xp]);
+                            base[4 * (NN + xp * K + Z)] = tf32r(__uint_as_float(Y < K ? v[N2 + xp] : v[xp]));
                     }
-                }
+                });
             }
             publish();
-            if (tid == 0) issue_pass(dR, G::LBO_R, dBs + (uint64_t)(G::BSZ >> 4), G::MT, tD, false, 2);
-            wait(2);
-            t5_after_sync();
-            // ---- y epilogue: D row (X', Z) -> c * A_z rows (Y', X') with k = Z; extra rows (Y', X' < K)
-            for (int i = half; i < G::MT; i += 2) {
-                float v[32];
-                t5_ld<K>(tD + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * N), v);
-                const int r = i * 128 + 32 * q + lane;
-                if (r < NN) {
-                    const int xp = r / N2, Z = r - xp * N2;
-                    float *base = r_at<K>(sR, 0, Z);
+            if (issuer) issue_pass(dR, G::LBO_R, dBs + (uint64_t)(G::BSZ >> 4), G::MT, tD, false, 2);
+            if (!producer) {
+                // ---- y epilogue: D row (X', Z) -> c * A_z rows (Y', X') with k = Z; extra rows (Y', X' < K)
+                const float cf = float(L.coef[j]);
+                wait(2);
+                t5_after_sync();
+                t5_epilogue<K>(tD, G::MT, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
+                    if (r < NN) {
+                        const int xp = r / N2, Z = r - xp * N2;
+                        float *base = r_at<K>(sR, 0, Z);
 #pragma unroll
-                    for (int yp = 0; yp < N2; yp++) base[4 * (yp * N2 + xp)] = tf32r(cf * v[yp]);
-                    if (Z >= K && xp < K) {
+                        for (int yp = 0; yp < N2; yp++) base[4 * (yp * N2 + xp)] = tf32r(cf * __uint_as_float(v[yp]));
+                        if (Z >= K && xp < K) {
 #pragma unroll
-                        for (int yp = 0; yp < K; yp++) base[4 * (NN + yp * K + xp)] = tf32r(cf * v[yp]);
+                            for (int yp = 0; yp < K; yp++)
+                                base[4 * (NN + yp * K + xp)] = tf32r(cf * __uint_as_float(v[yp]));
+                        }
+                    } else if (r < G::RE) {
+                        const int e = r - NN, xp = e / K, Z = e - xp * K;
+                        float *base = r_at<K>(sR, 0, Z);
+#pragma unroll
+                        for (int yp = 0; yp < K; yp++) base[4 * (NN + yp * K + xp)] = tf32r(cf * __uint_as_float(v[yp]));
                     }
-                } else if (r < G::RE) {
-                    const int e = r - NN, xp = e / K, Z = e - xp * K;
-                    float *base = r_at<K>(sR, 0, Z);
-#pragma unroll
-                    for (int yp = 0; yp < K; yp++) base[4 * (NN + yp * K + xp)] = tf32r(cf * v[yp]);
-                }
+                });
             }
             publish();
-            if (tid == 0) issue_pass(dR, G::LBO_R, dBs + (uint64_t)((2 * G::BSZ) >> 4), G::MT, tACC, j != b0, -1);
+            if (issuer) issue_pass(dR, G::LBO_R, dBs + (uint64_t)((2 * G::BSZ) >> 4), G::MT, tACC, j != b0, -1);
         }
         // ---- node epilogue: accumulator rows (Y', X'), columns Z' -> component-major FP64 block
-        if (b0 < b1) {
-            if (tid == 0 && !s_fail) t5_commit(&bar[3]);
-            wait(3);
-        }
-        t5_after_sync();
-        double *out = L.out[w];
-        for (int i = half; i < G::MT; i += 2) {
-            float v[32];
-            if (b0 < b1) {
-                t5_ld<K>(tACC + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * N), v);
-            } else {
-#pragma unroll
-                for (int c = 0; c < 32; c++) v[c] = 0.0f;
-            }
-            const int r = i * 128 + 32 * q + lane;
-            int yp = -1, xp = 0, zmax = 0, zmin = 0;
-            if (r < NN) {
-                yp = r / N2;
-                xp = r - yp * N2;
-                zmax = N2;
-                zmin = (excl && yp < K && xp < K) ? K : 0;  // Z' < K from the extra row
-            } else if (r < G::RE && excl) {
-                const int e = r - NN;
-                yp = e / K;
-                xp = e - yp * K;
-                zmax = K;
-            }
-            if (yp >= 0) {
+        if (b0 < b1 && issuer && !s_fail) t5_commit(&bar[3]);
+        if (!producer) {
+            if (b0 < b1) wait(3);
+            t5_after_sync();
+            double *out = L.out[w];
+            auto row = [&](int r, const uint32_t (&v)[32]) {
+                int yp = -1, xp = 0, zmax = 0, zmin = 0;
+                if (r < NN) {
+                    yp = r / N2;
+                    xp = r - yp * N2;
+                    zmax = N2;
+                    zmin = (excl && yp < K && xp < K) ? K : 0;  // Z' < K from the extra row
+                } else if (r < G::RE && excl) {
+                    const int e = r - NN;
+                    yp = e / K;
+                    xp = e - yp * K;
+                    zmax = K;
+                }
+                if (yp < 0) return;
                 const int cxy = (xp >= K ? 1 : 0) | (yp >= K ? 2 : 0);
                 const int off = (yp % K) * K + (xp % K);
 #pragma unroll
                 for (int zp = 0; zp < N2; zp++) {
                     if (zp < zmin || zp >= zmax) continue;
                     const int gi = (cxy | (zp >= K ? 4 : 0)) * K3 + (zp % K) * KK + off;
+                    const double val = b0 < b1 ? double(__uint_as_float(v[zp])) : 0.0;
                     if (L.set)
-                        out[gi] = double(v[zp]);
+                        out[gi] = val;
                     else
-                        out[gi] += double(v[zp]);
+                        out[gi] += val;
                 }
+            };
+            if (b0 < b1) {
+                t5_epilogue<K>(tACC, G::MT, q, half, lane, row);
+            } else {
+                uint32_t zero[32] = {};
+                for (int i = half; i < G::MT; i += 2) row(i * 128 + 32 * q + lane, zero);
             }
         }
         t5_before_sync();
         __syncthreads();
         t5_after_sync();
     }
-    if (s_fail && tid == 0) {
+    if (s_fail && issuer) {
         // a wait ran out: let whatever this CTA still has in flight end (bounded) before TMEM is freed
-        t5_commit(&bar[3]);
-        for (int b = 0; b < 4; b++)
-            for (int it = 0; it < TMA_WAIT_LIMIT; it++)
-                if (mbar_try_wait(&bar[b], ph[b])) break;
+        t5_commit(&bar[4]);
+        for (int it = 0; it < TMA_WAIT_LIMIT; it++)
+            if (mbar_try_wait(&bar[4], 0)) break;
+        for (int it = 0; it < TMA_WAIT_LIMIT; it++)
+            if (mbar_try_wait(&bar[0], ph & 1u)) break;
     }
     t5_before_sync();
     __syncthreads();
