@@ -254,6 +254,10 @@ def run(args):
     f32_ms, st_f32 = timed("mixed-fp32", 1)
     f32_err = max(rel_err(o, r) for o, r in zip(outs, ref))
 
+    # launch settings (job groups, chunk sizes) picked for this batch by the autotuner; the timed
+    # mixed steps below use them
+    tuned = (mw.autotune_batch([PREC] * NORB, outs, ops, phis, abs_prec=True, precision="mixed", repeats=5)
+             if args.autotune else None)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stats = []
     # the sampler starts before the warm-up steps (nvidia-smi takes a while to print its first
@@ -354,6 +358,7 @@ def run(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64+df32+f32+tf32", "data": "synthetic",
         "config": {"workload": "helmholtz-batch16-k9-prec1e-6", "orbitals": NORB, "order": ORDER, "prec": PREC,
+                   "tuned": tuned,
                    "basis": "interpolating", "box": "[-32,32]^3", "input_nodes": in_nodes,
                    "output_nodes": nodes, "l2": "inputs larger than L2 (%.1f GB of FP64 blocks)"
                    % (sum(in_nodes) * 8 * (ORDER + 1) ** 3 * 8 / 1e9),
@@ -404,6 +409,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-levels", type=int, default=-1)
+    ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
+                    help="pick the batch's launch settings with mw_apply_batch_autotune before timing")
     ap.add_argument("--cpu-s", type=float, default=12.0,
                     help="seconds of oracle apply time for the cpu_baseline sample")
     ap.add_argument("--ref-step-s", type=float, default=4.0,

@@ -112,6 +112,8 @@ int mw_ctx_synchronize(mw_ctx ctx);
  * mw_stats are exclusive.  Results are bit-identical either way.  No counterpart in the reference
  * (its applies are one per call). */
 int mw_ctx_set_overlap(mw_ctx ctx, int on);
+/* The number of job groups (1..8) batched applies split into; mw_ctx_set_overlap sets 4 or 1. */
+int mw_ctx_set_groups(mw_ctx ctx, int n);
 
 /* ---- trees (replaces FunctionTree<3>, src/qmfunctions/Orbital.h:51) ---- */
 int mw_tree_create(mw_ctx ctx, mw_tree *out);
@@ -185,6 +187,15 @@ int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const m
 int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *nprec,
                    const mw_tree *prec_trees, int max_iter, int abs_prec, int precision_mode);
 /* apply on a fixed output grid (the output's current grid, no refinement) */
+/* Autotuner of the batched apply's launch settings (no counterpart in the reference): runs the
+ * batch (as mw_apply_batch with no precision trees and max_iter = -1) `repeats` times for each
+ * candidate -- job groups 2..6, then the chunk size of the TF32, FP32 and double-FP32 tiers, one
+ * at a time -- and keeps the fastest (a candidate must beat the kept settings by 2%) in the context for this (order, n, precision_mode); later
+ * batched applies with the same key use it.  The outputs hold the result of a last run with the
+ * settings kept.  Returns the settings (groups, chunks[4] for FP64, FP32, TF32, double-FP32) and
+ * their median wall time in ms.  Needs job-group overlap on (mw_ctx_set_overlap). */
+int mw_apply_batch_autotune(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, int abs_prec,
+                            int precision_mode, int repeats, int *groups, long long *chunks, double *ms);
 int mw_apply_fixed(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec, int precision_mode);
 /* L2-adjoint of the fixed-grid FP64 apply y = A x (output grid = seed's grid, absolute precision):
  * out <- A^T seed on x's grid, with the forward's item set (screened with x's norms).  Transposed

@@ -74,7 +74,7 @@ EXPORTS = [
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
     "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
-    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap",
+    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap", "mw_ctx_set_groups", "mw_apply_batch_autotune",
     "mw_tree_upload_batch", "mw_tree_download_batch", "mw_pin_host", "mw_unpin_host",
 ]
 
@@ -97,6 +97,7 @@ def load_library(path=None):
         "mw_ctx_last_stats": [P, C.POINTER(Stats)],
         "mw_ctx_synchronize": [P],
         "mw_ctx_set_overlap": [P, I],
+        "mw_ctx_set_groups": [P, I],
         "mw_tree_create": [P, pp],
         "mw_tree_destroy": [P],
         "mw_tree_nnodes": [P, ip],
@@ -130,6 +131,7 @@ def load_library(path=None):
         "mw_op_block": [P, I, I, I, dp, dp],
         "mw_apply": [D, P, P, P, I, pp, I, I, I],
         "mw_apply_batch": [I, dp, pp, pp, pp, ip, pp, I, I, I],
+        "mw_apply_batch_autotune": [I, dp, pp, pp, pp, I, I, I, ip, C.POINTER(C.c_longlong), dp],
         "mw_multiply_batch": [I, dp, pp, dp, pp, pp, I, I, I],
         "mw_apply_fixed": [D, P, P, P, I, I],
         "mw_apply_adjoint": [D, P, P, P, P, I],
@@ -220,6 +222,10 @@ class MultiResolutionAnalysis:
     def set_overlap(self, on=True):
         """Pipelined job groups in batched applies (default on); off gives exclusive kernel times."""
         _check(_lib.mw_ctx_set_overlap(self.ptr, int(bool(on))), self.ptr)
+
+    def set_groups(self, n):
+        """Number of pipelined job groups (1..8) that batched applies split into (default 4)."""
+        _check(_lib.mw_ctx_set_groups(self.ptr, int(n)), self.ptr)
 
     def probe_fma_peak(self, fp64=True):
         """Measured FMA throughput of this GPU in TFLOP/s (FP64 or FP32 CUDA cores)."""
@@ -483,6 +489,21 @@ def apply_batch(precs, outs, opers, inps, prec_trees=None, max_iter=-1, abs_prec
                                _ip(npr) if npr is not None else None, _ptrs(flat), max_iter, int(abs_prec),
                                _PREC[precision]), outs[0].mra.ptr)
     return outs[0].mra.last_stats()
+
+
+def autotune_batch(precs, outs, opers, inps, abs_prec=False, precision="mixed", repeats=3):
+    """Pick the batched apply's launch settings for this batch shape by timing it (job groups 2..6,
+    then the chunk size of each reduced tier); later apply_batch calls with the same order, batch
+    size and precision use them.  Leaves the batch's result in outs.  Returns the settings."""
+    n = len(outs)
+    p = np.ascontiguousarray(precs if np.ndim(precs) else [precs] * n, dtype=np.float64)
+    g = np.zeros(1, dtype=np.int32)
+    ch = (C.c_longlong * 4)()
+    ms = np.zeros(1, dtype=np.float64)
+    _check(_lib.mw_apply_batch_autotune(n, _dp(p), _ptrs(outs), _ptrs(opers), _ptrs(inps), int(abs_prec),
+                                        _PREC[precision], int(repeats), _ip(g), ch, _dp(ms)), outs[0].mra.ptr)
+    return {"groups": int(g[0]), "chunk": {"fp64": ch[0], "fp32": ch[1], "tf32": ch[2], "df32": ch[3]},
+            "ms": float(ms[0])}
 
 
 def multiply_batch(precs, outs, coefs, as_, bs_, max_iter=-1, abs_prec=False, use_max_norms=False):

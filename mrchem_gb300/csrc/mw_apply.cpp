@@ -272,17 +272,18 @@ struct LevelItems {
 
 // tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores, 3 double-FP32.  Returns the pinned host copy of the
 // launch's status word (read it after the stream has been synchronised), or nullptr.
-int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, int tier, mw_stats &st) {
+int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, int tier, long long chunk,
+                 mw_stats &st) {
     const int nn = (int)li.nodes;
     const size_t ni = (size_t)li.items;
     if (nn == 0) return nullptr;
     // A node with many items runs as several chunks of about CHUNK items, each a CTA task that
     // writes a partial block; a second kernel sums every such node's partials in chunk order.
     // The split depends only on the tier and the node's own item count, so results do not depend
-    // on which nodes share the launch.  CHUNK is about half a millisecond of one CTA's work:
-    // an item costs ~200 us (FP64), ~20 us (FP32), ~6 us (TF32) and ~70 us (double-FP32).
-    static constexpr long long CHUNKS[4] = {4, 32, 96, 8};
-    const long long CHUNK = CHUNKS[tier];
+    // on which nodes share the launch.  CHUNK (Ctx::Tuning; by default 4, 32, 96 and 8 items) is
+    // about half a millisecond of one CTA's work: an item costs ~200 us (FP64), ~20 us (FP32),
+    // ~3 us (TF32) and ~70 us (double-FP32).
+    const long long CHUNK = chunk > 0 ? chunk : 1;
     const int bs = ctx.basis.bs;
     std::vector<double *> vout;
     std::vector<long long> vbeg, vend;
@@ -468,7 +469,14 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         StreamSwap(Ctx &c_, cudaStream_t s) : c(c_), saved(c_.stream) { c.stream = s; }
         ~StreamSwap() { c.stream = saved; }
     };
-    const int ngroups = std::max(1, std::min<int>(ctx.groups, (int)jobs.size()));
+    // launch settings: the autotuner's for this (order, jobs, mode) if it ran, else the context's
+    Ctx::Tuning tune;
+    tune.groups = ctx.groups;
+    {
+        auto it = ctx.tuned.find(std::make_tuple(b.K, (int)jobs.size(), precision_mode));
+        if (it != ctx.tuned.end() && ctx.groups > 1) tune = it->second;
+    }
+    const int ngroups = std::max(1, std::min<int>(tune.groups, (int)jobs.size()));
     std::vector<Group> groups(ngroups);
     {
         // balance the groups by input size, largest jobs first into the lightest group
@@ -746,7 +754,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         MWG_CUDA(cudaEventRecord(G.ev[0], ctx.stream));
         G.status.clear();
         for (int k = 0; k < NTIER; k++) {
-            int *hs = launch_tier(ctx, ar, lt[k], root, false, k, st);
+            int *hs = launch_tier(ctx, ar, lt[k], root, false, k, tune.chunk[k], st);
             if (hs) G.status.push_back(hs);
             MWG_CUDA(cudaEventRecord(G.ev[k + 1], ctx.stream));
         }
@@ -1219,7 +1227,7 @@ void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats 
         st.items += (long long)items.size();
         st.items_fp64 += (long long)items.size();
         st.out_nodes += (long long)li.out.size();
-        launch_tier(ctx, ctx.arena, li, root, true, 0, st);
+        launch_tier(ctx, ctx.arena, li, root, true, 0, Ctx::Tuning().chunk[0], st);
         ctx.sync();
         st.levels++;
     }

@@ -2,8 +2,11 @@
 // Every entry catches errors and returns a status; the message is kept on the
 // context for mw_last_error().  Nothing here falls back to host arithmetic:
 // without a usable CUDA device the calls fail with MW_ERR_CUDA.
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "mw_internal.h"
 
@@ -163,7 +166,13 @@ int mw_ctx_synchronize(mw_ctx c) {
 
 int mw_ctx_set_overlap(mw_ctx c, int on) {
     if (!c || (on != 0 && on != 1)) return MW_ERR_ARG;
-    c->ctx.groups = on ? mwg::Ctx::XGROUPS + 1 : 1;
+    c->ctx.groups = on ? mwg::Ctx::DEFAULT_GROUPS : 1;
+    return MW_OK;
+}
+
+int mw_ctx_set_groups(mw_ctx c, int n) {
+    if (!c || n < 1 || n > mwg::Ctx::XGROUPS + 1) return MW_ERR_ARG;
+    c->ctx.groups = n;
     return MW_OK;
 }
 
@@ -294,7 +303,8 @@ int mw_tree_eval(mw_tree t, int npts, const double *xyz, double *out) {
 
 int mw_tree_clear(mw_tree t) {
     if (!t) return MW_ERR_ARG;
-    return guard(ctx_of(t), [&] { mwg::tree_clear(t->tree); t->tree.ctx->sync(); });
+    // the zeroing of the roots is queued on the context's stream, ahead of any later use
+    return guard(ctx_of(t), [&] { mwg::tree_clear(t->tree); });
 }
 
 int mw_project_gauss(double prec, mw_tree out, int nterms, const mw_gterm *terms, int abs_prec) {
@@ -486,6 +496,67 @@ int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tre
         mw_stats st{};
         mwg::apply_batch(jobs, precision_mode, false, st);
         ctx->last = st;
+    });
+}
+
+int mw_apply_batch_autotune(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, int abs_prec,
+                            int precision_mode, int repeats, int *groups, long long *chunks, double *ms) {
+    if (n < 1 || !precs || !outs || !ops || !inps || repeats < 1 || repeats > 20) return MW_ERR_ARG;
+    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_DF) return MW_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (!outs[i] || !ops[i] || !inps[i] || !(precs[i] > 0.0) || outs[i] == inps[i]) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(outs[0]);
+    return guard(ctx, [&] {
+        if (ctx->groups == 1) throw mwg::Error(MW_ERR_STATE, "autotune: job-group overlap is off");
+        std::vector<mwg::ApplyJob> jobs(n);
+        for (int i = 0; i < n; i++)
+            jobs[i] = mwg::ApplyJob{&outs[i]->tree, &ops[i]->op, &inps[i]->tree, precs[i], abs_prec != 0, -1, {}};
+        const auto key = std::make_tuple(ctx->basis.K, n, precision_mode);
+        mw_stats st{};
+        // median wall time of `repeats` complete batched applies with the settings t (each apply
+        // ends with the device synchronised and the outputs' norms on the host)
+        auto run = [&](const mwg::Ctx::Tuning &t, int reps) {
+            ctx->tuned[key] = t;
+            std::vector<double> v;
+            for (int r = 0; r < reps; r++) {
+                for (int i = 0; i < n; i++) mwg::tree_clear(outs[i]->tree);
+                ctx->sync();
+                const auto t0 = std::chrono::steady_clock::now();
+                st = mw_stats{};
+                mwg::apply_batch(jobs, precision_mode, false, st);
+                v.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+            }
+            std::sort(v.begin(), v.end());
+            return v[v.size() / 2];
+        };
+        mwg::Ctx::Tuning best;
+        best.groups = ctx->groups;
+        run(best, 1);  // warm-up: allocations, arenas, shadows
+        double bt = run(best, repeats);
+        // coordinate search: the job-group count, then each tier's chunk size.  A candidate replaces
+        // the settings kept only when it is faster by more than the run-to-run noise (2%).
+        const double margin = 0.98;
+        for (int g : {2, 3, 4, 5, 6}) {
+            mwg::Ctx::Tuning t = best;
+            t.groups = g;
+            const double x = run(t, repeats);
+            if (x < margin * bt) bt = x, best = t;
+        }
+        const long long cand[4][3] = {{4, 4, 4}, {16, 32, 64}, {48, 96, 192}, {4, 8, 16}};
+        for (int tier : {2, 1, 3})
+            for (long long c : cand[tier]) {
+                mwg::Ctx::Tuning t = best;
+                t.chunk[tier] = c;
+                const double x = run(t, repeats);
+                if (x < margin * bt) bt = x, best = t;
+            }
+        run(best, 1);  // the outputs, from the settings kept
+        ctx->tuned[key] = best;
+        ctx->last = st;
+        if (groups) *groups = best.groups;
+        if (chunks)
+            for (int k = 0; k < 4; k++) chunks[k] = best.chunk[k];
+        if (ms) *ms = bt;
     });
 }
 

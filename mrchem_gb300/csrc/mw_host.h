@@ -11,7 +11,9 @@
 
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <stdexcept>
+#include <tuple>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -167,10 +169,20 @@ struct Ctx {
     // extra streams and arenas: the batched apply splits its jobs into up to XGROUPS + 1 groups
     // (group 0 on `stream` / `arena`), so that the host prepares one group's level while the GPU
     // computes the others'
-    static constexpr int XGROUPS = 3;
+    static constexpr int XGROUPS = 7;
+    static constexpr int DEFAULT_GROUPS = 4;
     cudaStream_t xstream[XGROUPS] = {};
     Arena xarena[XGROUPS];
-    int groups = XGROUPS + 1;  // job groups of a batched apply (1: no overlap)
+    int groups = DEFAULT_GROUPS;  // job groups of a batched apply (1: no overlap)
+    // launch settings of a batched apply: job groups, and the largest number of items one CTA
+    // task takes per tier (FP64, FP32, TF32, double-FP32) before a node is split into chunks
+    struct Tuning {
+        int groups = DEFAULT_GROUPS;
+        long long chunk[4] = {4, 32, 96, 8};
+    };
+    // settings picked by the autotuner (mw_apply_batch_autotune) per (order K, jobs, precision
+    // mode); a batched apply with the same key uses them unless overlap is off (groups == 1)
+    std::map<std::tuple<int, int, int>, Tuning> tuned;
     // high-priority stream for the generation of missing input nodes, which the host waits for
     // in the middle of preparing a level; the contraction kernels run one CTA per task, so the
     // generation gets the next free slot instead of waiting for whole kernels of other groups

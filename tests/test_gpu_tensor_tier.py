@@ -98,3 +98,62 @@ def test_overlapped_groups_bit_identical_to_serial(engine):
     mra.set_overlap(True)
     for (k1, c1, l1), (k2, c2, l2) in zip(res[True], res[False]):
         assert np.array_equal(k1, k2) and np.array_equal(c1, c2) and np.array_equal(l1, l2)
+
+
+@pytest.mark.gpu
+def test_job_group_count_bit_identical(engine):
+    # the number of pipelined job groups (1..8) changes only the schedule, never a result
+    prec = 1e-5
+    mra = engine.MultiResolutionAnalysis(9)
+    rng = np.random.default_rng(12)
+    phis, ops = [], []
+    for i in range(6):
+        c = tuple(rng.uniform(-1.0, 1.0, 3))
+        f = engine.project(prec, engine.FunctionTree(mra), [(1.0, float(rng.uniform(1.0, 20.0)), c, (i % 3, 0, 1))],
+                           abs_prec=True)
+        phis.append(f)
+        ops.append(engine.HelmholtzOperator(mra, float(rng.uniform(0.5, 2.0)), prec))
+    res = {}
+    for g in (1, 2, 3, 4, 6, 8):
+        mra.set_groups(g)
+        outs = [engine.FunctionTree(mra) for _ in phis]
+        st = engine.apply_batch([prec] * 6, outs, ops, phis, abs_prec=True, precision="mixed")
+        assert st["items_tf32"] > 0
+        res[g] = [o.download() for o in outs]
+    mra.set_overlap(True)
+    for g in res:
+        for (k1, c1, l1), (k2, c2, l2) in zip(res[1], res[g]):
+            assert np.array_equal(k1, k2) and np.array_equal(c1, c2) and np.array_equal(l1, l2)
+    with pytest.raises(engine.MWError):
+        mra.set_groups(9)
+
+
+def test_autotune_batch(engine):
+    # the autotuner keeps one of its candidates, and the tuned apply agrees with the default one
+    prec = 1e-5
+    mra = engine.MultiResolutionAnalysis(9)
+    rng = np.random.default_rng(13)
+    phis, ops = [], []
+    for i in range(5):
+        c = tuple(rng.uniform(-1.0, 1.0, 3))
+        f = engine.project(prec, engine.FunctionTree(mra), [(1.0, float(rng.uniform(1.0, 20.0)), c, (i % 2, 1, 0))],
+                           abs_prec=True)
+        phis.append(f)
+        ops.append(engine.HelmholtzOperator(mra, float(rng.uniform(0.5, 2.0)), prec))
+    ref = [engine.FunctionTree(mra) for _ in phis]
+    engine.apply_batch([prec] * 5, ref, ops, phis, abs_prec=True, precision="mixed")
+    outs = [engine.FunctionTree(mra) for _ in phis]
+    t = engine.autotune_batch([prec] * 5, outs, ops, phis, abs_prec=True, precision="mixed", repeats=1)
+    assert 2 <= t["groups"] <= 6 and t["ms"] > 0.0
+    assert t["chunk"]["tf32"] in (48, 96, 192) and t["chunk"]["fp32"] in (16, 32, 64) and t["chunk"]["df32"] in (4, 8, 16)
+    tuned = [engine.FunctionTree(mra) for _ in phis]
+    engine.apply_batch([prec] * 5, tuned, ops, phis, abs_prec=True, precision="mixed")
+    for a, b, r in zip(outs, tuned, ref):
+        for x in (a, b):
+            d = engine.FunctionTree(mra)
+            engine.add(-1.0, d, [(1.0, x), (-1.0, r)])
+            assert d.norm() <= 1e-7 * r.norm()
+    mra.set_overlap(False)
+    with pytest.raises(engine.MWError):
+        engine.autotune_batch([prec] * 5, outs, ops, phis, abs_prec=True, precision="mixed", repeats=1)
+    mra.set_overlap(True)
