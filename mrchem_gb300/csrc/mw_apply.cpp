@@ -278,7 +278,8 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     const size_t ni = (size_t)li.items;
     if (nn == 0) return nullptr;
     // A node with many items runs as several chunks of about CHUNK items, each a CTA task that
-    // writes a partial block; a second kernel sums every such node's partials in chunk order.
+    // writes a partial block; the CTA that ends a node's last chunk sums its partials in chunk
+    // order (mw_chunks.cuh).
     // The split depends only on the tier and the node's own item count, so results do not depend
     // on which nodes share the launch.  CHUNK (Ctx::Tuning; by default 4, 32, 96 and 8 items) is
     // about half a millisecond of one CTA's work: an item costs ~200 us (FP64), ~20 us (FP32),
@@ -287,6 +288,7 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     const int bs = ctx.basis.bs;
     std::vector<double *> vout;
     std::vector<long long> vbeg, vend;
+    std::vector<int> vred;  // per task: its node's ReduceTask, or -1
     std::vector<ReduceTask> red;
     long nsplit = 0;
     for (int i = 0; i < nn; i++) {
@@ -303,14 +305,16 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
             vout.push_back(li.out[i]);
             vbeg.push_back(b0);
             vend.push_back(b0 + m);
+            vred.push_back(-1);
             continue;
         }
-        red.push_back(ReduceTask{li.out[i], scratch + (size_t)used * bs, (int)pieces, set ? 1 : 0});
         for (long long k = 0; k < pieces; k++) {
             vout.push_back(scratch + (size_t)(used + k) * bs);
             vbeg.push_back(b0 + m * k / pieces);
             vend.push_back(b0 + m * (k + 1) / pieces);
+            vred.push_back((int)red.size());
         }
+        red.push_back(ReduceTask{li.out[i], scratch + (size_t)used * bs, (int)pieces, set ? 1 : 0});
         used += (long)pieces;
     }
     // tasks in decreasing item count (longest first) for the persistent grid's dynamic
@@ -322,10 +326,12 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
                      [&](int a, int b) { return vend[a] - vbeg[a] > vend[b] - vbeg[b]; });
     std::vector<double *> outp(nv);
     std::vector<long long> beg(nv), end(nv);
+    std::vector<int> redof(nv);
     for (int i = 0; i < nv; i++) {
         outp[i] = vout[ord[i]];
         beg[i] = vbeg[ord[i]];
         end[i] = vend[ord[i]];
+        redof[i] = vred[ord[i]];
     }
     Packer pk;
     pk.add(outp.data(), outp.size() * sizeof(double *));
@@ -337,8 +343,14 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     pk.add(li.az.data(), ni * sizeof(void *));
     pk.add(li.coef.data(), ni * sizeof(double));
     pk.add(red.data(), red.size() * sizeof(ReduceTask));
+    pk.add(redof.data(), redof.size() * sizeof(int));
     pk.ship(ctx, arena);
     int *counter = (int *)arena.alloc(2 * sizeof(int));
+    int *red_cnt = nullptr;
+    if (!red.empty()) {
+        red_cnt = (int *)arena.alloc(red.size() * sizeof(int));
+        MWG_CUDA(cudaMemsetAsync(red_cnt, 0, red.size() * sizeof(int), ctx.stream));
+    }
     ApplyLaunch L;
     L.nnodes = nv;
     L.root = root ? 1 : 0;
@@ -353,6 +365,11 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     L.coef = (const double *)pk.ptr(7);
     L.counter = counter;
     L.status = counter + 1;
+    if (!red.empty()) {
+        L.red = (const ReduceTask *)pk.ptr(8);
+        L.red_of = (const int *)pk.ptr(9);
+        L.red_cnt = red_cnt;
+    }
     st.launches++;
     int *hs = nullptr;
     if (tier == 3) {
@@ -367,10 +384,6 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
             *hs = 0;
             MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
         }
-    }
-    if (!red.empty()) {
-        k_reduce_partials((const ReduceTask *)pk.ptr(8), (int)red.size(), bs, ctx.stream);
-        st.launches++;
     }
     return hs;
 }

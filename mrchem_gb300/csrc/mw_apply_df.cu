@@ -21,6 +21,7 @@
 // thread per output column (Y', X')): the input cube, T1 and the node
 // accumulator as (hi, lo) float2 in shared memory, the operator rows of the
 // x and y passes in registers.
+#include "mw_chunks.cuh"
 #include "mw_host.h"
 
 namespace mwg {
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLau
     float2 *s_t2x = s_u + K3;      // t2x[Z][Y'][X'], Z, Y', X' < K
     float *s_Ah = reinterpret_cast<float *>(s_t2x + K3);  // A_x, A_y, A_z high parts
     float *s_Al = s_Ah + 3 * NC;                        // low parts
-    __shared__ int s_node;
+    __shared__ int s_node, s_redf;
     const int tid = threadIdx.x;
     const bool active = tid < NC;
     const int Yp = tid / N2, Xp = tid % N2;
@@ -220,6 +221,7 @@ __global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLau
             }
         }
         __syncthreads();
+        finish_chunk(L, w, 8 * K3, &s_redf);
     }
 }
 

@@ -55,6 +55,7 @@
 // Every wait on an mbarrier is bounded; one that runs out marks the launch failed (status word,
 // reported by the host as MW_ERR_TIMEOUT) and the kernel ends normally, freeing its TMEM.
 #include "mw_async.cuh"
+#include "mw_chunks.cuh"
 #include "mw_host.h"
 #include "mw_tc05_layout.h"
 
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
     // barriers: 0 staging copies, 1 x MMAs, 2 y MMAs, 3 end of a node, 4 draining after a failed wait
     __shared__ __align__(8) uint64_t bar[5];
     __shared__ uint32_t s_tmem;
-    __shared__ int s_node;
+    __shared__ int s_node, s_redf;
     __shared__ volatile int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const bool producer = warp == G::EPI_WARPS;  // copies and MMAs (lane 0)
@@ -386,6 +387,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
         t5_before_sync();
         __syncthreads();
         t5_after_sync();
+        finish_chunk(L, w, 8 * K3, &s_redf);
     }
     if (s_fail && issuer) {
         // a wait ran out: let whatever this CTA still has in flight end (bounded) before TMEM is freed

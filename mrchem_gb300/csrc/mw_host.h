@@ -231,6 +231,14 @@ struct ProjTask {
     int pad;
 };
 
+// a node whose items ran as several chunks: out (=|+=) the sum of its chunks' partial blocks, in order
+struct ReduceTask {
+    double *out;
+    const double *part;  // count consecutive partial blocks
+    int count;
+    int set;
+};
+
 struct ApplyLaunch {
     int nnodes;
     int root;                     // 1: include the (0,0) component pair
@@ -244,7 +252,13 @@ struct ApplyLaunch {
     const void *const *az;
     const double *coef;           // per item
     int *counter;                 // dynamic node counter (persistent grid)
-    int *status;                  // 0, or 1 when a bounded wait of the launch ran out (TF32 tier)
+    int *status;                  // 0, or non-zero when a bounded wait of the launch ran out (TF32 tier)
+    // chunked nodes: per task the index of its node's ReduceTask (-1: the task is a whole node),
+    // and per ReduceTask a counter of finished chunks (zero at launch).  The CTA that finishes a
+    // node's last chunk sums the partials into the node's block (mw_chunks.cuh).
+    const int *red_of = nullptr;
+    const ReduceTask *red = nullptr;
+    int *red_cnt = nullptr;
 };
 
 struct PairTask {  // parent -> children (8 consecutive blocks)
@@ -304,14 +318,6 @@ void k_to_fp32_cube(const double *in, float *out, size_t nblocks, int K, cudaStr
 void k_dot(const double *const *a, const double *const *b, const int *start, int n, int bs, double *partial,
            cudaStream_t s);
 void k_scale(double *x, size_t n, double c, cudaStream_t s);
-// a node whose items ran as several chunks: out (=|+=) the sum of its chunks' partial blocks, in order
-struct ReduceTask {
-    double *out;
-    const double *part;  // count consecutive partial blocks
-    int count;
-    int set;
-};
-void k_reduce_partials(const ReduceTask *tasks, int n, int bs, cudaStream_t s);
 // dst block j = src block map[j]; bs even
 void k_permute_blocks(double *dst, const double *src, const int *map, int n, int bs, cudaStream_t s);
 // true when the GPU's DMA engines can read / write the host buffer directly (pinned memory)

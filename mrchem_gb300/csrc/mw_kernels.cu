@@ -9,6 +9,7 @@
 
 #include <cstdint>
 
+#include "mw_chunks.cuh"
 #include "mw_host.h"
 
 namespace mwg {
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32) apply_kernel(App
     T *s_t1 = s_in + C;
     T *s_u = s_t1 + C;
     T *s_A = s_u + K3;
-    __shared__ int s_node;
+    __shared__ int s_node, s_redf;
     const int tid = threadIdx.x;
     const bool active = tid < NC;
     const int Yp = tid / N2, Xp = tid % N2;
@@ -406,6 +407,7 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32) apply_kernel(App
             }
         }
         __syncthreads();
+        finish_chunk(L, w, 8 * K3, &s_redf);
     }
 }
 
@@ -451,7 +453,7 @@ __global__ void __launch_bounds__(((2 * K * K + 31) / 32) * 32, 2) apply32_kerne
     float *s_acc = s_t1 + C;  // node accumulator acc[Z'][X'][Y']
     float *s_u = s_acc + C;   // u[Z][X'][Y], Z, X', Y < K
     float *s_A = s_u + U;
-    __shared__ int s_node;
+    __shared__ int s_node, s_redf;
     const int tid = threadIdx.x;
     const bool active = tid < NH;
     // x pass: thread (Y = Yp, X' = Xh and Xh + K), Xh fastest
@@ -578,6 +580,7 @@ __global__ void __launch_bounds__(((2 * K * K + 31) / 32) * 32, 2) apply32_kerne
             }
         }
         __syncthreads();
+        finish_chunk(L, w, 8 * K3, &s_redf);
     }
 }
 
@@ -852,23 +855,6 @@ void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s) {
 void k_to_fp32_cube(const double *in, float *out, size_t nblocks, int K, cudaStream_t s) {
     if (nblocks == 0) return;
     to_fp32_cube_kernel<<<4096, 256, 0, s>>>(in, out, nblocks, K);
-    MWG_CUDA(cudaGetLastError());
-}
-
-__global__ void reduce_partials_kernel(const ReduceTask *tasks, int n, int bs) {
-    for (int t = blockIdx.x; t < n; t += gridDim.x) {
-        const ReduceTask T = tasks[t];
-        for (int i = threadIdx.x; i < bs; i += blockDim.x) {
-            double v = T.set ? 0.0 : T.out[i];
-            for (int c = 0; c < T.count; c++) v += T.part[(size_t)c * bs + i];
-            T.out[i] = v;
-        }
-    }
-}
-
-void k_reduce_partials(const ReduceTask *tasks, int n, int bs, cudaStream_t s) {
-    if (n <= 0) return;
-    reduce_partials_kernel<<<std::min(n, 4096), 256, 0, s>>>(tasks, n, bs);
     MWG_CUDA(cudaGetLastError());
 }
 
