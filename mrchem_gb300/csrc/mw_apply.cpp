@@ -344,13 +344,13 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     pk.add(li.coef.data(), ni * sizeof(double));
     pk.add(red.data(), red.size() * sizeof(ReduceTask));
     pk.add(redof.data(), redof.size() * sizeof(int));
+    // the task counter, the status word and the chunk counters start at zero: they travel with the
+    // pack instead of being cleared by separate launches
+    std::vector<int> zeros(2 + red.size(), 0);
+    pk.add(zeros.data(), zeros.size() * sizeof(int));
     pk.ship(ctx, arena);
-    int *counter = (int *)arena.alloc(2 * sizeof(int));
-    int *red_cnt = nullptr;
-    if (!red.empty()) {
-        red_cnt = (int *)arena.alloc(red.size() * sizeof(int));
-        MWG_CUDA(cudaMemsetAsync(red_cnt, 0, red.size() * sizeof(int), ctx.stream));
-    }
+    int *counter = (int *)pk.ptr(10);
+    int *red_cnt = red.empty() ? nullptr : counter + 2;
     ApplyLaunch L;
     L.nnodes = nv;
     L.root = root ? 1 : 0;

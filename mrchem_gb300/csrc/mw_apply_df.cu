@@ -245,7 +245,6 @@ void launch_df(const ApplyLaunch &L, int nsm, cudaStream_t s) {
 
 void k_apply_df(const DevBasis &b, const ApplyLaunch &L, int nsm, cudaStream_t s) {
     if (L.nnodes <= 0) return;
-    MWG_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(int), s));
     switch (b.K) {
         case 4: launch_df<4>(L, nsm, s); break;
         case 5: launch_df<5>(L, nsm, s); break;

@@ -513,8 +513,6 @@ void k_to_tc_x(const float *cube32, float *out, size_t nblocks, int K, cudaStrea
 
 void k_apply_tc05(const DevBasis &b, const ApplyLaunch &L, cudaStream_t s) {
     if (L.nnodes <= 0) return;
-    MWG_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(int), s));
-    MWG_CUDA(cudaMemsetAsync(L.status, 0, sizeof(int), s));
     switch (b.K) {
         case 4: launch_tc05<4>(L, s); break;
         case 5: launch_tc05<5>(L, s); break;

@@ -251,7 +251,7 @@ struct ApplyLaunch {
     const void *const *ay;
     const void *const *az;
     const double *coef;           // per item
-    int *counter;                 // dynamic node counter (persistent grid)
+    int *counter;                 // dynamic node counter (persistent grid); zero at launch
     int *status;                  // 0, or non-zero when a bounded wait of the launch ran out (TF32 tier)
     // chunked nodes: per task the index of its node's ReduceTask (-1: the task is a whole node),
     // and per ReduceTask a counter of finished chunks (zero at launch).  The CTA that finishes a

@@ -802,7 +802,6 @@ void k_generate(const DevBasis &b, const GenTask *tasks, int n, double *scratch,
 
 void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s) {
     if (L.nnodes <= 0) return;
-    MWG_CUDA(cudaMemsetAsync(L.counter, 0, sizeof(int), s));
     if (fp32)
         launch_apply_k<float>(b.K, L, nsm, s);
     else
