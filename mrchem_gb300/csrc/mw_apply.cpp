@@ -657,6 +657,9 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             double tthr = !root ? thr
                           : s.job->abs_prec ? SCREEN_FAC * split_thr(s.job->prec, 1.0, n) / std::max(s.wgt[w], 1e-300)
                                             : -1.0;
+            // TF32 at the root scale only where its threshold is the plain one: absolute precision
+            // and no precision-steering trees (their weights shrink on the huge root boxes)
+            const bool tf32_here = !root || (s.job->abs_prec && s.job->prec_trees.empty());
             long long c[NTIER] = {0, 0, 0, 0};
             for (Cand &cd : s.cand[w]) {
                 const double *cn = cd.gen ? &s.gcn[8 * (size_t)cd.src] : &inp.cn[8 * (size_t)cd.src];
@@ -678,7 +681,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     tier = bd <= TIER_DF * tthr ? 3 : 0;
                 else if (bd > TIER_FP64 * tthr)
                     tier = (dfp && bd <= TIER_DF * tthr) ? 3 : 0;
-                else if (tensor && !root && bd <= TIER_TF32 * tthr)
+                else if (tensor && tf32_here && bd <= TIER_TF32 * tthr)
                     tier = 2;
                 else
                     tier = 1;
