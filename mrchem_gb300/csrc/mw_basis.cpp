@@ -185,6 +185,7 @@ double expansion_error(int kind, double mu, const std::vector<double> &c, const 
                        double rmax) {
     double err = 0.0;
     const int N = 4000;
+#pragma omp parallel for reduction(max : err) schedule(static)
     for (int i = 0; i <= N; i++) {
         double r = rmin * std::pow(rmax / rmin, (double)i / N), v = 0.0;
         for (size_t t = 0; t < c.size(); t++) v += c[t] * std::exp(-a[t] * r * r);
@@ -227,153 +228,7 @@ struct CrossCorr {
         }
     }
 
-    // G[p] = int_0^1 P_p(2z-1) exp(-beta (z + l)^2) dz
-    void moments(double beta, double l, int np, double *G) const {
-        std::fill(G, G + np, 0.0);
-        double c0 = -l, w = 1.0 / std::sqrt(beta);
-        double lo = std::max(0.0, c0 - 12.0 * w), hi = std::min(1.0, c0 + 12.0 * w);
-        if (lo >= hi) return;
-        double pw = std::min(0.125, 0.5 * w);
-        int npc = (int)std::ceil((hi - lo) / pw);
-        double step = (hi - lo) / npc;
-        double P[2 * KMAX + 2];
-        for (int k = 0; k < npc; k++) {
-            double a0 = lo + k * step;
-            for (int q = 0; q < QPTS; q++) {
-                double z = a0 + step * gx[q], e = beta * (z + l) * (z + l);
-                if (e > 745.0) continue;
-                double g = step * gw[q] * std::exp(-e);
-                legendre_shifted(np, z, P);
-                for (int p = 0; p < np; p++) G[p] += g * P[p];
-            }
-        }
-    }
-
-    // tau(m)_{ij} = 2^{-s} int int phi_i(u) phi_j(v) exp(-a 4^{-s} (u - v + m)^2)
-    void tau(double a, int s, int m, double *out) const {
-        int K2 = 2 * K;
-        double beta = a * std::pow(4.0, -s), pref = std::pow(2.0, -s);
-        double Gp[2 * KMAX + 2], Gm[2 * KMAX + 2];
-        moments(beta, (double)m, K2, Gp);
-        moments(beta, (double)(-m), K2, Gm);
-        for (int i = 0; i < K; i++)
-            for (int j = 0; j < K; j++) {
-                const double *aij = &coef[(i * K + j) * K2], *aji = &coef[(j * K + i) * K2];
-                double v = 0.0;
-                for (int p = 0; p < K2; p++) v += aij[p] * Gp[p] + aji[p] * Gm[p];
-                out[i * K + j] = pref * v;
-            }
-    }
 };
-
-struct TermScale {
-    int band = -1;
-    std::vector<double> blk, nrm;
-};
-
-void ns_block(const Basis &b, const double *tm1, const double *t0, const double *tp1, double *ns) {
-    int K = b.K, K2 = 2 * K;
-    std::vector<double> M(K2 * K2), T1(K2 * K2);
-    for (int i = 0; i < K; i++)
-        for (int j = 0; j < K; j++) {
-            M[i * K2 + j] = t0[i * K + j];
-            M[i * K2 + K + j] = tm1[i * K + j];
-            M[(K + i) * K2 + j] = tp1[i * K + j];
-            M[(K + i) * K2 + K + j] = t0[i * K + j];
-        }
-    for (int r = 0; r < K2; r++)
-        for (int c = 0; c < K2; c++) {
-            double v = 0.0;
-            for (int k = 0; k < K2; k++) v += b.W[r * K2 + k] * M[k * K2 + c];
-            T1[r * K2 + c] = v;
-        }
-    for (int r = 0; r < K2; r++)
-        for (int c = 0; c < K2; c++) {
-            double v = 0.0;
-            for (int k = 0; k < K2; k++) v += T1[r * K2 + k] * b.W[c * K2 + k];
-            ns[r * K2 + c] = v;
-        }
-}
-
-void sub_norms(int K, const double *ns, double *nr) {
-    int K2 = 2 * K;
-    for (int g = 0; g < 2; g++)
-        for (int f = 0; f < 2; f++) {
-            double s = 0.0;
-            for (int i = 0; i < K; i++)
-                for (int j = 0; j < K; j++) {
-                    double v = ns[(g * K + i) * K2 + f * K + j];
-                    s += v * v;
-                }
-            nr[2 * g + f] = std::sqrt(s);
-        }
-}
-
-void term_scale(const Basis &b, const CrossCorr &cc, double a, int n, TermScale &out) {
-    int K = b.K, K2 = 2 * K, bsz = K2 * K2, s = n + 1;
-    bool root = (n == b.n0);
-    int maxbox = std::max(b.boxes[0], std::max(b.boxes[1], b.boxes[2]));
-    long world = (long)maxbox << (n - b.n0);
-    int cap = (int)std::min<long>(1024, world - 1);
-    std::vector<double> pos, pnr;
-    std::vector<double> tm1(K * K), t0(K * K), tp1(K * K);
-    int L = -1;
-    double peak = 0.0;
-    for (int l = 0; l <= cap; l++) {
-        cc.tau(a, s, 2 * l - 1, tm1.data());
-        cc.tau(a, s, 2 * l, t0.data());
-        cc.tau(a, s, 2 * l + 1, tp1.data());
-        pos.resize((size_t)bsz * (l + 1));
-        pnr.resize(4 * (l + 1));
-        ns_block(b, tm1.data(), t0.data(), tp1.data(), &pos[(size_t)l * bsz]);
-        sub_norms(K, &pos[(size_t)l * bsz], &pnr[4 * l]);
-        L = l;
-        if (root) continue;
-        double mx = *std::max_element(&pnr[4 * l], &pnr[4 * l] + 4);
-        double nsn = std::max(pnr[4 * l + 1], std::max(pnr[4 * l + 2], pnr[4 * l + 3]));
-        if (l <= 1) peak = std::max(peak, mx);
-        if (l >= 2 && nsn < NS_CLEAN * peak) {
-            L = l - 1;
-            break;
-        }
-    }
-    if (!root) {
-        bool active = false;
-        for (int l = 0; l <= L; l++)
-            for (int g = 0; g < 2; g++)
-                for (int f = 0; f < 2; f++) {
-                    if (pnr[4 * l + 2 * g + f] < NS_CLEAN * peak) {
-                        pnr[4 * l + 2 * g + f] = 0.0;
-                        for (int i = 0; i < K; i++)
-                            for (int j = 0; j < K; j++) pos[(size_t)l * bsz + (g * K + i) * K2 + f * K + j] = 0.0;
-                    } else if (g + f > 0) {
-                        active = true;
-                    }
-                }
-        if (!active) L = -1;
-    }
-    out.band = L;
-    if (L < 0) return;
-    out.blk.assign((size_t)bsz * (2 * L + 1), 0.0);
-    out.nrm.assign(4 * (2 * L + 1), 0.0);
-    for (int l = -L; l <= L; l++) {
-        double *dst = &out.blk[(size_t)(l + L) * bsz];
-        double *dn = &out.nrm[4 * (l + L)];
-        if (l >= 0) {
-            std::memcpy(dst, &pos[(size_t)l * bsz], sizeof(double) * bsz);
-            std::memcpy(dn, &pnr[4 * l], sizeof(double) * 4);
-        } else {
-            // NS(-l) = NS(l)^T; transposition swaps the (0,1) and (1,0) sub-blocks
-            const double *src = &pos[(size_t)(-l) * bsz];
-            for (int r = 0; r < K2; r++)
-                for (int c = 0; c < K2; c++) dst[c * K2 + r] = src[r * K2 + c];
-            dn[0] = pnr[4 * (-l) + 0];
-            dn[1] = pnr[4 * (-l) + 2];
-            dn[2] = pnr[4 * (-l) + 1];
-            dn[3] = pnr[4 * (-l) + 3];
-        }
-    }
-}
 
 }  // namespace
 
@@ -390,72 +245,144 @@ void Oper::build(const Basis &b) {
     }
     T = (int)c.size();
     S = b.max_depth;
+    // NS blocks on the GPU (mw_opbuild.cu).  Phase 1 walks every (term, scale) and returns the
+    // sub-block norms of NS(0..L); the band cut below is the rule the walk and the clean-up of
+    // small sub-blocks follow; phase 2 writes the kept blocks.
     CrossCorr cc;
     cc.init(b);
-    std::vector<TermScale> ts((size_t)T * S);
-#pragma omp parallel for schedule(dynamic, 1) collapse(2)
+    const int K = b.K, K2 = 2 * K, bsz = K2 * K2;
+    const int ntask = T * S;
+    std::vector<OpBuildTask> tasks(ntask);
+    long nrm_total = 0;
     for (int t = 0; t < T; t++)
-        for (int s = 0; s < S; s++) term_scale(b, cc, a[t], b.n0 + s, ts[(size_t)t * S + s]);
-    band.assign(T * S, -1);
-    off.assign(T * S, 0);
+        for (int si = 0; si < S; si++) {
+            const int n = b.n0 + si, sc = n + 1;
+            const long world = (long)maxbox << (n - b.n0);
+            OpBuildTask &tk = tasks[(size_t)t * S + si];
+            tk.beta = a[t] * std::pow(4.0, -sc);
+            tk.pref = std::pow(2.0, -sc);
+            tk.root = n == b.n0 ? 1 : 0;
+            tk.cap = (int)std::min<long>(1024, world - 1);
+            tk.nrm_off = nrm_total;
+            nrm_total += 4L * (tk.cap + 1);
+        }
+    Ctx &cx = *ctx;
+    cudaStream_t st = cx.stream;
+    double *d_cc = nullptr, *d_q = nullptr, *d_nrm = nullptr, *d_peak = nullptr;
+    int *d_band = nullptr;
+    OpBuildTask *d_tasks = nullptr;
+    MWG_CUDA(cudaMalloc(&d_cc, sizeof(double) * cc.coef.size()));
+    MWG_CUDA(cudaMalloc(&d_q, sizeof(double) * 2 * 16));
+    MWG_CUDA(cudaMalloc(&d_tasks, sizeof(OpBuildTask) * ntask));
+    MWG_CUDA(cudaMalloc(&d_nrm, sizeof(double) * nrm_total));
+    MWG_CUDA(cudaMalloc(&d_band, sizeof(int) * ntask));
+    MWG_CUDA(cudaMalloc(&d_peak, sizeof(double) * ntask));
+    double *d_head = nullptr;
+    MWG_CUDA(cudaMalloc(&d_head, sizeof(double) * ntask * 4 * OP_NRM_HEAD));
+    double q[32];
+    std::copy(cc.gx, cc.gx + 16, q);
+    std::copy(cc.gw, cc.gw + 16, q + 16);
+    MWG_CUDA(cudaMemcpyAsync(d_cc, cc.coef.data(), sizeof(double) * cc.coef.size(), cudaMemcpyHostToDevice, st));
+    MWG_CUDA(cudaMemcpyAsync(d_q, q, sizeof(q), cudaMemcpyHostToDevice, st));
+    MWG_CUDA(cudaMemcpyAsync(d_tasks, tasks.data(), sizeof(OpBuildTask) * ntask, cudaMemcpyHostToDevice, st));
+    k_op_band(K, cx.dbasis.W, d_cc, d_q, d_q + 16, d_tasks, ntask, d_nrm, d_head, d_band, d_peak, st);
+    std::vector<int> walked(ntask);
+    std::vector<double> peak(ntask);
+    MWG_CUDA(cudaMemcpyAsync(walked.data(), d_band, sizeof(int) * ntask, cudaMemcpyDeviceToHost, st));
+    MWG_CUDA(cudaMemcpyAsync(peak.data(), d_peak, sizeof(double) * ntask, cudaMemcpyDeviceToHost, st));
+    std::vector<double> head((size_t)ntask * 4 * OP_NRM_HEAD);
+    MWG_CUDA(cudaMemcpyAsync(head.data(), d_head, sizeof(double) * head.size(), cudaMemcpyDeviceToHost, st));
+    MWG_CUDA(cudaStreamSynchronize(st));
+    // the walked norms: the first OP_NRM_HEAD translations of every task came in one copy, longer
+    // walks are fetched one by one
+    std::vector<std::vector<double>> pnr(ntask);
+    bool fetch = false;
+    for (int i = 0; i < ntask; i++) {
+        pnr[i].resize(4 * (size_t)(walked[i] + 1));
+        if (walked[i] < OP_NRM_HEAD) {
+            std::copy(&head[(size_t)i * 4 * OP_NRM_HEAD], &head[(size_t)i * 4 * OP_NRM_HEAD] + pnr[i].size(),
+                      pnr[i].begin());
+        } else {
+            MWG_CUDA(cudaMemcpyAsync(pnr[i].data(), d_nrm + tasks[i].nrm_off, sizeof(double) * pnr[i].size(),
+                                     cudaMemcpyDeviceToHost, st));
+            fetch = true;
+        }
+    }
+    if (fetch) MWG_CUDA(cudaStreamSynchronize(st));
+    // band cut: sub-blocks below NS_CLEAN x the (t, n) peak are zeroed, and a term with no
+    // scaling-wavelet, wavelet-scaling or wavelet-wavelet sub-block left is inactive at n
+    band.assign(ntask, -1);
+    off.assign(ntask, 0);
+    std::vector<std::vector<int>> zero(ntask);
+    for (int i = 0; i < ntask; i++) {
+        int L = walked[i];
+        zero[i].assign(L + 1, 0);
+        if (!tasks[i].root) {
+            bool active = false;
+            for (int l = 0; l <= L; l++)
+                for (int g = 0; g < 2; g++)
+                    for (int f = 0; f < 2; f++) {
+                        double &v = pnr[i][4 * l + 2 * g + f];
+                        if (v < NS_CLEAN * peak[i]) {
+                            v = 0.0;
+                            zero[i][l] |= 1 << (2 * g + f);
+                        } else if (g + f > 0) {
+                            active = true;
+                        }
+                    }
+            if (!active) L = -1;
+        }
+        band[i] = L;
+    }
     nblocks = 0;
-    for (int i = 0; i < T * S; i++) {
-        band[i] = ts[i].band;
+    for (int i = 0; i < ntask; i++) {
         off[i] = nblocks;
-        if (ts[i].band >= 0) nblocks += 2 * ts[i].band + 1;
+        if (band[i] >= 0) nblocks += 2 * band[i] + 1;
     }
-    int K = b.K, bsz = 4 * K * K;
-    std::vector<double> blocks((size_t)std::max<long>(nblocks, 1) * bsz, 0.0);
     norms.assign((size_t)std::max<long>(nblocks, 1) * 4, 0.0);
-    amax.assign(T * S, 0.0);
-    xmax.assign(T * S, 0.0);
-    for (int i = 0; i < T * S; i++) {
-        if (ts[i].band < 0) continue;
-        int cnt = 2 * ts[i].band + 1;
-        std::memcpy(&blocks[(size_t)off[i] * bsz], ts[i].blk.data(), sizeof(double) * bsz * cnt);
-        std::memcpy(&norms[(size_t)off[i] * 4], ts[i].nrm.data(), sizeof(double) * 4 * cnt);
-        for (int q = 0; q < 4 * cnt; q++) {
-            amax[i] = std::max(amax[i], ts[i].nrm[q]);
-            if (q % 4 > 0) xmax[i] = std::max(xmax[i], ts[i].nrm[q]);
+    amax.assign(ntask, 0.0);
+    xmax.assign(ntask, 0.0);
+    std::vector<OpBlockJob> jobs;
+    for (int i = 0; i < ntask; i++) {
+        const int L = band[i];
+        if (L < 0) continue;
+        for (int l = -L; l <= L; l++) {
+            double *dn = &norms[(size_t)(off[i] + l + L) * 4];
+            const double *src = &pnr[i][4 * std::abs(l)];
+            if (l >= 0) {
+                for (int k = 0; k < 4; k++) dn[k] = src[k];
+            } else {  // NS(-l) = NS(l)^T swaps the (0,1) and (1,0) sub-blocks
+                dn[0] = src[0];
+                dn[1] = src[2];
+                dn[2] = src[1];
+                dn[3] = src[3];
+            }
+            for (int k = 0; k < 4; k++) {
+                amax[i] = std::max(amax[i], dn[k]);
+                if (k > 0) xmax[i] = std::max(xmax[i], dn[k]);
+            }
         }
+        for (int l = 0; l <= L; l++) jobs.push_back(OpBlockJob{i, l, L, zero[i][l], off[i]});
     }
-    // device copies: FP64, and FP32 for the reduced tiers.  Each FP32 block is its high part (the
-    // value rounded to FP32, read by the FP32 and TF32 tiers) followed by its low part (the
-    // rounded remainder, read with the high part by the double-FP32 tier).
-    size_t nel = blocks.size();
-    std::vector<float> b32(2 * nel);
-    for (size_t i = 0; i < nel; i++) {
-        const size_t blk = i / (size_t)bsz, r = i - blk * (size_t)bsz;
-        const float h = (float)blocks[i];
-        b32[2 * blk * bsz + r] = h;
-        b32[2 * blk * bsz + bsz + r] = (float)(blocks[i] - (double)h);
-    }
+    const size_t nel = (size_t)std::max<long>(nblocks, 1) * bsz;
     MWG_CUDA(cudaMalloc(&d_blocks, sizeof(double) * nel));
-    MWG_CUDA(cudaMalloc(&d_blocks32, sizeof(float) * 2 * nel));
-    MWG_CUDA(cudaMemcpy(d_blocks, blocks.data(), sizeof(double) * nel, cudaMemcpyHostToDevice));
-    MWG_CUDA(cudaMemcpy(d_blocks32, b32.data(), sizeof(float) * 2 * nel, cudaMemcpyHostToDevice));
-    // the tensor-core tier's B operand of every block (mw_tc05_layout.h): k-groups of 4 columns,
-    // rows n < 2K = A[n][k], rows 2K + i (i < K) = A[i][k] for k >= K (zero for k < K), TF32
-    if (K >= 4 && K <= KMAX) {
-        const int N2 = 2 * K, NB = tc5_n(K);
-        const size_t per = tc5_b_floats(K), nb = nel / (size_t)bsz;
-        std::vector<float> tc(per * nb, 0.0f);
-        for (size_t blk = 0; blk < nb; blk++) {
-            const float *h = &b32[2 * blk * bsz];
-            float *o = &tc[blk * per];
-            for (int n = 0; n < NB; n++)
-                for (int k = 0; k < N2; k++) {
-                    float v = 0.0f;
-                    if (n < N2)
-                        v = h[n * N2 + k];
-                    else if (n < N2 + K && k >= K)
-                        v = h[(n - N2) * N2 + k];
-                    o[((size_t)(k / 4) * NB + n) * 4 + (k % 4)] = tf32_round_host(v);
-                }
-        }
-        MWG_CUDA(cudaMalloc(&d_blocks_tc, sizeof(float) * tc.size()));
-        MWG_CUDA(cudaMemcpy(d_blocks_tc, tc.data(), sizeof(float) * tc.size(), cudaMemcpyHostToDevice));
+    MWG_CUDA(cudaMemsetAsync(d_blocks, 0, sizeof(double) * nel, st));
+    OpBlockJob *d_jobs = nullptr;
+    if (!jobs.empty()) {
+        MWG_CUDA(cudaMalloc(&d_jobs, sizeof(OpBlockJob) * jobs.size()));
+        MWG_CUDA(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(OpBlockJob) * jobs.size(), cudaMemcpyHostToDevice, st));
+        k_op_blocks(K, cx.dbasis.W, d_cc, d_q, d_q + 16, d_tasks, d_jobs, (int)jobs.size(), d_blocks, st);
     }
+    // device copies for the reduced tiers: FP32 high part then low part per block (FP32 and
+    // double-FP32 tiers), and the tensor-core tier's B operand (mw_tc05_layout.h)
+    MWG_CUDA(cudaMalloc(&d_blocks32, sizeof(float) * 2 * nel));
+    const bool tc = K >= 4 && K <= KMAX;
+    if (tc) MWG_CUDA(cudaMalloc(&d_blocks_tc, sizeof(float) * tc5_b_floats(K) * (nel / bsz)));
+    k_op_convert(d_blocks, d_blocks32, tc ? d_blocks_tc : nullptr, (long)(nel / bsz), K, tc5_n(K), 2 * tc5_ks(K), st);
+    MWG_CUDA(cudaStreamSynchronize(st));
+    for (void *pp : {(void *)d_cc, (void *)d_q, (void *)d_tasks, (void *)d_nrm, (void *)d_band, (void *)d_peak,
+                     (void *)d_jobs, (void *)d_head})
+        if (pp) cudaFree(pp);
 }
 
 }  // namespace mwg

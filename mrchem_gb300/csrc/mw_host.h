@@ -312,6 +312,24 @@ void k_multiply(const DevBasis &b, const MulTask *tasks, int n, cudaStream_t s);
 void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
            cudaStream_t s);
 void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);
+// operator construction on the GPU (mw_opbuild.cu)
+struct OpBuildTask {  // one (term, scale): tau(m) = pref * (Legendre expansion . Gaussian moments of beta)
+    double beta, pref;
+    int root, cap;    // root scale: no early stop; cap: largest translation walked
+    long nrm_off;     // first of this task's 4 (cap + 1) sub-block norms
+};
+struct OpBlockJob {  // one block pair NS(+l), NS(-l) of a task, at off + band +- l
+    int task, l, band, zero;  // zero: bit 2g+f marks sub-block (g, f) as cut
+    long off;
+};
+size_t op_build_smem();
+constexpr int OP_NRM_HEAD = 64;  // translations per task whose norms phase 1 also writes compactly
+void k_op_band(int K, const double *W, const double *cc, const double *gx, const double *gw, const OpBuildTask *tasks,
+               int ntask, double *nrm, double *head, int *band, double *peak, cudaStream_t s);
+void k_op_blocks(int K, const double *W, const double *cc, const double *gx, const double *gw, const OpBuildTask *tasks,
+                 const OpBlockJob *jobs, int njob, double *blocks, cudaStream_t s);
+void k_op_convert(const double *blocks, float *b32, float *btc, long nblocks, int K, int NB, int groups,
+                  cudaStream_t s);
 // FP32 shadow of whole blocks in cube order cube[Z][Y][X] (X = cx*K + ix): per block a high cube
 // and a low cube (2 * 8K^3 floats, the low one holds the rounded remainder)
 void k_to_fp32_cube(const double *in, float *out, size_t nblocks, int K, cudaStream_t s);

@@ -74,12 +74,17 @@ def test_poisson_operator_matches_oracle(engine, oracle, k7):
         for n in (-5, -2, 0, 3, 6):
             L = P.band(t, n)
             assert L == Q.band(t, n)
-            for l in {-L, 0, L} if L >= 0 else ():
+            if L < 0:
+                continue
+            # tolerance relative to the (term, scale)'s largest block, NS(0): the blocks at the band
+            # edge are many orders smaller and come out of cancellation in the Gaussian moments,
+            # so their last digits depend on the order of the quadrature sums
+            scale = max(np.abs(Q.block(t, n, 0)[0]).max(), 1e-300)
+            for l in {-L, 0, L}:
                 b1, n1 = P.block(t, n, l)
                 b2, n2 = Q.block(t, n, l)
-                scale = max(np.abs(b2).max(), 1e-300)
                 assert np.abs(b1 - b2).max() <= 1e-12 * scale
-                assert np.allclose(n1, n2, rtol=1e-12, atol=1e-300)
+                assert np.allclose(n1, n2, rtol=1e-12, atol=1e-12 * scale)
 
 
 def test_projection_matches_oracle(engine, oracle, k7):
