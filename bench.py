@@ -201,7 +201,7 @@ def run(args):
         f.rescale(1.0 / f.norm())
         phis.append(f)
     t0 = time.perf_counter()
-    ops = [mw.HelmholtzOperator(mra, float(m), PREC) for m in mus]
+    ops = mw.HelmholtzOperator.batch(mra, mus, PREC)  # one operator per orbital, built together
     op_build_s = time.perf_counter() - t0
     in_nodes = [p.nnodes for p in phis]
 

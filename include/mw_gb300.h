@@ -168,6 +168,9 @@ int mw_dot_noalloc(mw_tree a, mw_tree b, double *out);
 /* ---- operators (src/driver.cpp:1131,1283; src/scf_solver/HelmholtzVector.cpp:144) ---- */
 int mw_op_create_poisson(mw_ctx ctx, double prec, mw_op *out);
 int mw_op_create_helmholtz(mw_ctx ctx, double mu, double prec, mw_op *out);
+/* n Helmholtz operators built together (their NS blocks in shared GPU launches); the loop that
+ * creates one operator per orbital in HelmholtzVector::apply, src/scf_solver/HelmholtzVector.cpp:144 */
+int mw_op_create_helmholtz_batch(mw_ctx ctx, int n, const double *mu, double prec, mw_op *out);
 int mw_op_destroy(mw_op op);
 int mw_op_nterms(mw_op op, int *n);
 int mw_op_terms(mw_op op, double *coefs, double *exps);

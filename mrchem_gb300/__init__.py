@@ -74,7 +74,7 @@ EXPORTS = [
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
     "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
-    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap", "mw_ctx_set_groups", "mw_apply_batch_autotune",
+    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap", "mw_ctx_set_groups", "mw_apply_batch_autotune", "mw_op_create_helmholtz_batch",
     "mw_tree_upload_batch", "mw_tree_download_batch", "mw_pin_host", "mw_unpin_host",
 ]
 
@@ -131,6 +131,7 @@ def load_library(path=None):
         "mw_op_block": [P, I, I, I, dp, dp],
         "mw_apply": [D, P, P, P, I, pp, I, I, I],
         "mw_apply_batch": [I, dp, pp, pp, pp, ip, pp, I, I, I],
+        "mw_op_create_helmholtz_batch": [P, I, dp, D, pp],
         "mw_apply_batch_autotune": [I, dp, pp, pp, pp, I, I, I, ip, C.POINTER(C.c_longlong), dp],
         "mw_multiply_batch": [I, dp, pp, dp, pp, pp, I, I, I],
         "mw_apply_fixed": [D, P, P, P, I, I],
@@ -456,10 +457,21 @@ class PoissonOperator(ConvolutionOperator):
 class HelmholtzOperator(ConvolutionOperator):
     """Separated Gaussian-sum expansion of exp(-mu r)/r (mrcpp::HelmholtzOperator(MRA, mu, prec))."""
 
-    def __init__(self, mra, mu, prec):
-        h = C.c_void_p()
-        _check(_lib.mw_op_create_helmholtz(mra.ptr, mu, prec, C.byref(h)), mra.ptr)
-        super().__init__(mra, h.value)
+    def __init__(self, mra, mu, prec, _handle=None):
+        if _handle is None:
+            h = C.c_void_p()
+            _check(_lib.mw_op_create_helmholtz(mra.ptr, mu, prec, C.byref(h)), mra.ptr)
+            _handle = h.value
+        self.mu = mu
+        super().__init__(mra, _handle)
+
+    @classmethod
+    def batch(cls, mra, mus, prec):
+        """One operator per mu, built together (shared GPU launches for their NS blocks)."""
+        mus = np.ascontiguousarray(mus, dtype=np.float64)
+        hs = (C.c_void_p * len(mus))()
+        _check(_lib.mw_op_create_helmholtz_batch(mra.ptr, len(mus), _dp(mus), float(prec), hs), mra.ptr)
+        return [cls(mra, float(m), prec, _handle=h) for m, h in zip(mus, hs)]
 
 
 def _ptrs(trees):

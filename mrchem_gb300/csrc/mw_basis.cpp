@@ -232,52 +232,66 @@ struct CrossCorr {
 
 }  // namespace
 
-void Oper::build(const Basis &b) {
-    eps = 0.1 * prec;
-    int maxbox = std::max(b.boxes[0], std::max(b.boxes[1], b.boxes[2]));
-    rmax = std::sqrt(3.0) * maxbox * std::ldexp(1.0, -b.n0);
-    rmin = std::ldexp(1.0, -(b.n0 + b.max_depth));
-    double h = M_PI * M_PI / (2.0 * std::log(1.0 / eps));
-    for (int it = 0; it < 60; it++) {
-        expansion(kind, mu, eps, rmin, rmax, h, c, a);
-        if (expansion_error(kind, mu, c, a, rmin, rmax) <= eps) break;
-        h *= 0.93;
+void Oper::build(const Basis &b) { build_operators({this}, b); }
+
+// Builds several operators of one context together: the Gaussian-sum fits on the host, then
+// one band walk (phase 1) over every (operator, term, scale), one copy of its results, the
+// band cuts on the host, and one launch (phase 2) for all the kept blocks.
+void build_operators(const std::vector<Oper *> &ops, const Basis &b) {
+    if (ops.empty()) return;
+    Ctx &cx = *ops[0]->ctx;
+    const int K = b.K, K2 = 2 * K, bsz = K2 * K2;
+    const int maxbox = std::max(b.boxes[0], std::max(b.boxes[1], b.boxes[2]));
+    // the fits, one operator per host thread (a single operator's error sampling is itself parallel)
+#pragma omp parallel for schedule(dynamic, 1) if (ops.size() > 1)
+    for (size_t o = 0; o < ops.size(); o++) {
+        Oper *op = ops[o];
+        op->eps = 0.1 * op->prec;
+        op->rmax = std::sqrt(3.0) * maxbox * std::ldexp(1.0, -b.n0);
+        op->rmin = std::ldexp(1.0, -(b.n0 + b.max_depth));
+        double h = M_PI * M_PI / (2.0 * std::log(1.0 / op->eps));
+        for (int it = 0; it < 60; it++) {
+            expansion(op->kind, op->mu, op->eps, op->rmin, op->rmax, h, op->c, op->a);
+            if (expansion_error(op->kind, op->mu, op->c, op->a, op->rmin, op->rmax) <= op->eps) break;
+            h *= 0.93;
+        }
+        op->T = (int)op->c.size();
+        op->S = b.max_depth;
     }
-    T = (int)c.size();
-    S = b.max_depth;
-    // NS blocks on the GPU (mw_opbuild.cu).  Phase 1 walks every (term, scale) and returns the
-    // sub-block norms of NS(0..L); the band cut below is the rule the walk and the clean-up of
-    // small sub-blocks follow; phase 2 writes the kept blocks.
+    // phase 1 tasks of all operators, operator after operator
     CrossCorr cc;
     cc.init(b);
-    const int K = b.K, K2 = 2 * K, bsz = K2 * K2;
-    const int ntask = T * S;
+    std::vector<int> base(ops.size() + 1, 0);
+    for (size_t o = 0; o < ops.size(); o++) base[o + 1] = base[o] + ops[o]->T * ops[o]->S;
+    const int ntask = base.back();
     std::vector<OpBuildTask> tasks(ntask);
     long nrm_total = 0;
-    for (int t = 0; t < T; t++)
-        for (int si = 0; si < S; si++) {
-            const int n = b.n0 + si, sc = n + 1;
-            const long world = (long)maxbox << (n - b.n0);
-            OpBuildTask &tk = tasks[(size_t)t * S + si];
-            tk.beta = a[t] * std::pow(4.0, -sc);
-            tk.pref = std::pow(2.0, -sc);
-            tk.root = n == b.n0 ? 1 : 0;
-            tk.cap = (int)std::min<long>(1024, world - 1);
-            tk.nrm_off = nrm_total;
-            nrm_total += 4L * (tk.cap + 1);
-        }
-    Ctx &cx = *ctx;
+    for (size_t o = 0; o < ops.size(); o++) {
+        const Oper &op = *ops[o];
+        for (int t = 0; t < op.T; t++)
+            for (int si = 0; si < op.S; si++) {
+                const int n = b.n0 + si, sc = n + 1;
+                const long world = (long)maxbox << (n - b.n0);
+                OpBuildTask &tk = tasks[(size_t)base[o] + (size_t)t * op.S + si];
+                tk.beta = op.a[t] * std::pow(4.0, -sc);
+                tk.pref = std::pow(2.0, -sc);
+                tk.root = n == b.n0 ? 1 : 0;
+                tk.cap = (int)std::min<long>(1024, world - 1);
+                tk.nrm_off = nrm_total;
+                nrm_total += 4L * (tk.cap + 1);
+            }
+    }
     cudaStream_t st = cx.stream;
-    double *d_cc = nullptr, *d_q = nullptr, *d_nrm = nullptr, *d_peak = nullptr;
+    double *d_cc = nullptr, *d_q = nullptr, *d_nrm = nullptr, *d_peak = nullptr, *d_head = nullptr;
     int *d_band = nullptr;
     OpBuildTask *d_tasks = nullptr;
+    OpBlockJob *d_jobs = nullptr;
     MWG_CUDA(cudaMalloc(&d_cc, sizeof(double) * cc.coef.size()));
     MWG_CUDA(cudaMalloc(&d_q, sizeof(double) * 2 * 16));
     MWG_CUDA(cudaMalloc(&d_tasks, sizeof(OpBuildTask) * ntask));
     MWG_CUDA(cudaMalloc(&d_nrm, sizeof(double) * nrm_total));
     MWG_CUDA(cudaMalloc(&d_band, sizeof(int) * ntask));
     MWG_CUDA(cudaMalloc(&d_peak, sizeof(double) * ntask));
-    double *d_head = nullptr;
     MWG_CUDA(cudaMalloc(&d_head, sizeof(double) * ntask * 4 * OP_NRM_HEAD));
     double q[32];
     std::copy(cc.gx, cc.gx + 16, q);
@@ -287,10 +301,9 @@ void Oper::build(const Basis &b) {
     MWG_CUDA(cudaMemcpyAsync(d_tasks, tasks.data(), sizeof(OpBuildTask) * ntask, cudaMemcpyHostToDevice, st));
     k_op_band(K, cx.dbasis.W, d_cc, d_q, d_q + 16, d_tasks, ntask, d_nrm, d_head, d_band, d_peak, st);
     std::vector<int> walked(ntask);
-    std::vector<double> peak(ntask);
+    std::vector<double> peak(ntask), head((size_t)ntask * 4 * OP_NRM_HEAD);
     MWG_CUDA(cudaMemcpyAsync(walked.data(), d_band, sizeof(int) * ntask, cudaMemcpyDeviceToHost, st));
     MWG_CUDA(cudaMemcpyAsync(peak.data(), d_peak, sizeof(double) * ntask, cudaMemcpyDeviceToHost, st));
-    std::vector<double> head((size_t)ntask * 4 * OP_NRM_HEAD);
     MWG_CUDA(cudaMemcpyAsync(head.data(), d_head, sizeof(double) * head.size(), cudaMemcpyDeviceToHost, st));
     MWG_CUDA(cudaStreamSynchronize(st));
     // the walked norms: the first OP_NRM_HEAD translations of every task came in one copy, longer
@@ -309,76 +322,86 @@ void Oper::build(const Basis &b) {
         }
     }
     if (fetch) MWG_CUDA(cudaStreamSynchronize(st));
-    // band cut: sub-blocks below NS_CLEAN x the (t, n) peak are zeroed, and a term with no
-    // scaling-wavelet, wavelet-scaling or wavelet-wavelet sub-block left is inactive at n
-    band.assign(ntask, -1);
-    off.assign(ntask, 0);
-    std::vector<std::vector<int>> zero(ntask);
-    for (int i = 0; i < ntask; i++) {
-        int L = walked[i];
-        zero[i].assign(L + 1, 0);
-        if (!tasks[i].root) {
-            bool active = false;
-            for (int l = 0; l <= L; l++)
-                for (int g = 0; g < 2; g++)
-                    for (int f = 0; f < 2; f++) {
-                        double &v = pnr[i][4 * l + 2 * g + f];
-                        if (v < NS_CLEAN * peak[i]) {
-                            v = 0.0;
-                            zero[i][l] |= 1 << (2 * g + f);
-                        } else if (g + f > 0) {
-                            active = true;
-                        }
-                    }
-            if (!active) L = -1;
-        }
-        band[i] = L;
-    }
-    nblocks = 0;
-    for (int i = 0; i < ntask; i++) {
-        off[i] = nblocks;
-        if (band[i] >= 0) nblocks += 2 * band[i] + 1;
-    }
-    norms.assign((size_t)std::max<long>(nblocks, 1) * 4, 0.0);
-    amax.assign(ntask, 0.0);
-    xmax.assign(ntask, 0.0);
+    // per operator: band cut (sub-blocks below NS_CLEAN x the (t, n) peak are zeroed, and a term
+    // with no scaling-wavelet, wavelet-scaling or wavelet-wavelet sub-block left is inactive at
+    // n), block offsets, host norm tables, device allocations and phase 2 jobs
     std::vector<OpBlockJob> jobs;
-    for (int i = 0; i < ntask; i++) {
-        const int L = band[i];
-        if (L < 0) continue;
-        for (int l = -L; l <= L; l++) {
-            double *dn = &norms[(size_t)(off[i] + l + L) * 4];
-            const double *src = &pnr[i][4 * std::abs(l)];
-            if (l >= 0) {
-                for (int k = 0; k < 4; k++) dn[k] = src[k];
-            } else {  // NS(-l) = NS(l)^T swaps the (0,1) and (1,0) sub-blocks
-                dn[0] = src[0];
-                dn[1] = src[2];
-                dn[2] = src[1];
-                dn[3] = src[3];
+    for (size_t o = 0; o < ops.size(); o++) {
+        Oper &op = *ops[o];
+        const int nt = op.T * op.S;
+        op.band.assign(nt, -1);
+        op.off.assign(nt, 0);
+        std::vector<std::vector<int>> zero(nt);
+        for (int i = 0; i < nt; i++) {
+            const int g0 = base[o] + i;
+            int L = walked[g0];
+            zero[i].assign(L + 1, 0);
+            if (!tasks[g0].root) {
+                bool active = false;
+                for (int l = 0; l <= L; l++)
+                    for (int g = 0; g < 2; g++)
+                        for (int f = 0; f < 2; f++) {
+                            double &v = pnr[g0][4 * l + 2 * g + f];
+                            if (v < NS_CLEAN * peak[g0]) {
+                                v = 0.0;
+                                zero[i][l] |= 1 << (2 * g + f);
+                            } else if (g + f > 0) {
+                                active = true;
+                            }
+                        }
+                if (!active) L = -1;
             }
-            for (int k = 0; k < 4; k++) {
-                amax[i] = std::max(amax[i], dn[k]);
-                if (k > 0) xmax[i] = std::max(xmax[i], dn[k]);
-            }
+            op.band[i] = L;
         }
-        for (int l = 0; l <= L; l++) jobs.push_back(OpBlockJob{i, l, L, zero[i][l], off[i]});
+        op.nblocks = 0;
+        for (int i = 0; i < nt; i++) {
+            op.off[i] = op.nblocks;
+            if (op.band[i] >= 0) op.nblocks += 2 * op.band[i] + 1;
+        }
+        op.norms.assign((size_t)std::max<long>(op.nblocks, 1) * 4, 0.0);
+        op.amax.assign(nt, 0.0);
+        op.xmax.assign(nt, 0.0);
+        const size_t nel = (size_t)std::max<long>(op.nblocks, 1) * bsz;
+        MWG_CUDA(cudaMalloc(&op.d_blocks, sizeof(double) * nel));
+        MWG_CUDA(cudaMemsetAsync(op.d_blocks, 0, sizeof(double) * nel, st));
+        for (int i = 0; i < nt; i++) {
+            const int L = op.band[i];
+            if (L < 0) continue;
+            const int g0 = base[o] + i;
+            for (int l = -L; l <= L; l++) {
+                double *dn = &op.norms[(size_t)(op.off[i] + l + L) * 4];
+                const double *src = &pnr[g0][4 * std::abs(l)];
+                if (l >= 0) {
+                    for (int k = 0; k < 4; k++) dn[k] = src[k];
+                } else {  // NS(-l) = NS(l)^T swaps the (0,1) and (1,0) sub-blocks
+                    dn[0] = src[0];
+                    dn[1] = src[2];
+                    dn[2] = src[1];
+                    dn[3] = src[3];
+                }
+                for (int k = 0; k < 4; k++) {
+                    op.amax[i] = std::max(op.amax[i], dn[k]);
+                    if (k > 0) op.xmax[i] = std::max(op.xmax[i], dn[k]);
+                }
+            }
+            for (int l = 0; l <= L; l++) jobs.push_back(OpBlockJob{g0, l, L, zero[i][l], op.off[i], op.d_blocks});
+        }
     }
-    const size_t nel = (size_t)std::max<long>(nblocks, 1) * bsz;
-    MWG_CUDA(cudaMalloc(&d_blocks, sizeof(double) * nel));
-    MWG_CUDA(cudaMemsetAsync(d_blocks, 0, sizeof(double) * nel, st));
-    OpBlockJob *d_jobs = nullptr;
     if (!jobs.empty()) {
         MWG_CUDA(cudaMalloc(&d_jobs, sizeof(OpBlockJob) * jobs.size()));
         MWG_CUDA(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(OpBlockJob) * jobs.size(), cudaMemcpyHostToDevice, st));
-        k_op_blocks(K, cx.dbasis.W, d_cc, d_q, d_q + 16, d_tasks, d_jobs, (int)jobs.size(), d_blocks, st);
+        k_op_blocks(K, cx.dbasis.W, d_cc, d_q, d_q + 16, d_tasks, d_jobs, (int)jobs.size(), st);
     }
     // device copies for the reduced tiers: FP32 high part then low part per block (FP32 and
     // double-FP32 tiers), and the tensor-core tier's B operand (mw_tc05_layout.h)
-    MWG_CUDA(cudaMalloc(&d_blocks32, sizeof(float) * 2 * nel));
     const bool tc = K >= 4 && K <= KMAX;
-    if (tc) MWG_CUDA(cudaMalloc(&d_blocks_tc, sizeof(float) * tc5_b_floats(K) * (nel / bsz)));
-    k_op_convert(d_blocks, d_blocks32, tc ? d_blocks_tc : nullptr, (long)(nel / bsz), K, tc5_n(K), 2 * tc5_ks(K), st);
+    for (Oper *op : ops) {
+        const long nb = std::max<long>(op->nblocks, 1);
+        MWG_CUDA(cudaMalloc(&op->d_blocks32, sizeof(float) * 2 * (size_t)nb * bsz));
+        if (tc) MWG_CUDA(cudaMalloc(&op->d_blocks_tc, sizeof(float) * tc5_b_floats(K) * (size_t)nb));
+        k_op_convert(op->d_blocks, op->d_blocks32, tc ? op->d_blocks_tc : nullptr, nb, K, tc5_n(K), 2 * tc5_ks(K),
+                     st);
+    }
     MWG_CUDA(cudaStreamSynchronize(st));
     for (void *pp : {(void *)d_cc, (void *)d_q, (void *)d_tasks, (void *)d_nrm, (void *)d_band, (void *)d_peak,
                      (void *)d_jobs, (void *)d_head})

@@ -402,6 +402,40 @@ int mw_op_create_poisson(mw_ctx c, double prec, mw_op *out) { return op_create(c
 
 int mw_op_create_helmholtz(mw_ctx c, double mu, double prec, mw_op *out) { return op_create(c, 1, mu, prec, out); }
 
+int mw_op_create_helmholtz_batch(mw_ctx c, int n, const double *mu, double prec, mw_op *out) {
+    if (!c || n < 1 || !mu || !out || !(prec > 0.0) || prec >= 1.0) return MW_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (!(mu[i] > 0.0)) {
+            c->ctx.err = "Helmholtz operator needs mu > 0";
+            return MW_ERR_ARG;
+        }
+    std::vector<mw_op> made(n, nullptr);
+    std::vector<mwg::Oper *> ops(n);
+    for (int i = 0; i < n; i++) {
+        made[i] = new mw_op_s;
+        made[i]->op.ctx = &c->ctx;
+        made[i]->op.kind = 1;
+        made[i]->op.mu = mu[i];
+        made[i]->op.prec = prec;
+        ops[i] = &made[i]->op;
+    }
+    int rc = guard(&c->ctx, [&] { mwg::build_operators(ops, c->ctx.basis); });
+    if (rc != MW_OK) {
+        for (mw_op o : made) {
+            if (o->op.d_blocks) cudaFree(o->op.d_blocks);
+            if (o->op.d_blocks32) cudaFree(o->op.d_blocks32);
+            if (o->op.d_blocks_tc) cudaFree(o->op.d_blocks_tc);
+            delete o;
+        }
+        return rc;
+    }
+    for (int i = 0; i < n; i++) {
+        c->ctx.live++;
+        out[i] = made[i];
+    }
+    return MW_OK;
+}
+
 int mw_op_destroy(mw_op o) {
     if (!o) return MW_ERR_ARG;
     cudaSetDevice(o->op.ctx->device);

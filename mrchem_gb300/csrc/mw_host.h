@@ -133,8 +133,11 @@ struct Oper {
     float *d_blocks_tc = nullptr; // TF32 B operand of the tensor-core tier per block (mw_tc05_layout.h)
     const double *norm(int t, int s, int l) const { return &norms[(size_t)(off[t * S + s] + l + band[t * S + s]) * 4]; }
     long block_index(int t, int s, int l) const { return off[t * S + s] + l + band[t * S + s]; }
-    void build(const Basis &b);
+    void build(const Basis &b);  // build_operators({this}, b)
 };
+// several operators of one context at once (mw_basis.cpp)
+void build_operators(const std::vector<Oper *> &ops, const Basis &b);
+
 
 // Device bump allocator for per-call scratch (task lists, items, generated
 // blocks).  reset() keeps one chunk large enough for the previous peak.
@@ -318,16 +321,17 @@ struct OpBuildTask {  // one (term, scale): tau(m) = pref * (Legendre expansion 
     int root, cap;    // root scale: no early stop; cap: largest translation walked
     long nrm_off;     // first of this task's 4 (cap + 1) sub-block norms
 };
-struct OpBlockJob {  // one block pair NS(+l), NS(-l) of a task, at off + band +- l
+struct OpBlockJob {  // one block pair NS(+l), NS(-l) of a task, at blocks + (off + band +- l) blocks
     int task, l, band, zero;  // zero: bit 2g+f marks sub-block (g, f) as cut
     long off;
+    double *blocks;           // the operator's FP64 blocks
 };
 size_t op_build_smem();
 constexpr int OP_NRM_HEAD = 64;  // translations per task whose norms phase 1 also writes compactly
 void k_op_band(int K, const double *W, const double *cc, const double *gx, const double *gw, const OpBuildTask *tasks,
                int ntask, double *nrm, double *head, int *band, double *peak, cudaStream_t s);
 void k_op_blocks(int K, const double *W, const double *cc, const double *gx, const double *gw, const OpBuildTask *tasks,
-                 const OpBlockJob *jobs, int njob, double *blocks, cudaStream_t s);
+                 const OpBlockJob *jobs, int njob, cudaStream_t s);
 void k_op_convert(const double *blocks, float *b32, float *btc, long nblocks, int K, int NB, int groups,
                   cudaStream_t s);
 // FP32 shadow of whole blocks in cube order cube[Z][Y][X] (X = cx*K + ix): per block a high cube

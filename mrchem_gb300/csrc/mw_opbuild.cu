@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(OB_THREADS) op_band_kernel(int K, const double
 // phase 2: block l of task `task` (one CTA per (task, l) pair); zero: 4 bits, sub-blocks to zero
 __global__ void __launch_bounds__(OB_THREADS) op_block_kernel(int K, const double *W, const double *cc, const double *gx,
                                                               const double *gw, const OpBuildTask *tasks,
-                                                              const OpBlockJob *jobs, int njob, double *blocks) {
+                                                              const OpBlockJob *jobs, int njob) {
     extern __shared__ __align__(16) unsigned char ob_smem[];
     ObShared &S = *reinterpret_cast<ObShared *>(ob_smem);
     ob_setup(gx, gw, S);
@@ -199,8 +199,8 @@ __global__ void __launch_bounds__(OB_THREADS) op_block_kernel(int K, const doubl
         ob_tau(K, T.beta, T.pref, 2 * l, cc, S, S.t0);
         ob_tau(K, T.beta, T.pref, 2 * l + 1, cc, S, S.tp1);
         ob_ns(K, W, S);
-        double *pos = blocks + (size_t)(J.off + J.band + l) * bsz;
-        double *neg = blocks + (size_t)(J.off + J.band - l) * bsz;
+        double *pos = J.blocks + (size_t)(J.off + J.band + l) * bsz;
+        double *neg = J.blocks + (size_t)(J.off + J.band - l) * bsz;
         for (int e = threadIdx.x; e < bsz; e += blockDim.x) {
             const int r = e / K2, c = e - r * K2;
             const int g = r / K, f = c / K;
@@ -258,11 +258,11 @@ void k_op_band(int K, const double *W, const double *cc, const double *gx, const
 }
 
 void k_op_blocks(int K, const double *W, const double *cc, const double *gx, const double *gw, const OpBuildTask *tasks,
-                 const OpBlockJob *jobs, int njob, double *blocks, cudaStream_t s) {
+                 const OpBlockJob *jobs, int njob, cudaStream_t s) {
     if (njob <= 0) return;
     const int smem = (int)sizeof(ObShared);
     MWG_CUDA(cudaFuncSetAttribute(op_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    op_block_kernel<<<njob < 65535 ? njob : 65535, OB_THREADS, smem, s>>>(K, W, cc, gx, gw, tasks, jobs, njob, blocks);
+    op_block_kernel<<<njob < 65535 ? njob : 65535, OB_THREADS, smem, s>>>(K, W, cc, gx, gw, tasks, jobs, njob);
     MWG_CUDA(cudaGetLastError());
 }
 

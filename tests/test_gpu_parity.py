@@ -87,6 +87,26 @@ def test_poisson_operator_matches_oracle(engine, oracle, k7):
                 assert np.allclose(n1, n2, rtol=1e-12, atol=1e-12 * scale)
 
 
+def test_helmholtz_batch_operators_identical(engine, k7):
+    # operators built together are the operators built one by one, bit for bit
+    mra, _ = k7
+    mus = [0.5, 1.1, 1.9]
+    one = [engine.HelmholtzOperator(mra, m, 1e-5) for m in mus]
+    many = engine.HelmholtzOperator.batch(mra, mus, 1e-5)
+    for p, q in zip(one, many):
+        c1, a1 = p.terms()
+        c2, a2 = q.terms()
+        assert np.array_equal(c1, c2) and np.array_equal(a1, a2)
+        for t in range(0, p.nterms, 5):
+            for n in (-5, -1, 2, 6):
+                L = p.band(t, n)
+                assert L == q.band(t, n)
+                for l in {-L, 0, L} if L >= 0 else ():
+                    b1, n1 = p.block(t, n, l)
+                    b2, n2 = q.block(t, n, l)
+                    assert np.array_equal(b1, b2) and np.array_equal(n1, n2)
+
+
 def test_projection_matches_oracle(engine, oracle, k7):
     mra, omra = k7
     t = engine.project(1e-6, engine.FunctionTree(mra), GAUSS4)
