@@ -317,6 +317,11 @@ def run(args):
     mra.set_overlap(False)
     serial_ms, st_ser = timed("mixed", 1)
     mra.set_overlap(True)
+    # the same mixed step with the enumeration, screening and item lists on the host (OpenMP)
+    # instead of the GPU; the item lists and results are identical
+    mra.set_screening("host")
+    host_scr_ms, st_hs = timed("mixed", 3)
+    mra.set_screening("gpu")
     fp64_tf = mra.probe_fma_peak(True)
     fp32_tf = mra.probe_fma_peak(False)
     tf32_tf = mra.probe_mma_peak("tc05")          # tcgen05 TF32, M128 N256 K8: the device's dense rate
@@ -386,6 +391,9 @@ def run(args):
                                       "from one step without overlap"},
         "no_overlap": {"value": st_ser["out_nodes"] * world / (serial_ms / 1e3), "unit": "nodes/s",
                        "ms_per_step": serial_ms, "policy": "job groups not pipelined (mw_ctx_set_overlap 0)"},
+        "host_screening": {"value": st_hs["out_nodes"] * world / (host_scr_ms / 1e3), "unit": "nodes/s",
+                           "ms_per_step": host_scr_ms,
+                           "policy": "enumeration, screening and item lists on the host cores (mw_ctx_set_screening 0)"},
         "gpu_launches": int(st["launches"]),
         "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": dict(roofs[dominant], tier=dominant),

@@ -114,6 +114,14 @@ int mw_ctx_synchronize(mw_ctx ctx);
 int mw_ctx_set_overlap(mw_ctx ctx, int on);
 /* The number of job groups (1..8) batched applies split into; mw_ctx_set_overlap sets 4 or 1. */
 int mw_ctx_set_groups(mw_ctx ctx, int n);
+/* Where applies enumerate their candidate items, screen them with the norm-product bound and
+ * build the per-tier item lists: on = 1 on the GPU (the default), on = 0 on the host (OpenMP over
+ * output nodes).  Both give the same items in the same order, so results are bit-identical.  Levels
+ * more than 20 scales below the root and operators with bands above 32767 are screened on the
+ * host either way.
+ * Replaces the screening inside mrcpp::apply (CoulombPotential.cpp:131, HelmholtzVector.cpp:149),
+ * which MRCPP runs on the host. */
+int mw_ctx_set_screening(mw_ctx ctx, int on);
 
 /* ---- trees (replaces FunctionTree<3>, src/qmfunctions/Orbital.h:51) ---- */
 int mw_tree_create(mw_ctx ctx, mw_tree *out);

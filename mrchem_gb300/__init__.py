@@ -74,7 +74,7 @@ EXPORTS = [
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
     "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
     "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
-    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap", "mw_ctx_set_groups", "mw_apply_batch_autotune", "mw_op_create_helmholtz_batch",
+    "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap", "mw_ctx_set_groups", "mw_ctx_set_screening", "mw_apply_batch_autotune", "mw_op_create_helmholtz_batch",
     "mw_tree_upload_batch", "mw_tree_download_batch", "mw_pin_host", "mw_unpin_host",
 ]
 
@@ -98,6 +98,7 @@ def load_library(path=None):
         "mw_ctx_synchronize": [P],
         "mw_ctx_set_overlap": [P, I],
         "mw_ctx_set_groups": [P, I],
+        "mw_ctx_set_screening": [P, I],
         "mw_tree_create": [P, pp],
         "mw_tree_destroy": [P],
         "mw_tree_nnodes": [P, ip],
@@ -227,6 +228,13 @@ class MultiResolutionAnalysis:
     def set_groups(self, n):
         """Number of pipelined job groups (1..8) that batched applies split into (default 4)."""
         _check(_lib.mw_ctx_set_groups(self.ptr, int(n)), self.ptr)
+
+    def set_screening(self, where="gpu"):
+        """Where applies enumerate, screen and list their items: "gpu" (the default) or "host"
+        (OpenMP).  Both give the same items in the same order (bit-identical results)."""
+        if where not in ("host", "gpu"):
+            raise ValueError("screening must be 'host' or 'gpu'")
+        _check(_lib.mw_ctx_set_screening(self.ptr, 1 if where == "gpu" else 0), self.ptr)
 
     def probe_fma_peak(self, fp64=True):
         """Measured FMA throughput of this GPU in TFLOP/s (FP64 or FP32 CUDA cores)."""

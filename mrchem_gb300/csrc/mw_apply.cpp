@@ -272,8 +272,16 @@ struct LevelItems {
 
 // tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores, 3 double-FP32.  Returns the pinned host copy of the
 // launch's status word (read it after the stream has been synchronised), or nullptr.
+// item arrays written on the GPU by the screening kernels (mw_screen.cu): the tiers one after the
+// other, tier k from base[k]
+struct DevItems {
+    const void **in = nullptr, **ax = nullptr, **ay = nullptr, **az = nullptr;
+    double *coef = nullptr;
+    long long base[NTIER] = {0, 0, 0, 0};
+};
+
 int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, int tier, long long chunk,
-                 mw_stats &st) {
+                 mw_stats &st, const DevItems *dv = nullptr) {
     const int nn = (int)li.nodes;
     const size_t ni = (size_t)li.items;
     if (nn == 0) return nullptr;
@@ -337,11 +345,12 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     pk.add(outp.data(), outp.size() * sizeof(double *));
     pk.add(beg.data(), beg.size() * sizeof(long long));
     pk.add(end.data(), end.size() * sizeof(long long));
-    pk.add(li.in.data(), ni * sizeof(void *));
-    pk.add(li.ax.data(), ni * sizeof(void *));
-    pk.add(li.ay.data(), ni * sizeof(void *));
-    pk.add(li.az.data(), ni * sizeof(void *));
-    pk.add(li.coef.data(), ni * sizeof(double));
+    const size_t nh = dv ? 0 : ni;  // item arrays shipped from the host (none when the GPU wrote them)
+    pk.add(li.in.data(), nh * sizeof(void *));
+    pk.add(li.ax.data(), nh * sizeof(void *));
+    pk.add(li.ay.data(), nh * sizeof(void *));
+    pk.add(li.az.data(), nh * sizeof(void *));
+    pk.add(li.coef.data(), nh * sizeof(double));
     pk.add(red.data(), red.size() * sizeof(ReduceTask));
     pk.add(redof.data(), redof.size() * sizeof(int));
     // the task counter, the status word and the chunk counters start at zero: they travel with the
@@ -363,6 +372,14 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     L.ay = (const void *const *)pk.ptr(5);
     L.az = (const void *const *)pk.ptr(6);
     L.coef = (const double *)pk.ptr(7);
+    if (dv) {
+        const long long b0 = dv->base[tier];
+        L.in = (const void *const *)(dv->in + b0);
+        L.ax = (const void *const *)(dv->ax + b0);
+        L.ay = (const void *const *)(dv->ay + b0);
+        L.az = (const void *const *)(dv->az + b0);
+        L.coef = dv->coef + b0;
+    }
     L.counter = counter;
     L.status = counter + 1;
     if (!red.empty()) {
@@ -386,6 +403,456 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
         }
     }
     return hs;
+}
+
+// runs host code with the context's stream pointing at another stream
+struct StreamSwap {
+    Ctx &c;
+    cudaStream_t saved;
+    StreamSwap(Ctx &c_, cudaStream_t s) : c(c_), saved(c_.stream) { c.stream = s; }
+    ~StreamSwap() { c.stream = saved; }
+};
+
+// ------------------------------------------------------------------ screening on the GPU
+// Per-apply tables of the GPU screening (mw_screen.cu): each operator's bands, offsets and
+// sub-block norms (uploaded once per operator), and per job the input tree's hash table and the
+// norms the host screens with.
+struct DevScreen {
+    bool on = false;
+    std::vector<double> op_max;  // per job: its operator's largest sub-block norm
+    int levels = 0;  // levels 0 .. levels-1 are screened on the GPU
+    int maxT = 0;
+    ScreenJob *djobs = nullptr;
+    cudaEvent_t ev_counts = nullptr;  // the write pass's per-node tier counts have reached the host
+};
+
+// layout of Oper::d_screen: int band[TS], int off[TS] | double amax[TS], xmax[TS], c[T], norms[4 nb]
+// | float amax32[TS], xmax32[TS], norms32[4 nb]   (TS = T * S, nb = blocks)
+struct OperScreenLayout {
+    size_t TS, nb, ib, db, fb;
+    explicit OperScreenLayout(const Oper &op) {
+        TS = (size_t)op.T * op.S;
+        nb = (size_t)std::max<long>(op.nblocks, 1);
+        ib = ((2 * TS * sizeof(int)) + 255) & ~size_t(255);
+        db = ((sizeof(double) * (2 * TS + (size_t)op.T + 4 * nb)) + 255) & ~size_t(255);
+        fb = sizeof(float) * (2 * TS + 4 * nb);
+    }
+};
+
+bool oper_screen_tables(Oper &op) {
+    if (op.d_screen) return true;
+    const OperScreenLayout ly(op);
+    const size_t TS = ly.TS;
+    for (size_t i = 0; i < TS; i++)
+        if (op.band[i] > 32767 || op.off[i] > 0x3fffffffL) return false;
+    if (op.nblocks > 0x3fffffffL) return false;
+    std::vector<char> h(ly.ib + ly.db + ly.fb, 0);
+    int *iv = (int *)h.data();
+    double *dd = (double *)(h.data() + ly.ib);
+    float *ff = (float *)(h.data() + ly.ib + ly.db);
+    for (size_t i = 0; i < TS; i++) {
+        iv[i] = op.band[i];
+        iv[TS + i] = (int)op.off[i];
+        dd[i] = op.amax[i];
+        dd[TS + i] = op.xmax[i];
+        ff[i] = (float)op.amax[i];
+        ff[TS + i] = (float)op.xmax[i];
+    }
+    for (int t = 0; t < op.T; t++) dd[2 * TS + t] = op.c[t];
+    for (size_t i = 0; i < op.norms.size(); i++) {
+        dd[2 * TS + op.T + i] = op.norms[i];
+        ff[2 * TS + i] = (float)op.norms[i];
+    }
+    MWG_CUDA(cudaMalloc(&op.d_screen, h.size()));
+    MWG_CUDA(cudaMemcpy(op.d_screen, h.data(), h.size(), cudaMemcpyHostToDevice));
+    return true;
+}
+
+ScreenOp oper_screen_view(const Oper &op) {
+    const OperScreenLayout ly(op);
+    const size_t TS = ly.TS;
+    const int *iv = (const int *)op.d_screen;
+    const double *dd = (const double *)((const char *)op.d_screen + ly.ib);
+    const float *ff = (const float *)((const char *)op.d_screen + ly.ib + ly.db);
+    ScreenOp so;
+    so.band = iv;
+    so.off = iv + TS;
+    so.amax = dd;
+    so.xmax = dd + TS;
+    so.c = dd + 2 * TS;
+    so.norms = dd + 2 * TS + op.T;
+    so.amax32 = ff;
+    so.xmax32 = ff + TS;
+    so.norms32 = ff + 2 * TS;
+    so.b64 = op.d_blocks;
+    so.b32 = op.d_blocks32;
+    so.btc = op.d_blocks_tc;
+    so.T = op.T;
+    so.S = op.S;
+    return so;
+}
+
+// the largest sub-block norm of an operator (the FP32 estimates need it well inside FP32's range)
+double oper_norm_max(const Oper &op) {
+    double m = 0.0;
+    for (double v : op.amax) m = std::max(m, v);
+    return m;
+}
+
+// Builds the per-apply tables on the context's stream; false when an operator falls outside what
+// the kernels encode (bands above 32767), and the host screens instead.
+bool screen_setup(Ctx &ctx, std::vector<ApplyJob> &jobs, DevScreen &ds) {
+    const Basis &b = ctx.basis;
+    // levels whose translations fit the generation tables' 21-bit fields (deeper levels, about
+    // 20 scales below the root, are screened on the host)
+    ds.levels = 0;
+    while (ds.levels < 40) {
+        bool fits = true;
+        for (int d = 0; d < 3; d++) fits &= ((long)b.boxes[d] << ds.levels) < (1L << 21);
+        if (!fits) break;
+        ds.levels++;
+    }
+    for (ApplyJob &job : jobs)
+        if (!oper_screen_tables(*job.op)) return false;
+    // one hash table and norm copy per distinct input tree
+    std::vector<const Tree *> trees;
+    std::unordered_map<const Tree *, int> tix;
+    for (ApplyJob &job : jobs)
+        if (tix.emplace(job.inp, (int)trees.size()).second) trees.push_back(job.inp);
+    std::vector<size_t> cap(trees.size()), off(trees.size() + 1, 0);
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    for (size_t i = 0; i < trees.size(); i++) {
+        size_t c = 64;
+        while (c < 2 * (size_t)trees[i]->nn()) c <<= 1;
+        cap[i] = c;
+        off[i + 1] = off[i] + al(c * sizeof(int4)) + al(c * sizeof(int)) + al(sizeof(double) * 9 * trees[i]->nn()) +
+                     al(sizeof(float) * 9 * trees[i]->nn());
+    }
+    const size_t jb = al(sizeof(ScreenJob) * jobs.size());
+    const size_t total = off.back() + jb;
+    char *h = (char *)ctx.sarena.halloc(total);
+    char *d = (char *)ctx.sarena.alloc(total);
+    std::vector<ScreenJob> sj(jobs.size());
+    for (size_t i = 0; i < trees.size(); i++) {
+        const Tree &t = *trees[i];
+        const size_t c = cap[i];
+        int4 *hk = (int4 *)(h + off[i]);
+        int *hv = (int *)(h + off[i] + al(c * sizeof(int4)));
+        double *cn = (double *)(h + off[i] + al(c * sizeof(int4)) + al(c * sizeof(int)));
+        for (size_t e = 0; e < c; e++) {
+            hk[e] = make_int4(HASH_EMPTY, 0, 0, 0);
+            hv[e] = -1;
+        }
+        for (int n = 0; n < t.nn(); n++) {
+            const NodeInfo &ni = t.nodes[n];
+            unsigned e = key_hash(ni.n, ni.l[0], ni.l[1], ni.l[2]) & (unsigned)(c - 1);
+            while (hk[e].x != HASH_EMPTY) e = (e + 1) & (unsigned)(c - 1);
+            hk[e] = make_int4(ni.n, ni.l[0], ni.l[1], ni.l[2]);
+            hv[e] = n;
+        }
+        std::memcpy(cn, t.cn.data(), sizeof(double) * 8 * t.nn());
+        for (int n = 0; n < t.nn(); n++) cn[8 * (size_t)t.nn() + n] = block_norm8(&t.cn[8 * (size_t)n]);
+        float *cn32 = (float *)((char *)cn + al(sizeof(double) * 9 * t.nn()));
+        for (size_t e = 0; e < 9 * (size_t)t.nn(); e++) cn32[e] = (float)cn[e];
+    }
+    for (size_t j = 0; j < jobs.size(); j++) {
+        const int i = tix[jobs[j].inp];
+        const Tree &t = *trees[i];
+        const size_t c = cap[i];
+        ScreenJob &J = sj[j];
+        J.op = oper_screen_view(*jobs[j].op);
+        J.hkey = (const int4 *)(d + off[i]);
+        J.hval = (const int *)(d + off[i] + al(c * sizeof(int4)));
+        J.hmask = (int)(c - 1);
+        J.pad = 0;
+        J.cn = (const double *)(d + off[i] + al(c * sizeof(int4)) + al(c * sizeof(int)));
+        J.bn = J.cn + 8 * (size_t)t.nn();
+        J.cn32 = (const float *)((const char *)J.cn + al(sizeof(double) * 9 * t.nn()));
+        J.bn32 = J.cn32 + 8 * (size_t)t.nn();
+        ds.op_max.push_back(oper_norm_max(*jobs[j].op));
+        J.in64 = t.d_coefs;
+        J.in32 = t.d_coefs32;
+        J.intc = t.d_coefs_tc;
+        ds.maxT = std::max(ds.maxT, jobs[j].op->T);
+    }
+    std::memcpy(h + off.back(), sj.data(), sizeof(ScreenJob) * sj.size());
+    MWG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, ctx.stream));
+    ds.djobs = (ScreenJob *)(d + off.back());
+    if (!ds.ev_counts) MWG_CUDA(cudaEventCreateWithFlags(&ds.ev_counts, cudaEventDisableTiming));
+    ds.on = true;
+    return true;
+}
+
+struct TierRule {  // the apply's precision mode, as the tier choice reads it
+    bool mixed, near_fp64, df_only, dfp, tensor;
+};
+
+// One level of a job group screened on the GPU (mw_screen.cu).  The walk, the generation of
+// missing inputs, the exact screening, the tiers and the item arrays run on the high-priority
+// stream; the host reads back two small arrays (per-node candidate counts, then per-node tier
+// counts), from which it sizes the buffers and builds each tier's node list exactly as the host
+// screening does.  The group's stream waits for the item arrays with an event.
+// the walk kernels' (t, lz) rows at a scale: the most over the group's operators
+int level_zrows(const std::vector<JobState *> &jp, int sidx) {
+    int zmax = 1;
+    for (const JobState *sp : jp) {
+        const Oper &op = *sp->job->op;
+        int z = 0;
+        for (int t = 0; t < op.T; t++) {
+            const int L = op.band[t * op.S + sidx];
+            if (L >= 0) z += 2 * L + 1;
+        }
+        zmax = std::max(zmax, z);
+    }
+    return zmax;
+}
+constexpr size_t SCREEN_SMEM_MAX = 96 * 1024;  // larger walks (very wide bands) are screened on the host
+
+void screen_level_gpu(Ctx &ctx, Arena &ar, DevScreen &ds, const std::vector<JobState *> &jp,
+                      const std::vector<int> &jglob, int level, int zmax, const TierRule &rule, LevelItems *lt,
+                      DevItems &dv, mw_stats &st, double &t_enum, double &t_gen, double &t_items) {
+    const Basis &b = ctx.basis;
+    const int K = b.K, bs = b.bs, bsz = 4 * K * K;
+    const double K4 = (double)K * K * K * K;
+    const int n = b.n0 + level, sidx = level;
+    const bool root = level == 0;
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point c) {
+        return std::chrono::duration<double, std::milli>(c - a).count();
+    };
+    const auto tA = now();
+    cudaStream_t gstream = ctx.stream;
+    // node records in the host's order (jobs of the group, then their work lists)
+    std::vector<ScreenNode> nodes;
+    std::vector<double *> outb;
+    std::vector<long> gcap(jp.size(), 0);
+    long gtot = 0;
+    for (size_t j = 0; j < jp.size(); j++) {
+        JobState &s = *jp[j];
+        long c = 256;
+        while (c < 16 * (long)s.work.size()) c <<= 1;
+        gcap[j] = c;
+        const double fm = BOUND_PRUNE * s.fmax_at(sidx);
+        const double base = SCREEN_FAC * split_thr(s.job->prec, s.R, n);
+        for (size_t w = 0; w < s.work.size(); w++) {
+            ScreenNode nd;
+            const double wg = s.wgt[w], wgc = std::max(wg, 1e-300);
+            nd.thr = root ? 0.0 : (wg > 0.0 ? base / wg : 0.0);
+            nd.thr2 = root ? 0.0 : base / wgc;
+            nd.tthr = !root ? nd.thr2
+                      : s.job->abs_prec ? SCREEN_FAC * split_thr(s.job->prec, 1.0, n) / wgc
+                                        : -1.0;
+            nd.fm = fm;
+            nd.job = jglob[j];
+            const NodeInfo &o = s.job->out->nodes[s.work[w]];
+            for (int d = 0; d < 3; d++) nd.l[d] = o.l[d];
+            nd.flags = ((!root && wg <= 0.0) ? 1 : 0) | ((!root || (s.job->abs_prec && s.job->prec_trees.empty())) ? 2 : 0);
+            nd.gtab = (int)gtot;
+            nd.gmask = (int)(gcap[j] - 1);
+            // FP32 estimates decide clear cases when every factor of a bound is at most 1e6 (input
+            // norms are at most fm) and the thresholds are at least 1e-14: then FP32 rounding (2e-6
+            // relative) and products flushed below FP32's range (< 1e-24 in all) stay well inside
+            // the 1e-4 relative bands, and FP64 decides inside them
+            constexpr double BAND = 1e-4, BIG = 1e6, SMALL = 1e-14;
+            const bool fast = fm <= BIG && ds.op_max[nd.job] <= BIG &&
+                              (root || (nd.thr >= SMALL && nd.thr2 >= SMALL)) &&
+                              (nd.tthr < 0.0 || nd.tthr >= SMALL);
+            if (fast) nd.flags |= 4;
+            nd.thr_lo = (float)(nd.thr * (1.0 - BAND));
+            nd.thr_hi = (float)(nd.thr * (1.0 + BAND));
+            nd.thr2_lo = (float)(nd.thr2 * (1.0 - BAND));
+            nd.thr2_hi = (float)(nd.thr2 * (1.0 + BAND));
+            const double tb[3] = {TIER_TF32, TIER_FP64, TIER_DF};
+            for (int k = 0; k < 3; k++) {
+                const double B = nd.tthr >= 0.0 ? tb[k] * nd.tthr : 0.0;
+                nd.tier_lo[k] = (float)(B * (1.0 - BAND));
+                nd.tier_hi[k] = (float)(B * (1.0 + BAND));
+            }
+            nd.fm32 = (float)fm;
+            nd.prune32 = (float)(nd.thr * (1.0 - BAND));
+            nodes.push_back(nd);
+            outb.push_back(s.job->out->block(s.work[w]));
+        }
+        gtot += gcap[j];
+    }
+    const int NN = (int)nodes.size();
+    ScreenLevel P{};
+    P.jobs = ds.djobs;
+    P.nn = NN;
+    P.n = n;
+    P.sidx = sidx;
+    P.root = root ? 1 : 0;
+    P.n0 = b.n0;
+    P.bs = bs;
+    P.bsz = bsz;
+    for (int d = 0; d < 3; d++) {
+        P.lo[d] = (int)((long)b.corner[d] * (1L << (n - b.n0)));
+        P.hi[d] = (int)((long)(b.corner[d] + b.boxes[d]) * (1L << (n - b.n0)));
+    }
+    P.mixed = rule.mixed;
+    P.near_fp64 = rule.near_fp64;
+    P.df_only = rule.df_only;
+    P.dfp = rule.dfp;
+    P.tensor = rule.tensor;
+    P.tier_fp64 = TIER_FP64;
+    P.tier_tf32 = TIER_TF32;
+    P.tier_df = TIER_DF;
+    P.tx = tc5_x_floats(K);
+    P.tb = tc5_b_floats(K);
+    // walk 1: candidate counts and generation requests (tables grown and the walk repeated if a
+    // job's generation table fills up)
+    int *hc = nullptr;
+    int ngen = 0;
+    {
+        StreamSwap fast(ctx, ctx.fast);
+        for (int attempt = 0;; attempt++) {
+            if (attempt == 3) throw Error(MW_ERR_STATE, "apply: generation tables of the GPU screening overflowed");
+            if (attempt > 0) {
+                gtot = 0;
+                for (size_t j = 0, q = 0; j < jp.size(); j++) {
+                    gcap[j] *= 8;
+                    for (size_t w = 0; w < jp[j]->work.size(); w++, q++) {
+                        nodes[q].gtab = (int)gtot;
+                        nodes[q].gmask = (int)(gcap[j] - 1);
+                    }
+                    gtot += gcap[j];
+                }
+            }
+            std::vector<unsigned long long> zeros((size_t)gtot + 1, 0ull);  // keys, then the counter and flag
+            Packer pk;
+            pk.add(nodes.data(), sizeof(ScreenNode) * NN);
+            pk.add(zeros.data(), sizeof(unsigned long long) * zeros.size());
+            pk.ship(ctx, ar);
+            P.nodes = (const ScreenNode *)pk.ptr(0);
+            P.gkey = (unsigned long long *)pk.ptr(1);
+            P.gen_cnt = (int *)(P.gkey + gtot);
+            P.overflow = P.gen_cnt + 1;
+            P.gval = (int *)ar.alloc(sizeof(int) * (size_t)gtot);
+            P.gen_cap = (int)gtot;
+            P.gen_info = (int *)ar.alloc(sizeof(int) * 6 * (size_t)gtot);
+            P.cnt = (int *)ar.alloc(sizeof(int) * (size_t)NN);
+            k_screen_count(P, ds.maxT, zmax, ctx.stream);
+            st.launches++;
+            hc = (int *)ar.halloc(sizeof(int) * ((size_t)NN + 2));
+            MWG_CUDA(cudaMemcpyAsync(hc, P.cnt, sizeof(int) * NN, cudaMemcpyDeviceToHost, ctx.stream));
+            MWG_CUDA(cudaMemcpyAsync(hc + NN, P.gen_cnt, sizeof(int) * 2, cudaMemcpyDeviceToHost, ctx.stream));
+            MWG_CUDA(cudaStreamSynchronize(ctx.stream));
+            if (hc[NN + 1] == 0) break;
+        }
+        ngen = hc[NN];
+    }
+    const auto tB = now();
+    t_enum += ms(tA, tB);
+    // buffers sized by the counts; generation of the missing inputs
+    std::vector<long long> coff(NN);
+    long long ctot = 0;
+    for (int q = 0; q < NN; q++) {
+        coff[q] = ctot;
+        ctot += hc[q];
+    }
+    const size_t cap = (size_t)std::max<long long>(ctot, 1);
+    P.cand = (ScreenCand *)ar.alloc(sizeof(ScreenCand) * cap);
+    dv.in = (const void **)ar.alloc(sizeof(void *) * cap);
+    dv.ax = (const void **)ar.alloc(sizeof(void *) * cap);
+    dv.ay = (const void **)ar.alloc(sizeof(void *) * cap);
+    dv.az = (const void **)ar.alloc(sizeof(void *) * cap);
+    dv.coef = (double *)ar.alloc(sizeof(double) * cap);
+    P.in = dv.in;
+    P.ax = dv.ax;
+    P.ay = dv.ay;
+    P.az = dv.az;
+    P.coef = dv.coef;
+    P.tcnt = (int *)ar.alloc(sizeof(int) * 8 * (size_t)NN);
+    P.tier_off = (long long *)ar.alloc(sizeof(long long) * 4 * (size_t)NN);
+    P.tier_tot = (long long *)ar.alloc(sizeof(long long) * 4);
+    const size_t ng = (size_t)std::max(ngen, 1);
+    P.gcn = (double *)ar.alloc(sizeof(double) * 8 * ng);
+    P.gcn32 = (float *)ar.alloc(sizeof(float) * 8 * ng);
+    P.g64 = (const double *)ar.alloc(sizeof(double) * (size_t)bs * ng);
+    P.g32 = rule.mixed ? (const float *)ar.alloc(sizeof(float) * 2 * (size_t)bs * ng) : nullptr;
+    P.gtc = rule.tensor ? (const float *)ar.alloc(sizeof(float) * P.tx * ng) : nullptr;
+    int *hs = (int *)ar.halloc(sizeof(int) * (8 * (size_t)NN + 1));
+    {
+        StreamSwap fast(ctx, ctx.fast);
+        Packer pk;
+        pk.add(coff.data(), sizeof(long long) * NN);
+        pk.ship(ctx, ar);
+        P.cand_off = (const long long *)pk.ptr(0);
+        if (ngen > 0) {
+            GenTask *tasks = (GenTask *)ar.alloc(sizeof(GenTask) * (size_t)ngen);
+            k_screen_gen_tasks(P, tasks, ngen, ctx.stream);
+            const int ggrid = std::min(ngen, 4 * std::max(ctx.nsm, 1));
+            double *gscratch = (double *)ar.alloc(sizeof(double) * generate_scratch_doubles(K) * ggrid);
+            k_generate(ctx.dbasis, tasks, ngen, gscratch, ggrid, ctx.stream);
+            k_screen_gen_norms32(P, ngen, ctx.stream);
+            st.launches += 3;
+            st.generated += ngen;
+            if (rule.mixed) {
+                k_to_fp32_cube(P.g64, const_cast<float *>(P.g32), (size_t)ngen, K, ctx.stream);
+                st.launches++;
+                if (rule.tensor) {
+                    k_to_tc_x(P.g32, const_cast<float *>(P.gtc), (size_t)ngen, K, ctx.stream);
+                    st.launches++;
+                }
+            }
+        }
+        const auto tC = now();
+        t_gen += ms(tB, tC);
+        // walk 2: items with their tiers, per-node tier counts back to the host, then the item arrays
+        k_screen_write(P, ds.maxT, zmax, ctx.stream);
+        st.launches += 2;
+        MWG_CUDA(cudaMemcpyAsync(hs, P.tcnt, sizeof(int) * 8 * NN, cudaMemcpyDeviceToHost, ctx.stream));
+        MWG_CUDA(cudaMemcpyAsync(hs + 8 * NN, P.overflow, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+        MWG_CUDA(cudaEventRecord(ds.ev_counts, ctx.stream));
+        k_screen_fill(P, ctx.stream);
+        st.launches++;
+        MWG_CUDA(cudaEventRecord(ctx.fast_done, ctx.stream));
+    }
+    MWG_CUDA(cudaStreamWaitEvent(gstream, ctx.fast_done, 0));
+    MWG_CUDA(cudaEventSynchronize(ds.ev_counts));
+    if (hs[8 * NN] != 0) throw Error(MW_ERR_STATE, "apply: a generated input was missing from the GPU screening's tables");
+    const auto tD = now();
+    // each tier's node list in node order, as the host screening builds it
+    long long tot[NTIER] = {0, 0, 0, 0}, pairs[NTIER] = {0, 0, 0, 0};
+    long nnt[NTIER] = {0, 0, 0, 0};
+    for (int q = 0; q < NN; q++)
+        for (int k = 0; k < NTIER; k++) {
+            if (hs[8 * q + k] > 0) nnt[k]++;
+            tot[k] += hs[8 * q + k];
+            pairs[k] += hs[8 * q + 4 + k];
+        }
+    long long base = 0;
+    for (int k = 0; k < NTIER; k++) {
+        dv.base[k] = base;
+        base += tot[k];
+        LevelItems &T = lt[k];
+        T.nodes = nnt[k];
+        T.items = tot[k];
+        if ((long)T.out.size() < nnt[k]) T.out.resize(nnt[k]);
+        if ((long)T.begin.size() < nnt[k] + 1) T.begin.resize(nnt[k] + 1);
+        T.begin[0] = 0;
+        long slot = 0;
+        long long run = 0;
+        for (int q = 0; q < NN; q++) {
+            const int c = hs[8 * q + k];
+            if (c <= 0) continue;
+            run += c;
+            T.out[slot] = outb[q];
+            T.begin[++slot] = run;
+        }
+    }
+    st.items += tot[0] + tot[1] + tot[2] + tot[3];
+    st.items_fp64 += tot[0];
+    st.items_fp32 += tot[1];
+    st.items_tf32 += tot[2];
+    st.items_df += tot[3];
+    st.flops += 6.0 * K4 * (double)(pairs[0] + pairs[1] + pairs[2] + pairs[3]);
+    st.flops_issued += 96.0 * K4 * (double)(tot[0] + tot[1] + tot[2] + tot[3]);
+    st.flops_fp64 += 6.0 * K4 * (double)pairs[0];
+    st.flops_fp32 += 6.0 * K4 * (double)pairs[1];
+    st.flops_tf32 += 6.0 * K4 * (double)pairs[2];
+    st.flops_df += 6.0 * K4 * (double)pairs[3];
+    t_items += ms(tD, now());
 }
 
 void check_status(const int *hs) {
@@ -453,6 +920,13 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         if (fixed_grid) max_levels = std::max(max_levels, job.out->max_scale() - b.n0 + 1);
         s.R = 1.0;
     }
+    // screening on the GPU (mw_screen.cu) when the context asks for it and the jobs fit its tables
+    const TierRule rule{mixed, near_fp64, df_only, dfp, tensor};
+    DevScreen ds;
+    if (ctx.screening == 1) {
+        ctx.sarena.reset();
+        screen_setup(ctx, jobs, ds);
+    }
     // fixed grid: per level, the output's nodes at that scale
     auto fixed_level_nodes = [&](JobState &s, int n) {
         s.work.clear();
@@ -474,13 +948,6 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         cudaEvent_t ev[NTIER + 1];
         std::vector<int *> status;  // pinned copies of the launches' status words
         std::vector<double *> h_cn;  // pinned staging of each job's component norms
-    };
-    // runs the host side with the context's stream pointing at the group's stream
-    struct StreamSwap {
-        Ctx &c;
-        cudaStream_t saved;
-        StreamSwap(Ctx &c_, cudaStream_t s) : c(c_), saved(c_.stream) { c.stream = s; }
-        ~StreamSwap() { c.stream = saved; }
     };
     // launch settings: the autotuner's for this (order, jobs, mode) if it ran, else the context's
     Ctx::Tuning tune;
@@ -558,219 +1025,228 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     s.wgt[w] = prec_weight(s.job->prec_trees, n, s.job->out->nodes[s.work[w]].l);
             s.cand.assign(s.work.size(), {});
         }
-        // phase A: candidate enumeration (host, all the group's nodes in parallel)
-        auto tA = std::chrono::steady_clock::now();
-        std::vector<std::pair<int, int>> flat;
-        for (size_t j = 0; j < jp.size(); j++)
-            for (size_t w = 0; w < jp[j]->work.size(); w++) flat.push_back({(int)j, (int)w});
-#pragma omp parallel
-        {
-            LookupCache cache;
-#pragma omp for schedule(dynamic, 4)
-            for (long q = 0; q < (long)flat.size(); q++) {
-                JobState &s = *jp[flat[q].first];
-                int w = flat[q].second;
-                if (!root && s.wgt[w] <= 0.0) {
-                    s.cand[w].clear();
-                    continue;
-                }
-                double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / s.wgt[w];
-                enumerate_node(s, w, sidx, root, thr, cache);
-            }
-        }
-        auto tB = std::chrono::steady_clock::now();
-        st.host_enum_ms += std::chrono::duration<double, std::milli>(tB - tA).count();
-        // phase B: generated input nodes (each job has its own set: jobs in parallel, each in order)
-#pragma omp parallel for schedule(dynamic, 1)
-        for (long j = 0; j < (long)jp.size(); j++) {
-            JobState &s = *jp[j];
-            s.gens.clear();
-            for (size_t w = 0; w < s.work.size(); w++) {
-                const NodeInfo &o = s.job->out->nodes[s.work[w]];
-                for (Cand &c : s.cand[w]) {
-                    if (!c.gen) continue;
-                    int p[3] = {o.l[0] - c.lx, o.l[1] - c.ly, o.l[2] - c.lz};
-                    c.src = s.gens.request(*s.job->inp, n, p, c.src);
+        LevelItems *lt = G.lt;
+        DevItems dv;
+        const int zmax = ds.on ? level_zrows(jp, sidx) : 0;
+        const bool dscreen = ds.on && level < ds.levels && screen_smem(ds.maxT, zmax) <= SCREEN_SMEM_MAX;
+        if (dscreen) {
+            screen_level_gpu(ctx, ar, ds, jp, G.jobs, level, zmax, rule, G.lt, dv, st, st.host_enum_ms,
+                             st.host_gen_ms, st.host_items_ms);
+        } else {
+            // phase A: candidate enumeration (host, all the group's nodes in parallel)
+            auto tA = std::chrono::steady_clock::now();
+            std::vector<std::pair<int, int>> flat;
+            for (size_t j = 0; j < jp.size(); j++)
+                for (size_t w = 0; w < jp[j]->work.size(); w++) flat.push_back({(int)j, (int)w});
+    #pragma omp parallel
+            {
+                LookupCache cache;
+    #pragma omp for schedule(dynamic, 4)
+                for (long q = 0; q < (long)flat.size(); q++) {
+                    JobState &s = *jp[flat[q].first];
+                    int w = flat[q].second;
+                    if (!root && s.wgt[w] <= 0.0) {
+                        s.cand[w].clear();
+                        continue;
+                    }
+                    double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / s.wgt[w];
+                    enumerate_node(s, w, sidx, root, thr, cache);
                 }
             }
-        }
-        {
-            // one generation launch for the group; the blocks are contiguous in job order
-            std::vector<std::pair<GenSet *, const Tree *>> sets;
-            size_t total = 0;
-            for (JobState *sp : jp) {
-                sets.push_back({&sp->gens, sp->job->inp});
-                total += sp->gens.keys.size();
+            auto tB = std::chrono::steady_clock::now();
+            st.host_enum_ms += std::chrono::duration<double, std::milli>(tB - tA).count();
+            // phase B: generated input nodes (each job has its own set: jobs in parallel, each in order)
+    #pragma omp parallel for schedule(dynamic, 1)
+            for (long j = 0; j < (long)jp.size(); j++) {
+                JobState &s = *jp[j];
+                s.gens.clear();
+                for (size_t w = 0; w < s.work.size(); w++) {
+                    const NodeInfo &o = s.job->out->nodes[s.work[w]];
+                    for (Cand &c : s.cand[w]) {
+                        if (!c.gen) continue;
+                        int p[3] = {o.l[0] - c.lx, o.l[1] - c.ly, o.l[2] - c.lz};
+                        c.src = s.gens.request(*s.job->inp, n, p, c.src);
+                    }
+                }
             }
             {
-                // generation on the high-priority stream: its kernel and norm download are what
-                // the host waits for before the exact screening; the group's stream then waits
-                // for the generated blocks with an event
-                StreamSwap fast(ctx, ctx.fast);
-                generate_all(sets, ar, &st);
-                MWG_CUDA(cudaEventRecord(ctx.fast_done, ctx.fast));
-            }
-            MWG_CUDA(cudaStreamWaitEvent(ctx.stream, ctx.fast_done, 0));
-            double *first = nullptr;
-            for (JobState *sp : jp)
-                if (sp->gens.base && !first) first = sp->gens.base;
-            float *first32 = nullptr, *firsttc = nullptr;
-            if (mixed && total > 0) {
-                first32 = (float *)ar.alloc(sizeof(float) * 2 * (size_t)bs * total);
-                k_to_fp32_cube(first, first32, total, b.K, ctx.stream);
-                st.launches++;
-                if (tensor) {
-                    firsttc = (float *)ar.alloc(sizeof(float) * tc5_x_floats(b.K) * total);
-                    k_to_tc_x(first32, firsttc, total, b.K, ctx.stream);
+                // one generation launch for the group; the blocks are contiguous in job order
+                std::vector<std::pair<GenSet *, const Tree *>> sets;
+                size_t total = 0;
+                for (JobState *sp : jp) {
+                    sets.push_back({&sp->gens, sp->job->inp});
+                    total += sp->gens.keys.size();
+                }
+                {
+                    // generation on the high-priority stream: its kernel and norm download are what
+                    // the host waits for before the exact screening; the group's stream then waits
+                    // for the generated blocks with an event
+                    StreamSwap fast(ctx, ctx.fast);
+                    generate_all(sets, ar, &st);
+                    MWG_CUDA(cudaEventRecord(ctx.fast_done, ctx.fast));
+                }
+                MWG_CUDA(cudaStreamWaitEvent(ctx.stream, ctx.fast_done, 0));
+                double *first = nullptr;
+                for (JobState *sp : jp)
+                    if (sp->gens.base && !first) first = sp->gens.base;
+                float *first32 = nullptr, *firsttc = nullptr;
+                if (mixed && total > 0) {
+                    first32 = (float *)ar.alloc(sizeof(float) * 2 * (size_t)bs * total);
+                    k_to_fp32_cube(first, first32, total, b.K, ctx.stream);
                     st.launches++;
+                    if (tensor) {
+                        firsttc = (float *)ar.alloc(sizeof(float) * tc5_x_floats(b.K) * total);
+                        k_to_tc_x(first32, firsttc, total, b.K, ctx.stream);
+                        st.launches++;
+                    }
+                }
+                for (JobState *sp : jp) {
+                    JobState &s = *sp;
+                    s.gbase = s.gens.base;
+                    s.gcn.swap(s.gens.cn);
+                    s.gbase32 = (first32 && s.gbase) ? first32 + 2 * (s.gbase - first) : nullptr;
+                    s.gbase_tc = (firsttc && s.gbase) ? firsttc + tc5_x_floats(b.K) * (size_t)((s.gbase - first) / bs) : nullptr;
                 }
             }
-            for (JobState *sp : jp) {
-                JobState &s = *sp;
-                s.gbase = s.gens.base;
-                s.gcn.swap(s.gens.cn);
-                s.gbase32 = (first32 && s.gbase) ? first32 + 2 * (s.gbase - first) : nullptr;
-                s.gbase_tc = (firsttc && s.gbase) ? firsttc + tc5_x_floats(b.K) * (size_t)((s.gbase - first) / bs) : nullptr;
-            }
-        }
-        auto tC = std::chrono::steady_clock::now();
-        st.host_gen_ms += std::chrono::duration<double, std::milli>(tC - tB).count();
-        // phase C: exact screening and tier per candidate (parallel), then the
-        // per-tier item lists in node order (prefix sums + parallel fill)
-        std::vector<std::pair<int, int>> nodes_flat;  // (job, work index) in launch order
-        for (size_t j = 0; j < jp.size(); j++)
-            for (size_t w = 0; w < jp[j]->work.size(); w++) nodes_flat.push_back({(int)j, (int)w});
-        const long NN = (long)nodes_flat.size();
-        // per tier (0 FP64, 1 FP32, 2 TF32): per-node item counts, then prefix sums
-        std::vector<long long> cnt[NTIER];
-        for (int k = 0; k < NTIER; k++) cnt[k].assign(NN + 1, 0);
-        long long pairs_tot = 0, pairs_t0 = 0, pairs_t1 = 0, pairs_t2 = 0, pairs_t3 = 0;
-#pragma omp parallel for schedule(dynamic, 4) reduction(+ : pairs_tot, pairs_t0, pairs_t1, pairs_t2, pairs_t3)
-        for (long q = 0; q < NN; q++) {
-            JobState &s = *jp[nodes_flat[q].first];
-            int w = nodes_flat[q].second;
-            const Tree &inp = *s.job->inp;
-            const Oper &op = *s.job->op;
-            double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / std::max(s.wgt[w], 1e-300);
-            // tier threshold: the screening threshold; at the root scale (no screening) it is known in
-            // advance only for absolute precision, otherwise root items stay in FP64
-            double tthr = !root ? thr
-                          : s.job->abs_prec ? SCREEN_FAC * split_thr(s.job->prec, 1.0, n) / std::max(s.wgt[w], 1e-300)
-                                            : -1.0;
-            // TF32 at the root scale only where its threshold is the plain one: absolute precision
-            // and no precision-steering trees (their weights shrink on the huge root boxes)
-            const bool tf32_here = !root || (s.job->abs_prec && s.job->prec_trees.empty());
-            long long c[NTIER] = {0, 0, 0, 0};
-            for (Cand &cd : s.cand[w]) {
-                const double *cn = cd.gen ? &s.gcn[8 * (size_t)cd.src] : &inp.cn[8 * (size_t)cd.src];
-                const double *nx = op.norm(cd.t, sidx, cd.lx), *ny = op.norm(cd.t, sidx, cd.ly),
-                             *nz = op.norm(cd.t, sidx, cd.lz);
-                // real inputs keep their bound from the enumeration; generated ones get their own
-                const double bd = cd.gen ? item_bound(nx, ny, nz, cn, root) : cd.bd;
-                if (!root && bd < thr) {
-                    cd.tier = -1;
-                    continue;
+            auto tC = std::chrono::steady_clock::now();
+            st.host_gen_ms += std::chrono::duration<double, std::milli>(tC - tB).count();
+            // phase C: exact screening and tier per candidate (parallel), then the
+            // per-tier item lists in node order (prefix sums + parallel fill)
+            std::vector<std::pair<int, int>> nodes_flat;  // (job, work index) in launch order
+            for (size_t j = 0; j < jp.size(); j++)
+                for (size_t w = 0; w < jp[j]->work.size(); w++) nodes_flat.push_back({(int)j, (int)w});
+            const long NN = (long)nodes_flat.size();
+            // per tier (0 FP64, 1 FP32, 2 TF32): per-node item counts, then prefix sums
+            std::vector<long long> cnt[NTIER];
+            for (int k = 0; k < NTIER; k++) cnt[k].assign(NN + 1, 0);
+            long long pairs_tot = 0, pairs_t0 = 0, pairs_t1 = 0, pairs_t2 = 0, pairs_t3 = 0;
+    #pragma omp parallel for schedule(dynamic, 4) reduction(+ : pairs_tot, pairs_t0, pairs_t1, pairs_t2, pairs_t3)
+            for (long q = 0; q < NN; q++) {
+                JobState &s = *jp[nodes_flat[q].first];
+                int w = nodes_flat[q].second;
+                const Tree &inp = *s.job->inp;
+                const Oper &op = *s.job->op;
+                double thr = root ? 0.0 : SCREEN_FAC * split_thr(s.job->prec, s.R, n) / std::max(s.wgt[w], 1e-300);
+                // tier threshold: the screening threshold; at the root scale (no screening) it is known in
+                // advance only for absolute precision, otherwise root items stay in FP64
+                double tthr = !root ? thr
+                              : s.job->abs_prec ? SCREEN_FAC * split_thr(s.job->prec, 1.0, n) / std::max(s.wgt[w], 1e-300)
+                                                : -1.0;
+                // TF32 at the root scale only where its threshold is the plain one: absolute precision
+                // and no precision-steering trees (their weights shrink on the huge root boxes)
+                const bool tf32_here = !root || (s.job->abs_prec && s.job->prec_trees.empty());
+                long long c[NTIER] = {0, 0, 0, 0};
+                for (Cand &cd : s.cand[w]) {
+                    const double *cn = cd.gen ? &s.gcn[8 * (size_t)cd.src] : &inp.cn[8 * (size_t)cd.src];
+                    const double *nx = op.norm(cd.t, sidx, cd.lx), *ny = op.norm(cd.t, sidx, cd.ly),
+                                 *nz = op.norm(cd.t, sidx, cd.lz);
+                    // real inputs keep their bound from the enumeration; generated ones get their own
+                    const double bd = cd.gen ? item_bound(nx, ny, nz, cn, root) : cd.bd;
+                    if (!root && bd < thr) {
+                        cd.tier = -1;
+                        continue;
+                    }
+                    int np_ = item_pairs(nx, ny, nz, cn, root);
+                    pairs_tot += np_;
+                    bool near = std::max(std::abs(cd.lx), std::max(std::abs(cd.ly), std::abs(cd.lz))) <= 1;
+                    int tier;
+                    if (!mixed || tthr < 0.0 || (near_fp64 && near))
+                        tier = 0;
+                    else if (df_only)
+                        tier = bd <= TIER_DF * tthr ? 3 : 0;
+                    else if (bd > TIER_FP64 * tthr)
+                        tier = (dfp && bd <= TIER_DF * tthr) ? 3 : 0;
+                    else if (tensor && tf32_here && bd <= TIER_TF32 * tthr)
+                        tier = 2;
+                    else
+                        tier = 1;
+                    cd.tier = tier;
+                    c[tier]++;
+                    (tier == 0 ? pairs_t0 : tier == 1 ? pairs_t1 : tier == 2 ? pairs_t2 : pairs_t3) += np_;
                 }
-                int np_ = item_pairs(nx, ny, nz, cn, root);
-                pairs_tot += np_;
-                bool near = std::max(std::abs(cd.lx), std::max(std::abs(cd.ly), std::abs(cd.lz))) <= 1;
-                int tier;
-                if (!mixed || tthr < 0.0 || (near_fp64 && near))
-                    tier = 0;
-                else if (df_only)
-                    tier = bd <= TIER_DF * tthr ? 3 : 0;
-                else if (bd > TIER_FP64 * tthr)
-                    tier = (dfp && bd <= TIER_DF * tthr) ? 3 : 0;
-                else if (tensor && tf32_here && bd <= TIER_TF32 * tthr)
-                    tier = 2;
-                else
-                    tier = 1;
-                cd.tier = tier;
-                c[tier]++;
-                (tier == 0 ? pairs_t0 : tier == 1 ? pairs_t1 : tier == 2 ? pairs_t2 : pairs_t3) += np_;
+                for (int k = 0; k < NTIER; k++) cnt[k][q + 1] = c[k];
             }
-            for (int k = 0; k < NTIER; k++) cnt[k][q + 1] = c[k];
-        }
-        // every tier adds to the output blocks (zeroed when their nodes were created), so each
-        // tier launches only the nodes that have items in it
-        LevelItems *lt = G.lt;
-        std::vector<long> slot[NTIER];
-        long nnt[NTIER] = {0, 0, 0, 0};
-        for (int k = 0; k < NTIER; k++) slot[k].assign(NN, -1);
-        for (long q = 0; q < NN; q++) {
-            for (int k = 0; k < NTIER; k++)
-                if (cnt[k][q + 1] > 0) slot[k][q] = nnt[k]++;
-            for (int k = 0; k < NTIER; k++) cnt[k][q + 1] += cnt[k][q];
-        }
-        long long ntot[NTIER];
-        for (int k = 0; k < NTIER; k++) {
-            ntot[k] = cnt[k][NN];
-            lt[k].resize(nnt[k], ntot[k]);
-        }
-#pragma omp parallel for schedule(dynamic, 4)
-        for (long q = 0; q < NN; q++) {
-            JobState &s = *jp[nodes_flat[q].first];
-            int w = nodes_flat[q].second;
-            const Tree &inp = *s.job->inp;
-            const Oper &op = *s.job->op;
-            double *ob = s.job->out->block(s.work[w]);
-            long long p[NTIER];
+            // every tier adds to the output blocks (zeroed when their nodes were created), so each
+            // tier launches only the nodes that have items in it
+            std::vector<long> slot[NTIER];
+            long nnt[NTIER] = {0, 0, 0, 0};
+            for (int k = 0; k < NTIER; k++) slot[k].assign(NN, -1);
+            for (long q = 0; q < NN; q++) {
+                for (int k = 0; k < NTIER; k++)
+                    if (cnt[k][q + 1] > 0) slot[k][q] = nnt[k]++;
+                for (int k = 0; k < NTIER; k++) cnt[k][q + 1] += cnt[k][q];
+            }
+            long long ntot[NTIER];
             for (int k = 0; k < NTIER; k++) {
-                p[k] = cnt[k][q];
-                if (slot[k][q] >= 0) {
-                    lt[k].out[slot[k][q]] = ob;
-                    lt[k].begin[slot[k][q] + 1] = cnt[k][q + 1];
+                ntot[k] = cnt[k][NN];
+                lt[k].resize(nnt[k], ntot[k]);
+            }
+    #pragma omp parallel for schedule(dynamic, 4)
+            for (long q = 0; q < NN; q++) {
+                JobState &s = *jp[nodes_flat[q].first];
+                int w = nodes_flat[q].second;
+                const Tree &inp = *s.job->inp;
+                const Oper &op = *s.job->op;
+                double *ob = s.job->out->block(s.work[w]);
+                long long p[NTIER];
+                for (int k = 0; k < NTIER; k++) {
+                    p[k] = cnt[k][q];
+                    if (slot[k][q] >= 0) {
+                        lt[k].out[slot[k][q]] = ob;
+                        lt[k].begin[slot[k][q] + 1] = cnt[k][q + 1];
+                    }
+                }
+                for (const Cand &cd : s.cand[w]) {
+                    if (cd.tier < 0) continue;
+                    long bxi = op.block_index(cd.t, sidx, cd.lx), byi = op.block_index(cd.t, sidx, cd.ly),
+                         bzi = op.block_index(cd.t, sidx, cd.lz);
+                    LevelItems &T = lt[cd.tier];
+                    long long &pi = p[cd.tier];
+                    if (cd.tier == 0) {
+                        T.in[pi] = cd.gen ? (const void *)(s.gbase + (size_t)cd.src * bs) : (const void *)inp.block(cd.src);
+                        T.ax[pi] = op.d_blocks + (size_t)bxi * bsz;
+                        T.ay[pi] = op.d_blocks + (size_t)byi * bsz;
+                        T.az[pi] = op.d_blocks + (size_t)bzi * bsz;
+                    } else if (cd.tier == 2) {
+                        // the tensor-core tier reads its own operand layouts (mw_tc05_layout.h)
+                        const size_t tx = tc5_x_floats(b.K), tb = tc5_b_floats(b.K);
+                        T.in[pi] = cd.gen ? (const void *)(s.gbase_tc + tx * (size_t)cd.src)
+                                          : (const void *)(inp.d_coefs_tc + tx * (size_t)cd.src);
+                        T.ax[pi] = op.d_blocks_tc + tb * (size_t)bxi;
+                        T.ay[pi] = op.d_blocks_tc + tb * (size_t)byi;
+                        T.az[pi] = op.d_blocks_tc + tb * (size_t)bzi;
+                    } else {
+                        // the reduced tiers read the FP32 cube-order shadows and the FP32 operator blocks
+                        // (high part first, low part after it)
+                        T.in[pi] = cd.gen ? (const void *)(s.gbase32 + 2 * (size_t)cd.src * bs)
+                                          : (const void *)(inp.d_coefs32 + 2 * (size_t)cd.src * bs);
+                        T.ax[pi] = op.d_blocks32 + 2 * (size_t)bxi * bsz;
+                        T.ay[pi] = op.d_blocks32 + 2 * (size_t)byi * bsz;
+                        T.az[pi] = op.d_blocks32 + 2 * (size_t)bzi * bsz;
+                    }
+                    T.coef[pi] = op.c[cd.t];
+                    pi++;
                 }
             }
-            for (const Cand &cd : s.cand[w]) {
-                if (cd.tier < 0) continue;
-                long bxi = op.block_index(cd.t, sidx, cd.lx), byi = op.block_index(cd.t, sidx, cd.ly),
-                     bzi = op.block_index(cd.t, sidx, cd.lz);
-                LevelItems &T = lt[cd.tier];
-                long long &pi = p[cd.tier];
-                if (cd.tier == 0) {
-                    T.in[pi] = cd.gen ? (const void *)(s.gbase + (size_t)cd.src * bs) : (const void *)inp.block(cd.src);
-                    T.ax[pi] = op.d_blocks + (size_t)bxi * bsz;
-                    T.ay[pi] = op.d_blocks + (size_t)byi * bsz;
-                    T.az[pi] = op.d_blocks + (size_t)bzi * bsz;
-                } else if (cd.tier == 2) {
-                    // the tensor-core tier reads its own operand layouts (mw_tc05_layout.h)
-                    const size_t tx = tc5_x_floats(b.K), tb = tc5_b_floats(b.K);
-                    T.in[pi] = cd.gen ? (const void *)(s.gbase_tc + tx * (size_t)cd.src)
-                                      : (const void *)(inp.d_coefs_tc + tx * (size_t)cd.src);
-                    T.ax[pi] = op.d_blocks_tc + tb * (size_t)bxi;
-                    T.ay[pi] = op.d_blocks_tc + tb * (size_t)byi;
-                    T.az[pi] = op.d_blocks_tc + tb * (size_t)bzi;
-                } else {
-                    // the reduced tiers read the FP32 cube-order shadows and the FP32 operator blocks
-                    // (high part first, low part after it)
-                    T.in[pi] = cd.gen ? (const void *)(s.gbase32 + 2 * (size_t)cd.src * bs)
-                                      : (const void *)(inp.d_coefs32 + 2 * (size_t)cd.src * bs);
-                    T.ax[pi] = op.d_blocks32 + 2 * (size_t)bxi * bsz;
-                    T.ay[pi] = op.d_blocks32 + 2 * (size_t)byi * bsz;
-                    T.az[pi] = op.d_blocks32 + 2 * (size_t)bzi * bsz;
-                }
-                T.coef[pi] = op.c[cd.t];
-                pi++;
-            }
+            st.items += ntot[0] + ntot[1] + ntot[2] + ntot[3];
+            st.items_fp64 += ntot[0];
+            st.items_fp32 += ntot[1];
+            st.items_tf32 += ntot[2];
+            st.items_df += ntot[3];
+            st.flops += 6.0 * K4 * (double)pairs_tot;
+            st.flops_issued += 96.0 * K4 * (double)(ntot[0] + ntot[1] + ntot[2] + ntot[3]);
+            st.flops_fp64 += 6.0 * K4 * (double)pairs_t0;
+            st.flops_fp32 += 6.0 * K4 * (double)pairs_t1;
+            st.flops_tf32 += 6.0 * K4 * (double)pairs_t2;
+            st.flops_df += 6.0 * K4 * (double)pairs_t3;
+            st.host_items_ms +=
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tC).count();
         }
-        st.items += ntot[0] + ntot[1] + ntot[2] + ntot[3];
-        st.items_fp64 += ntot[0];
-        st.items_fp32 += ntot[1];
-        st.items_tf32 += ntot[2];
-        st.items_df += ntot[3];
-        st.flops += 6.0 * K4 * (double)pairs_tot;
-        st.flops_issued += 96.0 * K4 * (double)(ntot[0] + ntot[1] + ntot[2] + ntot[3]);
-        st.flops_fp64 += 6.0 * K4 * (double)pairs_t0;
-        st.flops_fp32 += 6.0 * K4 * (double)pairs_t1;
-        st.flops_tf32 += 6.0 * K4 * (double)pairs_t2;
-        st.flops_df += 6.0 * K4 * (double)pairs_t3;
-        auto tD = std::chrono::steady_clock::now();
-        st.host_items_ms += std::chrono::duration<double, std::milli>(tD - tC).count();
+        const auto tD = std::chrono::steady_clock::now();
         MWG_CUDA(cudaEventRecord(G.ev[0], ctx.stream));
         G.status.clear();
         for (int k = 0; k < NTIER; k++) {
-            int *hs = launch_tier(ctx, ar, lt[k], root, false, k, tune.chunk[k], st);
+            int *hs = launch_tier(ctx, ar, lt[k], root, false, k, tune.chunk[k], st, dscreen ? &dv : nullptr);
             if (hs) G.status.push_back(hs);
             MWG_CUDA(cudaEventRecord(G.ev[k + 1], ctx.stream));
         }
@@ -957,6 +1433,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         st.gpu_post_ms += c;
     }
     for (auto &e : ev_span) cudaEventDestroy(e);
+    if (ds.ev_counts) cudaEventDestroy(ds.ev_counts);
     st.kernel_ms += kernel_ms;
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }

@@ -408,4 +408,15 @@ void build_operators(const std::vector<Oper *> &ops, const Basis &b) {
         if (pp) cudaFree(pp);
 }
 
+void Oper::free_device() {
+    if (d_blocks) cudaFree(d_blocks);
+    if (d_blocks32) cudaFree(d_blocks32);
+    if (d_blocks_tc) cudaFree(d_blocks_tc);
+    if (d_screen) cudaFree(d_screen);
+    d_blocks = nullptr;
+    d_blocks32 = nullptr;
+    d_blocks_tc = nullptr;
+    d_screen = nullptr;
+}
+
 }  // namespace mwg

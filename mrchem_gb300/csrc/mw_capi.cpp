@@ -117,6 +117,7 @@ static void ctx_free(mw_ctx c) {
         if (xs) cudaStreamSynchronize(xs);
     if (c->ctx.fast) cudaStreamSynchronize(c->ctx.fast);
     c->ctx.arena.release();
+    c->ctx.sarena.release();
     for (auto &xa : c->ctx.xarena) xa.release();
     if (c->ctx.h_pinned) cudaFreeHost(c->ctx.h_pinned);
     if (c->ctx.d_basis) cudaFree(c->ctx.d_basis);
@@ -173,6 +174,12 @@ int mw_ctx_set_overlap(mw_ctx c, int on) {
 int mw_ctx_set_groups(mw_ctx c, int n) {
     if (!c || n < 1 || n > mwg::Ctx::XGROUPS + 1) return MW_ERR_ARG;
     c->ctx.groups = n;
+    return MW_OK;
+}
+
+int mw_ctx_set_screening(mw_ctx c, int on) {
+    if (!c || (on != 0 && on != 1)) return MW_ERR_ARG;
+    c->ctx.screening = on;
     return MW_OK;
 }
 
@@ -422,9 +429,7 @@ int mw_op_create_helmholtz_batch(mw_ctx c, int n, const double *mu, double prec,
     int rc = guard(&c->ctx, [&] { mwg::build_operators(ops, c->ctx.basis); });
     if (rc != MW_OK) {
         for (mw_op o : made) {
-            if (o->op.d_blocks) cudaFree(o->op.d_blocks);
-            if (o->op.d_blocks32) cudaFree(o->op.d_blocks32);
-            if (o->op.d_blocks_tc) cudaFree(o->op.d_blocks_tc);
+            o->op.free_device();
             delete o;
         }
         return rc;
@@ -440,9 +445,7 @@ int mw_op_destroy(mw_op o) {
     if (!o) return MW_ERR_ARG;
     cudaSetDevice(o->op.ctx->device);
     cudaStreamSynchronize(o->op.ctx->stream);
-    if (o->op.d_blocks) cudaFree(o->op.d_blocks);
-    if (o->op.d_blocks32) cudaFree(o->op.d_blocks32);
-    if (o->op.d_blocks_tc) cudaFree(o->op.d_blocks_tc);
+    o->op.free_device();
     mwg::Ctx *ctx = o->op.ctx;
     delete o;
     ctx_child_gone(ctx);

@@ -131,6 +131,10 @@ struct Oper {
     double *d_blocks = nullptr;  // (2K)^2 per block, FP64
     float *d_blocks32 = nullptr; // FP32 copy: per block the high part, then the low part (2 x (2K)^2)
     float *d_blocks_tc = nullptr; // TF32 B operand of the tensor-core tier per block (mw_tc05_layout.h)
+    // the screening tables on the device (bands, block offsets, sub-block norms, amax, xmax, term
+    // coefficients), uploaded by the first apply that screens on the GPU (mw_screen.cu)
+    void *d_screen = nullptr;
+    void free_device();
     const double *norm(int t, int s, int l) const { return &norms[(size_t)(off[t * S + s] + l + band[t * S + s]) * 4]; }
     long block_index(int t, int s, int l) const { return off[t * S + s] + l + band[t * S + s]; }
     void build(const Basis &b);  // build_operators({this}, b)
@@ -177,6 +181,10 @@ struct Ctx {
     cudaStream_t xstream[XGROUPS] = {};
     Arena xarena[XGROUPS];
     int groups = DEFAULT_GROUPS;  // job groups of a batched apply (1: no overlap)
+    // where a batched apply enumerates, screens and lists its items: 1 on the GPU (mw_screen.cu,
+    // the default), 0 on the host (OpenMP); both give the same items in the same order
+    int screening = 1;
+    Arena sarena;  // per-apply tables of the GPU screening (input hash tables and norms)
     // launch settings of a batched apply: job groups, and the largest number of items one CTA
     // task takes per tier (FP64, FP32, TF32, double-FP32) before a node is split into chunks
     struct Tuning {
@@ -342,6 +350,98 @@ void k_dot(const double *const *a, const double *const *b, const int *start, int
 void k_scale(double *x, size_t n, double c, cudaStream_t s);
 // dst block j = src block map[j]; bs even
 void k_permute_blocks(double *dst, const double *src, const int *map, int n, int bs, cudaStream_t s);
+// ---------------------------------------------------------------- screening on the GPU (mw_screen.cu)
+// Hash of a node key, shared by the host (which fills an input tree's table) and the device (which
+// looks positions up in it).
+__host__ __device__ inline unsigned key_hash(int n, int x, int y, int z) {
+    uint64_t h = (uint64_t)(uint32_t)n * 0x9E3779B97F4A7C15ULL;
+    h ^= (uint64_t)(uint32_t)x * 0xC2B2AE3D27D4EB4FULL;
+    h = (h << 21) | (h >> 43);
+    h ^= (uint64_t)(uint32_t)y * 0x165667B19E3779F9ULL;
+    h = (h << 21) | (h >> 43);
+    h ^= (uint64_t)(uint32_t)z * 0xD6E8FEB86659FD93ULL;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ULL;
+    h ^= h >> 29;
+    return (unsigned)h;
+}
+constexpr int HASH_EMPTY = (int)0x80000000;  // n of an empty slot of an input tree's table
+
+struct ScreenOp {  // one operator's tables (device)
+    const int *band, *off;             // [T*S]: band L(t, n), block index of l = -L
+    const double *norms;               // 4 sub-block norms per block
+    const float *norms32;              // the same rounded to FP32 (the fast path's estimates)
+    const double *amax, *xmax, *c;     // [T*S], [T*S], [T]
+    const float *amax32, *xmax32;
+    const double *b64;                 // blocks in the tier kernels' layouts
+    const float *b32, *btc;
+    int T, S;
+};
+struct ScreenJob {  // one job of the apply (device)
+    ScreenOp op;
+    const int4 *hkey;  // the input tree's hash table: key (n, l) per slot, n = HASH_EMPTY when free
+    const int *hval;   // node index per slot
+    int hmask, pad;
+    const double *cn;  // the input's component norms (8 per node) and block norms, as the host has them
+    const double *bn;
+    const float *cn32, *bn32;  // the same rounded to FP32
+    const double *in64;  // the input's blocks and shadows
+    const float *in32, *intc;
+};
+struct ScreenNode {  // one output node of the level (device)
+    double thr, thr2;      // screening threshold of the walk, and of the items after generation
+    double tthr, fm;       // tier threshold (< 0: FP64 only), pruning norm
+    int job, l[3];
+    int flags;             // bit 0: zero weight below the root scale (no items), bit 1: TF32 allowed,
+                           // bit 2: FP32 estimates decide where they are clear of the thresholds
+    int gtab, gmask;       // the job's generation table: first slot, mask
+    // FP32 decision bands: an FP32 bound below lo fails, above hi passes, in between FP64 decides
+    float thr_lo, thr_hi, thr2_lo, thr2_hi;
+    float tier_lo[3], tier_hi[3];  // around TIER_TF32, TIER_FP64 and TIER_DF times tthr
+    float fm32, prune32;           // fm, and thr (1 - margin): prune where fm32 * expr < prune32
+};
+struct ScreenCand {  // one item in walk order
+    int src;                    // input node, or generated slot when gen = 1
+    short lx, ly, lz;
+    unsigned char tier, gen;
+    int t;
+};
+struct ScreenLevel {
+    const ScreenNode *nodes;
+    const ScreenJob *jobs;
+    int nn, n, sidx, root, n0, bs, bsz;
+    int lo[3], hi[3];  // the world's translations at scale n: lo <= l < hi
+    int mixed, near_fp64, df_only, dfp, tensor;
+    double tier_fp64, tier_tf32, tier_df;
+    // generation tables: per job gmask + 1 keys (0 = free) and slots; slot counter, overflow flag;
+    // per slot: job, ancestor, ancestor scale, l[3]
+    unsigned long long *gkey;
+    int *gval, *gen_cnt, *overflow, *gen_info;
+    int gen_cap;
+    int *cnt;                   // [nn] items before the exact screening of generated inputs
+    const long long *cand_off;  // [nn] first ScreenCand of each node
+    ScreenCand *cand;
+    double *gcn;                // generated blocks' component norms
+    float *gcn32;               // the same rounded to FP32
+    int *tcnt;                  // [nn][8]: items per tier, then component pairs per tier
+    long long *tier_off;        // [nn][4]: first item of each node in each tier's arrays
+    long long *tier_tot;        // [4]
+    const void **in, **ax, **ay, **az;  // item arrays, the tiers one after the other
+    double *coef;
+    const double *g64;          // generated blocks and their shadows
+    const float *g32, *gtc;
+    size_t tx, tb;              // floats per block in the TF32 layouts (input, operator)
+};
+// shared memory of the walk kernels: maxT = most terms of an operator, zmax = most (t, lz) rows of
+// one at the level's scale (sum over terms of 2 L(t, n) + 1)
+size_t screen_smem(int maxT, int zmax);
+void k_screen_count(const ScreenLevel &P, int maxT, int zmax, cudaStream_t s);
+void k_screen_gen_tasks(const ScreenLevel &P, GenTask *tasks, int ngen, cudaStream_t s);
+// FP32 copies of the generated blocks' component norms (after the generation kernel)
+void k_screen_gen_norms32(const ScreenLevel &P, int ngen, cudaStream_t s);
+void k_screen_write(const ScreenLevel &P, int maxT, int zmax, cudaStream_t s);
+void k_screen_fill(const ScreenLevel &P, cudaStream_t s);
+
 // true when the GPU's DMA engines can read / write the host buffer directly (pinned memory)
 bool host_is_pinned(const void *p);
 double probe_fma_tflops(int fp64, int nsm, cudaStream_t s);

@@ -1,0 +1,165 @@
+"""Screening on the GPU (mw_screen.cu) against screening on the host.
+
+Both walk the candidate items (term, then lz, ly, lx in the operator band) with the same pruning,
+screen them with the same norm-product bound in the same floating-point order, and assign the
+same tiers, so the item lists and hence the results must be bit-identical.  Checked on:
+- a batch of Helmholtz applies of uneven polynomial-Gaussian orbitals (k=9, absolute prec 1e-6),
+  in every precision mode (FP64, four tiers, FP64/FP32, double-FP32, near-diagonal FP64);
+- a Poisson apply under relative precision (k=7, FP64 and mixed);
+- exchange-like Poisson applies of pair products with precision-steering trees (mixed);
+- a fixed-grid apply (maxIter = 0), mixed;
+with pipelined job groups on and off.  Also: per-tier item counts and component pairs agree, and
+GPU-screened reruns are bit-identical.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+SEED = 20261203
+
+
+def poly_orbitals(rng, n, lo, hi):
+    mons = [(a, b, c) for a in range(4) for b in range(4) for c in range(4) if a + b + c <= 3]
+    out = []
+    for _ in range(n):
+        alpha = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        R = rng.uniform(-2.0, 2.0, 3)
+        out.append([(float(c), alpha, tuple(R), m) for c, m in zip(rng.standard_normal(len(mons)), mons)])
+    return out
+
+
+def same_trees(a, b):
+    ka, ca, la = a.download()
+    kb, cb, lb = b.download()
+    return np.array_equal(ka, kb) and np.array_equal(ca, cb) and np.array_equal(la, lb)
+
+
+STAT_KEYS = ("out_nodes", "items", "items_fp64", "items_fp32", "items_tf32", "items_df", "generated", "flops")
+
+
+def both(engine, mra, run):
+    """run() once with host screening and once with GPU screening; returns (outs, stats) pairs."""
+    res = []
+    for where in ("host", "gpu"):
+        mra.set_screening(where)
+        outs = run()
+        res.append((outs, mra.last_stats()))
+    mra.set_screening("gpu")
+    return res
+
+
+def check_identical(res):
+    (oh, sh), (og, sg) = res
+    for a, b in zip(oh, og):
+        assert same_trees(a, b)
+    for k in STAT_KEYS:
+        assert sh[k] == sg[k], (k, sh[k], sg[k])
+
+
+@pytest.fixture(scope="module")
+def helmholtz_batch(engine):
+    prec = 1e-6
+    rng = np.random.default_rng(SEED)
+    mra = engine.MultiResolutionAnalysis(9)
+    orbs = []
+    for terms in poly_orbitals(rng, 4, 0.3, 20.0):
+        f = engine.project(prec, engine.FunctionTree(mra), terms, abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        orbs.append(f)
+    eps = rng.uniform(-2.0, -0.1, 4)
+    ops = [engine.HelmholtzOperator(mra, math.sqrt(-2.0 * e), prec) for e in eps]
+    return mra, prec, orbs, ops
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed-fp32", "df", "mixed-near64"])
+@pytest.mark.parametrize("overlap", [True, False])
+def test_helmholtz_batch_bit_identical(engine, helmholtz_batch, precision, overlap):
+    mra, prec, orbs, ops = helmholtz_batch
+    if precision == "fp64" and overlap is False:
+        pytest.skip("FP64 is covered with overlap on")
+    mra.set_overlap(overlap)
+
+    def run():
+        outs = [engine.FunctionTree(mra) for _ in orbs]
+        engine.apply_batch([prec] * len(orbs), outs, ops, orbs, abs_prec=True, precision=precision)
+        return outs
+
+    try:
+        res = both(engine, mra, run)
+    finally:
+        mra.set_overlap(True)
+    check_identical(res)
+    assert res[1][1]["items"] > 0
+    assert res[1][1]["generated"] > 0  # inputs missing at an output's scale are generated on the GPU
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_poisson_relative_precision(engine, precision):
+    prec = 1e-5
+    rng = np.random.default_rng(SEED + 1)
+    mra = engine.MultiResolutionAnalysis(7)
+    terms = []
+    for _ in range(4):
+        a = float(np.exp(rng.uniform(np.log(0.5), np.log(50.0))))
+        terms.append(((a / math.pi) ** 1.5, a, tuple(rng.uniform(-2, 2, 3)), (0, 0, 0)))
+    rho = engine.project(prec, engine.FunctionTree(mra), terms, abs_prec=True)
+    P = engine.PoissonOperator(mra, prec)
+
+    def run():
+        V = engine.FunctionTree(mra)
+        engine.apply(prec, V, P, rho, abs_prec=False, precision=precision)
+        return [V]
+
+    check_identical(both(engine, mra, run))
+
+
+def test_exchange_pairs_with_precision_trees(engine):
+    prec = 1e-5
+    rng = np.random.default_rng(SEED + 2)
+    mra = engine.MultiResolutionAnalysis(7)
+    orbs = []
+    for terms in poly_orbitals(rng, 4, 0.3, 20.0):
+        f = engine.project(prec, engine.FunctionTree(mra), terms, abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        orbs.append(f)
+    pairs = [(i, j) for i in range(4) for j in range(i, 4)]
+    prods = [engine.FunctionTree(mra) for _ in pairs]
+    engine.multiply_batch([prec / 10] * len(pairs), prods, [1.0] * len(pairs), [orbs[i] for i, _ in pairs],
+                          [orbs[j] for _, j in pairs], abs_prec=False, use_max_norms=True)
+    P = engine.PoissonOperator(mra, prec)
+
+    def run():
+        outs = [engine.FunctionTree(mra) for _ in pairs]
+        engine.apply_batch([prec * 10] * len(pairs), outs, [P] * len(pairs), prods,
+                           prec_trees=[[orbs[i], orbs[j]] for i, j in pairs], abs_prec=False, precision="mixed")
+        return outs
+
+    res = both(engine, mra, run)
+    check_identical(res)
+
+
+def test_fixed_grid(engine, helmholtz_batch):
+    mra, prec, orbs, ops = helmholtz_batch
+    f, H = orbs[0], ops[0]
+
+    def run():
+        V = engine.FunctionTree(mra)
+        engine.copy_grid(V, f)
+        engine.apply_fixed(prec, V, H, f, abs_prec=True, precision="mixed")
+        return [V]
+
+    check_identical(both(engine, mra, run))
+
+
+def test_gpu_screening_rerun_bit_identical(engine, helmholtz_batch):
+    mra, prec, orbs, ops = helmholtz_batch
+    mra.set_screening("gpu")
+    runs = []
+    for _ in range(2):
+        outs = [engine.FunctionTree(mra) for _ in orbs]
+        engine.apply_batch([prec] * len(orbs), outs, ops, orbs, abs_prec=True, precision="mixed")
+        runs.append(outs)
+    for a, b in zip(*runs):
+        assert same_trees(a, b)
