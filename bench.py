@@ -287,12 +287,20 @@ def run(args):
     h2d = sum(k.nbytes + c.nbytes for k, c, _ in host_inputs)
     host_outputs = [None] * NORB
 
+    e2e_parts = {"upload_ms": 0.0, "apply_ms": 0.0, "download_ms": 0.0}
+
     def e2e_step():
+        t0 = time.perf_counter()
         mw.upload_batch(e2e_phis, host_inputs)
+        t1 = time.perf_counter()
         for o in outs:
             o.clear()
         mw.apply_batch([PREC] * NORB, outs, ops, e2e_phis, abs_prec=True, precision="mixed")
+        t2 = time.perf_counter()
         host_outputs[:] = mw.download_batch(outs, outs=host_outputs if host_outputs[0] is not None else None)
+        t3 = time.perf_counter()
+        for k, v in zip(e2e_parts, (t1 - t0, t2 - t1, t3 - t2)):
+            e2e_parts[k] += v * 1e3
         return sum(a.nbytes for r in host_outputs for a in r)
 
     e2e_step()
@@ -303,6 +311,8 @@ def run(args):
     for r in host_outputs:
         mw.pin_host(mra, r[1])
     barrier()
+    for k in e2e_parts:
+        e2e_parts[k] = 0.0
     t0 = time.perf_counter()
     d2h = 0
     for _ in range(args.e2e_steps):
@@ -395,7 +405,8 @@ def run(args):
                            "ms_per_step": host_scr_ms,
                            "policy": "enumeration, screening and item lists on the host cores (mw_ctx_set_screening 0)"},
         "gpu_launches": int(st["launches"]),
-        "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "ms_per_step": e2e_ms, **{k: v / args.e2e_steps for k, v in e2e_parts.items()}},
         "roofline": dict(roofs[dominant], tier=dominant),
         "roofline_tiers": roofs,
         "clocks": clk.summary(),
@@ -415,7 +426,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-levels", type=int, default=-1)
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="pick the batch's launch settings with mw_apply_batch_autotune before timing")
