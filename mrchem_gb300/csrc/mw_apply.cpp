@@ -1325,14 +1325,104 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         st.host_refine_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tR).count();
     };
 
+    // post-processing of a set of jobs on the context's current stream: top-down sum over scales,
+    // bottom-up compression, leaf norms, and the norms' download into pinned staging (copied into
+    // the trees after the final synchronisation)
+    std::vector<std::pair<Tree *, double *>> cn_staging;
+    auto post_process = [&](const std::vector<JobState *> &jset, Arena &ar) {
+        int maxn = b.n0;
+        for (JobState *sp : jset) maxn = std::max(maxn, sp->job->out->max_scale());
+        for (int n = b.n0; n < maxn; n++) {
+            std::vector<PairTask> tasks;
+            for (JobState *sp : jset) {
+                Tree &out = *sp->job->out;
+                for (int i = 0; i < out.nn(); i++)
+                    if (out.nodes[i].n == n && out.nodes[i].child0 >= 0)
+                        tasks.push_back({out.block(i), out.block(out.nodes[i].child0)});
+            }
+            if (tasks.empty()) continue;
+            Packer pk;
+            pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
+            pk.ship(ctx, ar);
+            if (mixed)
+                k_topdown_df(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
+            else
+                k_topdown(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
+            st.launches++;
+        }
+        for (int n = maxn - 1; n >= b.n0; n--) {
+            std::vector<PairTask> tasks;
+            std::vector<double *> cnp;
+            for (JobState *sp : jset) {
+                Tree &out = *sp->job->out;
+                for (int i = 0; i < out.nn(); i++)
+                    if (out.nodes[i].n == n && out.nodes[i].child0 >= 0) {
+                        tasks.push_back({out.block(i), out.block(out.nodes[i].child0)});
+                        cnp.push_back(out.d_cn + (size_t)8 * i);
+                    }
+            }
+            if (tasks.empty()) continue;
+            Packer pk;
+            pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
+            pk.add(cnp.data(), cnp.size() * sizeof(double *));
+            pk.ship(ctx, ar);
+            if (mixed)
+                k_compress_df(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1),
+                              (int)tasks.size(), ctx.stream);
+            else
+                k_compress(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(),
+                           ctx.stream);
+            st.launches++;
+        }
+        // leaf norms after the top-down pass
+        std::vector<double *> bl, cnp;
+        for (JobState *sp : jset) {
+            Tree &out = *sp->job->out;
+            for (int i = 0; i < out.nn(); i++)
+                if (out.nodes[i].child0 < 0) {
+                    bl.push_back(out.block(i));
+                    cnp.push_back(out.d_cn + (size_t)8 * i);
+                }
+        }
+        if (!bl.empty()) {
+            Packer pk;
+            pk.add(bl.data(), bl.size() * sizeof(double *));
+            pk.add(cnp.data(), cnp.size() * sizeof(double *));
+            pk.ship(ctx, ar);
+            k_norms(ctx.dbasis, (double *const *)pk.ptr(0), (double *const *)pk.ptr(1), (int)bl.size(), ctx.stream);
+            st.launches++;
+        }
+        for (JobState *sp : jset) {
+            Tree &out = *sp->job->out;
+            double *h = (double *)ar.halloc(sizeof(double) * 8 * out.nn());
+            MWG_CUDA(cudaMemcpyAsync(h, out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost, ctx.stream));
+            cn_staging.push_back({&out, h});
+        }
+    };
+
+    // the levels of the job groups, pipelined; a group's post-processing starts on its own stream
+    // as soon as its last level is launched, beside the other groups' levels
+    std::vector<cudaEvent_t> ev_post(2 * ngroups, nullptr);
+    for (auto &e : ev_post) MWG_CUDA(cudaEventCreate(&e));
     while (true) {
         bool active = false;
-        for (auto &G : groups) {
+        for (int g = 0; g < ngroups; g++) {
+            Group &G = groups[g];
             if (G.pending) {
                 finish_level(G);
                 G.pending = false;
             }
-            if (!G.done) G.done = !launch_level(G);
+            if (!G.done) {
+                G.done = !launch_level(G);
+                if (G.done) {
+                    StreamSwap swap(ctx, G.stream);
+                    std::vector<JobState *> jset;
+                    for (int j : G.jobs) jset.push_back(&js[j]);
+                    MWG_CUDA(cudaEventRecord(ev_post[2 * g], ctx.stream));
+                    post_process(jset, *G.arena);
+                    MWG_CUDA(cudaEventRecord(ev_post[2 * g + 1], ctx.stream));
+                }
+            }
             if (!G.done) {
                 G.pending = true;
                 active = true;
@@ -1340,7 +1430,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         }
         if (!active) break;
     }
-    // the post-processing on the context's stream follows every group's last work
+    // the context's stream follows every group's last work
     for (int g = 1; g < ngroups; g++) {
         MWG_CUDA(cudaEventRecord(ev_end[g], groups[g].stream));
         MWG_CUDA(cudaStreamWaitEvent(ctx.stream, ev_end[g], 0));
@@ -1352,86 +1442,24 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         if (e) cudaEventDestroy(e);
     // input bytes: every distinct input block read once per apply (FP64 or FP32 shadow) + operator blocks
     for (auto &s : js) st.bytes += 8.0 * bs * (double)s.job->inp->nn();
-
     MWG_CUDA(cudaEventRecord(ev_span[1], ctx.stream));
-    // post-processing: top-down sum over scales, then bottom-up compression
-    int maxn = b.n0;
-    for (auto &s : js) maxn = std::max(maxn, s.job->out->max_scale());
-    for (int n = b.n0; n < maxn; n++) {
-        std::vector<PairTask> tasks;
-        for (auto &s : js) {
-            Tree &out = *s.job->out;
-            for (int i = 0; i < out.nn(); i++)
-                if (out.nodes[i].n == n && out.nodes[i].child0 >= 0)
-                    tasks.push_back({out.block(i), out.block(out.nodes[i].child0)});
-        }
-        if (tasks.empty()) continue;
-        Packer pk;
-        pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
-        pk.ship(ctx, arena);
-        if (mixed)
-            k_topdown_df(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
-        else
-            k_topdown(ctx.dbasis, (const PairTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
-        st.launches++;
-    }
-    for (int n = maxn - 1; n >= b.n0; n--) {
-        std::vector<PairTask> tasks;
-        std::vector<double *> cnp;
-        for (auto &s : js) {
-            Tree &out = *s.job->out;
-            for (int i = 0; i < out.nn(); i++)
-                if (out.nodes[i].n == n && out.nodes[i].child0 >= 0) {
-                    tasks.push_back({out.block(i), out.block(out.nodes[i].child0)});
-                    cnp.push_back(out.d_cn + (size_t)8 * i);
-                }
-        }
-        if (tasks.empty()) continue;
-        Packer pk;
-        pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
-        pk.add(cnp.data(), cnp.size() * sizeof(double *));
-        pk.ship(ctx, arena);
-        if (mixed)
-            k_compress_df(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(),
-                          ctx.stream);
-        else
-            k_compress(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(),
-                       ctx.stream);
-        st.launches++;
-    }
-    // leaf norms after the top-down pass
-    {
-        std::vector<double *> bl, cnp;
-        for (auto &s : js) {
-            Tree &out = *s.job->out;
-            for (int i = 0; i < out.nn(); i++)
-                if (out.nodes[i].child0 < 0) {
-                    bl.push_back(out.block(i));
-                    cnp.push_back(out.d_cn + (size_t)8 * i);
-                }
-        }
-        Packer pk;
-        pk.add(bl.data(), bl.size() * sizeof(double *));
-        pk.add(cnp.data(), cnp.size() * sizeof(double *));
-        pk.ship(ctx, arena);
-        k_norms(ctx.dbasis, (double *const *)pk.ptr(0), (double *const *)pk.ptr(1), (int)bl.size(), ctx.stream);
-        st.launches++;
-    }
-    for (auto &s : js) {
-        Tree &out = *s.job->out;
-        MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
-                                 ctx.stream));
-    }
     MWG_CUDA(cudaEventRecord(ev_span[2], ctx.stream));
     ctx.sync();
+    for (auto &p : cn_staging) std::copy(p.second, p.second + 8 * (size_t)p.first->nn(), p.first->cn.begin());
     arena.reset();
+    for (int g = 1; g < ngroups; g++) ctx.xarena[g - 1].reset();
     {
+        // levels: from the start to the last group's end; post: the groups' post-processing
+        // spans summed (they overlap other groups' levels)
         float a = 0.0f, c = 0.0f;
         MWG_CUDA(cudaEventElapsedTime(&a, ev_span[0], ev_span[1]));
-        MWG_CUDA(cudaEventElapsedTime(&c, ev_span[1], ev_span[2]));
         st.gpu_levels_ms += a;
-        st.gpu_post_ms += c;
+        for (int g = 0; g < ngroups; g++) {
+            MWG_CUDA(cudaEventElapsedTime(&c, ev_post[2 * g], ev_post[2 * g + 1]));
+            st.gpu_post_ms += c;
+        }
     }
+    for (auto &e : ev_post) cudaEventDestroy(e);
     for (auto &e : ev_span) cudaEventDestroy(e);
     if (ds.ev_counts) cudaEventDestroy(ds.ev_counts);
     st.kernel_ms += kernel_ms;
