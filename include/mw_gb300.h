@@ -81,8 +81,10 @@ typedef struct {
     double flops_fp32;       /* ... of the FP32 tier */
     double kernel_ms_fp64;   /* CUDA-event time of the FP64 contraction launches */
     double kernel_ms_fp32;   /* ... of the FP32 contraction launches */
-    double host_enum_ms;     /* host: candidate enumeration (screening bounds, lookups) */
-    double host_items_ms;    /* host: exact screening, tiers, item lists */
+    double host_enum_ms;     /* host: candidate enumeration (screening bounds, lookups); with GPU
+                                screening, the wait for the GPU's candidate counts */
+    double host_items_ms;    /* host: exact screening, tiers, item lists (GPU screening: the
+                                per-tier node lists built from the GPU's counts) */
     double host_wait_ms;     /* host: waiting for the level's kernels and norm downloads */
     double flops_tf32;       /* algorithmic flops of the TF32 tier */
     double kernel_ms_tf32;   /* CUDA-event time of the TF32 contraction launches */
@@ -93,7 +95,9 @@ typedef struct {
     double host_launch_ms;   /* host: ordering, chunking and packing the item lists, launches */
     double host_refine_ms;   /* host: refinement decisions after each level */
     double gpu_levels_ms;    /* GPU time from the call's first queued work to the end of its last level */
-    double gpu_post_ms;      /* GPU time of the post-processing (sum over scales, compression, norms) */
+    double gpu_post_ms;      /* GPU time of the post-processing (sum over scales, compression, norms),
+                                summed over the job groups, which overlap other groups' levels */
+    long long screen_regrows; /* GPU screening: levels walked again after a generation table filled up */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */
@@ -218,6 +222,12 @@ int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree x, mw_tree seed
  * (QMPotential.cpp:147; ExchangePotential.cpp:175,213,223); out's current grid is the start grid */
 int mw_multiply(double prec, mw_tree out, double coef, mw_tree a, mw_tree b, int max_iter, int abs_prec,
                 int use_max_norms);
+/* L2-adjoint of the fixed-grid product h = coef a b (mw_multiply with max_iter = 0 on h's grid)
+ * in its first factor: out <- coef P_a(seed b), the product of the seed (on h's grid) and b on the
+ * seed's grid, projected onto a's grid.  <seed, coef a b> = <out, a> to rounding.  No MRCPP
+ * counterpart: it is the transpose of mrcpp::multiply (QMPotential.cpp:147,
+ * density_utils.cpp:73) for gradients through orbital products and densities. */
+int mw_multiply_adjoint(double prec, mw_tree out, double coef, mw_tree a, mw_tree b, mw_tree seed);
 /* n independent products out_i = coef_i a_i b_i, level-synchronous (exchange pair products,
  * src/qmoperators/two_electron/ExchangePotential.cpp:175) */
 int mw_multiply_batch(int n, const double *precs, mw_tree *outs, const double *coefs, mw_tree *as, mw_tree *bs,

@@ -58,7 +58,8 @@ class Stats(C.Structure):
                 ("host_items_ms", C.c_double), ("host_wait_ms", C.c_double), ("flops_tf32", C.c_double),
                 ("kernel_ms_tf32", C.c_double), ("items_df", C.c_longlong), ("flops_df", C.c_double),
                 ("kernel_ms_df", C.c_double), ("host_gen_ms", C.c_double), ("host_launch_ms", C.c_double),
-                ("host_refine_ms", C.c_double), ("gpu_levels_ms", C.c_double), ("gpu_post_ms", C.c_double)]
+                ("host_refine_ms", C.c_double), ("gpu_levels_ms", C.c_double), ("gpu_post_ms", C.c_double),
+                ("screen_regrows", C.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -72,7 +73,7 @@ EXPORTS = [
     "mw_tree_download", "mw_tree_squared_norm", "mw_tree_integrate", "mw_tree_rescale", "mw_tree_eval",
     "mw_tree_clear", "mw_project_gauss", "mw_project_hydrogen", "mw_copy_grid", "mw_build_grid", "mw_copy_func",
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
-    "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint",
+    "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint", "mw_multiply_adjoint",
     "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
     "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap", "mw_ctx_set_groups", "mw_ctx_set_screening", "mw_apply_batch_autotune", "mw_op_create_helmholtz_batch",
     "mw_tree_upload_batch", "mw_tree_download_batch", "mw_pin_host", "mw_unpin_host",
@@ -137,6 +138,7 @@ def load_library(path=None):
         "mw_multiply_batch": [I, dp, pp, dp, pp, pp, I, I, I],
         "mw_apply_fixed": [D, P, P, P, I, I],
         "mw_apply_adjoint": [D, P, P, P, P, I],
+        "mw_multiply_adjoint": [D, P, D, P, P, P],
         "mw_multiply": [D, P, D, P, P, I, I, I],
         "mw_square": [D, P, P, I, I],
         "mw_add": [D, P, I, dp, pp, I],
@@ -545,6 +547,13 @@ def apply_fixed(prec, out, oper, inp, abs_prec=False, precision="fp64"):
 def apply_adjoint(prec, out, oper, x, seed):
     """L2-adjoint of the fixed-grid FP64 apply on seed's grid (absolute precision): out <- A^T seed on x's grid."""
     _check(_lib.mw_apply_adjoint(prec, out.ptr, oper.ptr, x.ptr, seed.ptr, 1), out.mra.ptr)
+    return out.mra.last_stats()
+
+
+def multiply_adjoint(prec, out, coef, a, b, seed):
+    """L2-adjoint of the fixed-grid product h = coef a b in a: out <- coef P_a(seed b) on a's grid
+    (seed on h's grid), so that <seed, coef a b> = <out, a>."""
+    _check(_lib.mw_multiply_adjoint(prec, out.ptr, coef, a.ptr, b.ptr, seed.ptr), out.mra.ptr)
     return out.mra.last_stats()
 
 

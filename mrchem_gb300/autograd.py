@@ -1,4 +1,5 @@
-"""torch.autograd wrapper of the Coulomb energy, for verifying the adjoint apply.
+"""torch.autograd wrappers of the Coulomb energy and of an orbital density, for verifying the
+adjoint apply and the adjoint multiply.
 
 J(rho) = 1/2 <rho, P rho> with P the fixed-grid FP64 Poisson apply on rho's grid.  The
 differentiable input is rho's vector of orthonormal coordinates on a fixed grid: the
@@ -95,3 +96,29 @@ class CoulombEnergy(torch.autograd.Function):
 
 def coulomb_energy(x, grid, oper, prec):
     return CoulombEnergy.apply(x, grid, oper, prec)
+
+
+class OrbitalDensity(torch.autograd.Function):
+    """rho = occ phi^2 on a fixed grid (mw_multiply with max_iter = 0 on phi's grid); backward
+    through the adjoint multiply: (d rho / d phi)^T g = 2 occ P_phi(g phi)."""
+
+    @staticmethod
+    def forward(ctx, x, grid, occ, prec):
+        phi = grid.to_tree(x.detach().cpu().numpy())
+        rho = mw.FunctionTree(grid.mra)
+        mw.copy_grid(rho, phi)
+        mw.multiply(prec, rho, occ, phi, phi, max_iter=0, abs_prec=True)
+        ctx.grid, ctx.occ, ctx.prec, ctx.phi = grid, occ, prec, phi
+        return torch.from_numpy(grid.to_vec(rho))
+
+    @staticmethod
+    def backward(ctx, g):
+        grid = ctx.grid
+        seed = grid.to_tree(g.detach().cpu().numpy())
+        adj = mw.FunctionTree(grid.mra)
+        mw.multiply_adjoint(ctx.prec, adj, 2.0 * ctx.occ, ctx.phi, ctx.phi, seed)
+        return torch.from_numpy(grid.to_vec(adj)), None, None, None
+
+
+def orbital_density(x, grid, occ, prec):
+    return OrbitalDensity.apply(x, grid, occ, prec)

@@ -631,6 +631,10 @@ void screen_level_gpu(Ctx &ctx, Arena &ar, DevScreen &ds, const std::vector<JobS
         JobState &s = *jp[j];
         long c = 256;
         while (c < 16 * (long)s.work.size()) c <<= 1;
+        if (ctx.screen_gen_slots > 0) {
+            c = 1;
+            while (c < ctx.screen_gen_slots) c <<= 1;
+        }
         gcap[j] = c;
         const double fm = BOUND_PRUNE * s.fmax_at(sidx);
         const double base = SCREEN_FAC * split_thr(s.job->prec, s.R, n);
@@ -706,7 +710,8 @@ void screen_level_gpu(Ctx &ctx, Arena &ar, DevScreen &ds, const std::vector<JobS
     {
         StreamSwap fast(ctx, ctx.fast);
         for (int attempt = 0;; attempt++) {
-            if (attempt == 3) throw Error(MW_ERR_STATE, "apply: generation tables of the GPU screening overflowed");
+            if (attempt > 0) st.screen_regrows++;
+            if (gtot > (1L << 26)) throw Error(MW_ERR_STATE, "apply: generation tables of the GPU screening overflowed");
             if (attempt > 0) {
                 gtot = 0;
                 for (size_t j = 0, q = 0; j < jp.size(); j++) {
@@ -1792,6 +1797,28 @@ void add(Tree &out, const std::vector<const Tree *> &trees, const std::vector<do
 // orbital's grid (refined adaptively at prec), the squares added on their union grid, and the
 // sum cropped at prec / N_el when crop is set.  The squares of all orbitals run as one batched
 // multiply.
+// ------------------------------------------------------------------ adjoint multiply
+// L2-adjoint of the fixed-grid product h = coef a b in its first factor.  The forward map
+// a -> h represents a at h's end nodes (generated from a's coarser leaves, or with a's finer
+// detail left out), multiplies the values at the children's quadrature points by b's and maps
+// them back; the value <-> coefficient maps are orthogonal, so the transpose is the same
+// product with the seed in place of a, on h's grid (the seed's), followed by the transpose of
+// the representation step: the projection onto a's grid (copy_func: compression where a's grid
+// is coarser, exact injection where it is finer).  out <- coef P_a (seed b), on a's grid.
+void multiply_adjoint(double prec, Tree &out, double coef, const Tree &a, Tree &b, Tree &seed, mw_stats &st) {
+    Ctx &ctx = *out.ctx;
+    if (a.ctx != &ctx || b.ctx != &ctx || seed.ctx != &ctx) throw Error(MW_ERR_ARG, "multiply adjoint: mixed contexts");
+    Tree t;
+    t.ctx = &ctx;
+    copy_grid(t, seed);
+    std::vector<MulJob> jobs{MulJob{&t, &seed, &b, coef, prec, 0, true, false}};
+    multiply_batch(jobs, st);
+    copy_grid(out, a);
+    copy_func(out, t, ctx.arena);
+    ctx.sync();
+    t.free_device();
+}
+
 void density(double prec, Tree &rho, const std::vector<Tree *> &orbs, const std::vector<double> &occ, bool crop_sum,
              mw_stats &st) {
     Ctx &ctx = *rho.ctx;

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -104,6 +105,7 @@ int mw_ctx_create(int device, int root_scale, const int corner[3], const int box
         return rc;
     }
     c->ctx.owner = c;
+    if (const char *e = std::getenv("MW_SCREEN_GEN_SLOTS")) c->ctx.screen_gen_slots = std::max(0L, std::atol(e));
     *out = c;
     return MW_OK;
 }
@@ -622,6 +624,19 @@ int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree x, mw_tree seed
         check_same(out->tree, seed->tree);
         mw_stats st{};
         mwg::apply_adjoint(prec, out->tree, op->op, x->tree, seed->tree, st);
+        ctx->last = st;
+    });
+}
+
+int mw_multiply_adjoint(double prec, mw_tree out, double coef, mw_tree a, mw_tree b, mw_tree seed) {
+    if (!out || !a || !b || !seed || !(prec > 0.0) || out == a || out == b || out == seed) return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(out);
+    return guard(ctx, [&] {
+        check_same(out->tree, a->tree);
+        check_same(out->tree, b->tree);
+        check_same(out->tree, seed->tree);
+        mw_stats st{};
+        mwg::multiply_adjoint(prec, out->tree, coef, a->tree, b->tree, seed->tree, st);
         ctx->last = st;
     });
 }

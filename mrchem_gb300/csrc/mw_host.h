@@ -184,6 +184,11 @@ struct Ctx {
     // where a batched apply enumerates, screens and lists its items: 1 on the GPU (mw_screen.cu,
     // the default), 0 on the host (OpenMP); both give the same items in the same order
     int screening = 1;
+    // first size of a job's generation table in the GPU screening (slots; 0: 16 x the job's
+    // output nodes at the level, at least 256).  A table that fills up is grown 8x and the level's
+    // walk repeated.  MW_SCREEN_GEN_SLOTS in the environment at context creation sets it, which
+    // the tests use to run the growth path.
+    long screen_gen_slots = 0;
     Arena sarena;  // per-apply tables of the GPU screening (input hash tables and norms)
     // launch settings of a batched apply: job groups, and the largest number of items one CTA
     // task takes per tier (FP64, FP32, TF32, double-FP32) before a node is split into chunks

@@ -3,7 +3,11 @@
 - dot-product test: <y, A x> = <A^T y, x> for the fixed-grid apply A (same item set);
 - dJ/drho for J = 1/2 <rho, P rho> equals the forward potential V (symmetric kernel);
 - dJ/dR (Gaussian centre, through torch.autograd and the adjoint) against central finite
-  differences with h = 1e-4 on the same fixed grid.
+  differences with h = 1e-4 on the same fixed grid;
+- adjoint multiply: <s, a b> = <M_b^T s, a> for the fixed-grid product on a grid finer than a's
+  in some boxes and coarser in others; the gradient of J(phi) = 1/2 <rho, P rho> with
+  rho = 2 phi^2 (torch.autograd through the adjoint multiply and the adjoint apply) against
+  central finite differences along a direction on phi's grid.
 """
 import math
 
@@ -126,3 +130,49 @@ def test_centre_gradient_vs_finite_differences(engine, setup):
     fd = np.array(fd)
     g = R.grad.numpy()
     assert np.abs(g - fd).max() <= 1e-3 * max(np.abs(fd).max(), 1e-3), (g, fd)
+
+
+def test_multiply_adjoint_dot_product(engine, setup):
+    mra, alphas, centres, rho, P = setup
+    prec = 1e-7
+    a = engine.project(prec, engine.FunctionTree(mra), [(1.0, 2.0, (0.3, -0.2, 0.1), (1, 0, 0))], abs_prec=True)
+    b = engine.project(prec, engine.FunctionTree(mra), [(0.8, 5.0, (-0.4, 0.2, 0.3), (0, 0, 0))], abs_prec=True)
+    # the product's grid: rho's (finer than a's in some boxes, coarser in others)
+    h = engine.FunctionTree(mra)
+    engine.copy_grid(h, rho)
+    engine.multiply(prec, h, 1.7, a, b, max_iter=0, abs_prec=True)
+    s = on_grid(engine, mra, rho, [(1.0, 0.9, (0.2, 0.1, -0.5), (0, 1, 0)), (0.5, 6.0, (-0.3, 0.4, 0.2), (0, 0, 0))])
+    out = engine.FunctionTree(mra)
+    engine.multiply_adjoint(prec, out, 1.7, a, b, s)
+    ka, _, _ = a.download()
+    ko, _, _ = out.download()
+    assert np.array_equal(ka, ko)  # on a's grid
+    lhs, rhs = engine.dot(s, h), engine.dot(out, a)
+    assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), 1e-300), (lhs, rhs)
+
+
+def test_density_gradient_vs_finite_differences(engine, setup):
+    torch = pytest.importorskip("torch")
+    from mrchem_gb300.autograd import FixedGrid, coulomb_energy, orbital_density
+    mra, alphas, centres, rho, P = setup
+    prec = 1e-7
+    phi = engine.project(prec, engine.FunctionTree(mra),
+                         [(1.0, 1.5, (0.2, -0.1, 0.3), (0, 0, 0)), (0.6, 4.0, (-0.5, 0.4, -0.2), (0, 0, 1))],
+                         abs_prec=True)
+    grid = FixedGrid(mra, phi.download()[0])
+    x = torch.from_numpy(grid.to_vec(phi)).requires_grad_(True)
+    J = coulomb_energy(orbital_density(x, grid, 2.0, prec), grid, P, PREC)
+    J.backward()
+    # direction: a Gaussian-polynomial projected on phi's grid
+    d = torch.from_numpy(grid.to_vec(on_grid(engine, mra, phi, [(1.0, 2.5, (0.1, 0.2, -0.2), (1, 1, 0))])))
+    h = 1e-3
+    vals = []
+    for sgn in (1, -1):
+        xs = (x.detach() + sgn * h * d).clone()
+        vals.append(float(coulomb_energy(orbital_density(xs, grid, 2.0, prec), grid, P, PREC)))
+    fd = (vals[0] - vals[1]) / (2 * h)
+    an = float(x.grad @ d)
+    # J is quartic in phi, so the central difference carries an h^2 term (about 1e-6 relative
+    # here), and the screened apply's item set follows rho's norms (items near the threshold,
+    # about prec relative, over 2h); an error in either adjoint would be of order one
+    assert abs(an - fd) <= 1e-4 * abs(fd), (an, fd)

@@ -163,3 +163,29 @@ def test_gpu_screening_rerun_bit_identical(engine, helmholtz_batch):
         runs.append(outs)
     for a, b in zip(*runs):
         assert same_trees(a, b)
+
+
+def test_generation_tables_grow(engine, monkeypatch):
+    # generation tables of two slots per job fill up on the first levels: the walk is repeated with
+    # tables 8x larger until every missing input has a slot, and the items stay the host's
+    prec = 1e-6
+    rng = np.random.default_rng(SEED)
+    monkeypatch.setenv("MW_SCREEN_GEN_SLOTS", "2")
+    mra = engine.MultiResolutionAnalysis(9)
+    monkeypatch.delenv("MW_SCREEN_GEN_SLOTS")
+    orbs = []
+    for terms in poly_orbitals(rng, 4, 0.3, 20.0):
+        f = engine.project(prec, engine.FunctionTree(mra), terms, abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        orbs.append(f)
+    eps = rng.uniform(-2.0, -0.1, 4)
+    ops = [engine.HelmholtzOperator(mra, math.sqrt(-2.0 * e), prec) for e in eps]
+
+    def run():
+        outs = [engine.FunctionTree(mra) for _ in orbs]
+        engine.apply_batch([prec] * len(orbs), outs, ops, orbs, abs_prec=True, precision="mixed")
+        return outs
+
+    res = both(engine, mra, run)
+    check_identical(res)
+    assert res[1][1]["screen_regrows"] > 0 and res[1][1]["generated"] > 0
