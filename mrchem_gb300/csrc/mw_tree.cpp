@@ -627,18 +627,37 @@ void tree_upload_batch(const std::vector<Tree *> &trees, const int *nnodes, cons
     const int bs = ctx.basis.bs, n = (int)trees.size();
     std::vector<std::vector<int>> from(n);
     std::vector<size_t> first(n + 1, 0);
-    for (int i = 0; i < n; i++) {
-        from[i] = upload_structure(*trees[i], nnodes[i], keys[i]);
-        first[i + 1] = first[i] + (size_t)nnodes[i];
-    }
+    for (int i = 0; i < n; i++) first[i + 1] = first[i] + (size_t)nnodes[i];
+    // the trees' device arrays are sized first, so that building the structures below is host
+    // work only and runs for all trees in parallel
+    for (int i = 0; i < n; i++) trees[i]->reserve((size_t)nnodes[i]);
     ctx.sync();
+    auto structures = [&] {
+        std::vector<std::string> err(n);
+        std::vector<int> code(n, MW_OK);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int i = 0; i < n; i++) {
+            try {
+                from[i] = upload_structure(*trees[i], nnodes[i], keys[i]);
+            } catch (const Error &e) {
+                code[i] = e.code;
+                err[i] = e.what();
+            }
+        }
+        for (int i = 0; i < n; i++)
+            if (code[i] != MW_OK) throw Error(code[i], err[i]);
+    };
     bool pinned = true;
     for (int i = 0; i < n && pinned; i++) pinned = host_is_pinned(coefs[i]);
     if (pinned) {
-        // the caller's blocks go straight to device scratch; the permutation into tree order
-        // runs on the device
+        // the caller's blocks go straight to device scratch while the host builds the trees'
+        // structures; the permutation into tree order runs on the device
         arena.reset();
         double *scratch = (double *)arena.alloc(sizeof(double) * (size_t)bs * first[n]);
+        for (int i = 0; i < n; i++)
+            MWG_CUDA(cudaMemcpyAsync(scratch + first[i] * bs, coefs[i], sizeof(double) * (size_t)bs * nnodes[i],
+                                     cudaMemcpyHostToDevice, ctx.stream));
+        structures();
         std::vector<int> maps;
         maps.reserve(first[n]);
         for (int i = 0; i < n; i++) maps.insert(maps.end(), from[i].begin(), from[i].end());
@@ -646,14 +665,12 @@ void tree_upload_batch(const std::vector<Tree *> &trees, const int *nnodes, cons
         pk.add(maps.data(), maps.size() * sizeof(int));
         pk.ship(ctx, arena);
         const int *dmap = (const int *)pk.ptr(0);
-        for (int i = 0; i < n; i++) {
-            MWG_CUDA(cudaMemcpyAsync(scratch + first[i] * bs, coefs[i], sizeof(double) * (size_t)bs * nnodes[i],
-                                     cudaMemcpyHostToDevice, ctx.stream));
+        for (int i = 0; i < n; i++)
             k_permute_blocks(trees[i]->d_coefs, scratch + first[i] * bs, dmap + first[i], nnodes[i], bs, ctx.stream);
-        }
         tree_norms_batch(trees, nnodes, arena);
         return;
     }
+    structures();
     double *h = (double *)ctx.pinned(sizeof(double) * (size_t)bs * first[n]);
     std::vector<std::pair<int, int>> all;  // (tree, node)
     all.reserve(first[n]);
@@ -707,6 +724,7 @@ void tree_download_batch(const std::vector<Tree *> &trees, int *const *keys, dou
     std::vector<std::vector<int>> idx(n);
     std::vector<size_t> first(n + 1, 0);
     for (int i = 0; i < n; i++) first[i + 1] = first[i] + (size_t)trees[i]->nn();
+#pragma omp parallel for schedule(dynamic, 1)
     for (int i = 0; i < n; i++) idx[i] = canonical_order(*trees[i]);
     bool pinned = true;
     for (int i = 0; i < n && pinned; i++) pinned = !coefs[i] || host_is_pinned(coefs[i]);
