@@ -202,6 +202,17 @@ int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const m
 int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *nprec,
                    const mw_tree *prec_trees, int max_iter, int abs_prec, int precision_mode);
 /* apply on a fixed output grid (the output's current grid, no refinement) */
+/* mw_tree_upload_batch of the inputs followed by mw_apply_batch (no precision trees), with the
+ * upload overlapped: each job group's input blocks go up on the group's stream, and a group starts
+ * computing as soon as its own inputs have landed, while the copy engine still moves the later
+ * groups' blocks.  in_keys / in_coefs as in mw_tree_upload_batch.  The overlap needs distinct input
+ * trees that are not outputs, and coefficient buffers pinned with mw_pin_host; otherwise the inputs
+ * go up first.  Results are bit-identical to the two calls.  The reference has no counterpart
+ * (HelmholtzVector::operator(), src/scf_solver/HelmholtzVector.cpp:70-91, applies orbitals that
+ * already live in memory). */
+int mw_apply_batch_host(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *in_nnodes,
+                        const int *const *in_keys, const double *const *in_coefs, int max_iter, int abs_prec,
+                        int precision_mode);
 /* Autotuner of the batched apply's launch settings (no counterpart in the reference): runs the
  * batch (as mw_apply_batch with no precision trees and max_iter = -1) `repeats` times for each
  * candidate -- job groups 2..6, then the chunk size of the TF32, FP32 and double-FP32 tiers, one

@@ -73,7 +73,7 @@ EXPORTS = [
     "mw_tree_download", "mw_tree_squared_norm", "mw_tree_integrate", "mw_tree_rescale", "mw_tree_eval",
     "mw_tree_clear", "mw_project_gauss", "mw_project_hydrogen", "mw_copy_grid", "mw_build_grid", "mw_copy_func",
     "mw_crop", "mw_dot", "mw_op_create_poisson", "mw_op_create_helmholtz", "mw_op_destroy", "mw_op_nterms",
-    "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint", "mw_multiply_adjoint",
+    "mw_op_terms", "mw_op_band", "mw_op_block", "mw_apply", "mw_apply_batch", "mw_apply_fixed", "mw_apply_adjoint", "mw_multiply_adjoint", "mw_apply_batch_host",
     "mw_multiply", "mw_multiply_batch", "mw_square", "mw_add", "mw_probe_fma_peak", "mw_density", "mw_rotate",
     "mw_tree_save", "mw_tree_load", "mw_probe_mma_peak", "mw_dot_noalloc", "mw_ctx_set_overlap", "mw_ctx_set_groups", "mw_ctx_set_screening", "mw_apply_batch_autotune", "mw_op_create_helmholtz_batch",
     "mw_tree_upload_batch", "mw_tree_download_batch", "mw_pin_host", "mw_unpin_host",
@@ -139,6 +139,7 @@ def load_library(path=None):
         "mw_apply_fixed": [D, P, P, P, I, I],
         "mw_apply_adjoint": [D, P, P, P, P, I],
         "mw_multiply_adjoint": [D, P, D, P, P, P],
+        "mw_apply_batch_host": [I, P, P, P, P, P, P, P, I, I, I],
         "mw_multiply": [D, P, D, P, P, I, I, I],
         "mw_square": [D, P, P, I, I],
         "mw_add": [D, P, I, dp, pp, I],
@@ -526,6 +527,22 @@ def autotune_batch(precs, outs, opers, inps, abs_prec=False, precision="mixed", 
                                         _PREC[precision], int(repeats), _ip(g), ch, _dp(ms)), outs[0].mra.ptr)
     return {"groups": int(g[0]), "chunk": {"fp64": ch[0], "fp32": ch[1], "tf32": ch[2], "df32": ch[3]},
             "ms": float(ms[0])}
+
+
+def apply_batch_host(precs, outs, opers, inps, inputs, max_iter=-1, abs_prec=False, precision="fp64"):
+    """upload_batch(inps, inputs) then apply_batch(...) as one call (mw_apply_batch_host): each job
+    group's inputs go up on its own stream and the group starts once they have landed.  inputs:
+    (keys, coefs, ...) per job, coefs pinned with pin_host for the overlap."""
+    n = len(outs)
+    p = np.ascontiguousarray(precs if np.ndim(precs) else [precs] * n, dtype=np.float64)
+    ks = [np.ascontiguousarray(x[0], dtype=np.int32) for x in inputs]
+    cs = [np.ascontiguousarray(x[1], dtype=np.float64) for x in inputs]
+    nn = np.ascontiguousarray([k.shape[0] for k in ks], dtype=np.int32)
+    kp = (C.c_void_p * n)(*[k.ctypes.data for k in ks])
+    cp = (C.c_void_p * n)(*[c.ctypes.data for c in cs])
+    _check(_lib.mw_apply_batch_host(n, _dp(p), _ptrs(outs), _ptrs(opers), _ptrs(inps), _ip(nn), kp, cp, max_iter,
+                                    int(abs_prec), _PREC[precision]), outs[0].mra.ptr)
+    return outs[0].mra.last_stats()
 
 
 def multiply_batch(precs, outs, coefs, as_, bs_, max_iter=-1, abs_prec=False, use_max_norms=False):

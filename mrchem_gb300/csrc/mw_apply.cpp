@@ -499,26 +499,15 @@ double oper_norm_max(const Oper &op) {
     return m;
 }
 
-// Builds the per-apply tables on the context's stream; false when an operator falls outside what
-// the kernels encode (bands above 32767), and the host screens instead.
-bool screen_setup(Ctx &ctx, std::vector<ApplyJob> &jobs, DevScreen &ds) {
-    const Basis &b = ctx.basis;
-    // levels whose translations fit the generation tables' 21-bit fields (deeper levels, about
-    // 20 scales below the root, are screened on the host)
-    ds.levels = 0;
-    while (ds.levels < 40) {
-        bool fits = true;
-        for (int d = 0; d < 3; d++) fits &= ((long)b.boxes[d] << ds.levels) < (1L << 21);
-        if (!fits) break;
-        ds.levels++;
-    }
-    for (ApplyJob &job : jobs)
-        if (!oper_screen_tables(*job.op)) return false;
-    // one hash table and norm copy per distinct input tree
+// The per-job tables that need the input trees' norms: a hash table of each input tree's keys and
+// its component and block norms (FP64 and FP32), and the jobs' ScreenJob entries, uploaded on the
+// context's current stream.  `idx`: the jobs to set up (all of them, or one job group's when the
+// group's inputs arrive during the apply).
+void screen_setup_inputs(Ctx &ctx, std::vector<ApplyJob> &jobs, const std::vector<int> &idx, DevScreen &ds) {
     std::vector<const Tree *> trees;
     std::unordered_map<const Tree *, int> tix;
-    for (ApplyJob &job : jobs)
-        if (tix.emplace(job.inp, (int)trees.size()).second) trees.push_back(job.inp);
+    for (int j : idx)
+        if (tix.emplace(jobs[j].inp, (int)trees.size()).second) trees.push_back(jobs[j].inp);
     std::vector<size_t> cap(trees.size()), off(trees.size() + 1, 0);
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     for (size_t i = 0; i < trees.size(); i++) {
@@ -528,11 +517,9 @@ bool screen_setup(Ctx &ctx, std::vector<ApplyJob> &jobs, DevScreen &ds) {
         off[i + 1] = off[i] + al(c * sizeof(int4)) + al(c * sizeof(int)) + al(sizeof(double) * 9 * trees[i]->nn()) +
                      al(sizeof(float) * 9 * trees[i]->nn());
     }
-    const size_t jb = al(sizeof(ScreenJob) * jobs.size());
-    const size_t total = off.back() + jb;
+    const size_t total = off.back() + al(sizeof(ScreenJob) * idx.size());
     char *h = (char *)ctx.sarena.halloc(total);
     char *d = (char *)ctx.sarena.alloc(total);
-    std::vector<ScreenJob> sj(jobs.size());
     for (size_t i = 0; i < trees.size(); i++) {
         const Tree &t = *trees[i];
         const size_t c = cap[i];
@@ -555,11 +542,13 @@ bool screen_setup(Ctx &ctx, std::vector<ApplyJob> &jobs, DevScreen &ds) {
         float *cn32 = (float *)((char *)cn + al(sizeof(double) * 9 * t.nn()));
         for (size_t e = 0; e < 9 * (size_t)t.nn(); e++) cn32[e] = (float)cn[e];
     }
-    for (size_t j = 0; j < jobs.size(); j++) {
+    ScreenJob *hj = (ScreenJob *)(h + off.back());
+    for (size_t q = 0; q < idx.size(); q++) {
+        const int j = idx[q];
         const int i = tix[jobs[j].inp];
         const Tree &t = *trees[i];
         const size_t c = cap[i];
-        ScreenJob &J = sj[j];
+        ScreenJob &J = hj[q];
         J.op = oper_screen_view(*jobs[j].op);
         J.hkey = (const int4 *)(d + off[i]);
         J.hval = (const int *)(d + off[i] + al(c * sizeof(int4)));
@@ -569,16 +558,49 @@ bool screen_setup(Ctx &ctx, std::vector<ApplyJob> &jobs, DevScreen &ds) {
         J.bn = J.cn + 8 * (size_t)t.nn();
         J.cn32 = (const float *)((const char *)J.cn + al(sizeof(double) * 9 * t.nn()));
         J.bn32 = J.cn32 + 8 * (size_t)t.nn();
-        ds.op_max.push_back(oper_norm_max(*jobs[j].op));
         J.in64 = t.d_coefs;
         J.in32 = t.d_coefs32;
         J.intc = t.d_coefs_tc;
-        ds.maxT = std::max(ds.maxT, jobs[j].op->T);
     }
-    std::memcpy(h + off.back(), sj.data(), sizeof(ScreenJob) * sj.size());
-    MWG_CUDA(cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, ctx.stream));
-    ds.djobs = (ScreenJob *)(d + off.back());
+    MWG_CUDA(cudaMemcpyAsync(d, h, off.back(), cudaMemcpyHostToDevice, ctx.stream));
+    // the entries go to their jobs' places in the apply's ScreenJob array (contiguous runs copied
+    // together)
+    for (size_t q = 0; q < idx.size();) {
+        size_t r = q + 1;
+        while (r < idx.size() && idx[r] == idx[r - 1] + 1) r++;
+        MWG_CUDA(cudaMemcpyAsync(ds.djobs + idx[q], hj + q, sizeof(ScreenJob) * (r - q), cudaMemcpyHostToDevice,
+                                 ctx.stream));
+        q = r;
+    }
+}
+
+// The per-apply part that needs no input data: the levels the GPU screens, the operators' tables,
+// and the ScreenJob array; false when an operator falls outside what the kernels encode (bands
+// above 32767), and the host screens instead.  With `inputs_now` the input tables are built too.
+bool screen_setup(Ctx &ctx, std::vector<ApplyJob> &jobs, DevScreen &ds, bool inputs_now) {
+    const Basis &b = ctx.basis;
+    // levels whose translations fit the generation tables' 21-bit fields (deeper levels, about
+    // 20 scales below the root, are screened on the host)
+    ds.levels = 0;
+    while (ds.levels < 40) {
+        bool fits = true;
+        for (int d = 0; d < 3; d++) fits &= ((long)b.boxes[d] << ds.levels) < (1L << 21);
+        if (!fits) break;
+        ds.levels++;
+    }
+    for (ApplyJob &job : jobs)
+        if (!oper_screen_tables(*job.op)) return false;
+    for (ApplyJob &job : jobs) {
+        ds.op_max.push_back(oper_norm_max(*job.op));
+        ds.maxT = std::max(ds.maxT, job.op->T);
+    }
+    ds.djobs = (ScreenJob *)ctx.sarena.alloc(sizeof(ScreenJob) * jobs.size());
     if (!ds.ev_counts) MWG_CUDA(cudaEventCreateWithFlags(&ds.ev_counts, cudaEventDisableTiming));
+    if (inputs_now) {
+        std::vector<int> all(jobs.size());
+        for (size_t j = 0; j < jobs.size(); j++) all[j] = (int)j;
+        screen_setup_inputs(ctx, jobs, all, ds);
+    }
     ds.on = true;
     return true;
 }
@@ -587,11 +609,6 @@ struct TierRule {  // the apply's precision mode, as the tier choice reads it
     bool mixed, near_fp64, df_only, dfp, tensor;
 };
 
-// One level of a job group screened on the GPU (mw_screen.cu).  The walk, the generation of
-// missing inputs, the exact screening, the tiers and the item arrays run on the high-priority
-// stream; the host reads back two small arrays (per-node candidate counts, then per-node tier
-// counts), from which it sizes the buffers and builds each tier's node list exactly as the host
-// screening does.  The group's stream waits for the item arrays with an event.
 // the walk kernels' (t, lz) rows at a scale: the most over the group's operators
 int level_zrows(const std::vector<JobState *> &jp, int sidx) {
     int zmax = 1;
@@ -608,6 +625,11 @@ int level_zrows(const std::vector<JobState *> &jp, int sidx) {
 }
 constexpr size_t SCREEN_SMEM_MAX = 96 * 1024;  // larger walks (very wide bands) are screened on the host
 
+// One level of a job group screened on the GPU (mw_screen.cu).  The walk, the generation of
+// missing inputs, the exact screening, the tiers and the item arrays run on the high-priority
+// stream; the host reads back two small arrays (per-node candidate counts, then per-node tier
+// counts), from which it sizes the buffers and builds each tier's node list exactly as the host
+// screening does.  The group's stream waits for the item arrays with an event.
 void screen_level_gpu(Ctx &ctx, Arena &ar, DevScreen &ds, const std::vector<JobState *> &jp,
                       const std::vector<int> &jglob, int level, int zmax, const TierRule &rule, LevelItems *lt,
                       DevItems &dv, mw_stats &st, double &t_enum, double &t_gen, double &t_items) {
@@ -773,9 +795,9 @@ void screen_level_gpu(Ctx &ctx, Arena &ar, DevScreen &ds, const std::vector<JobS
     const size_t ng = (size_t)std::max(ngen, 1);
     P.gcn = (double *)ar.alloc(sizeof(double) * 8 * ng);
     P.gcn32 = (float *)ar.alloc(sizeof(float) * 8 * ng);
-    P.g64 = (const double *)ar.alloc(sizeof(double) * (size_t)bs * ng);
-    P.g32 = rule.mixed ? (const float *)ar.alloc(sizeof(float) * 2 * (size_t)bs * ng) : nullptr;
-    P.gtc = rule.tensor ? (const float *)ar.alloc(sizeof(float) * P.tx * ng) : nullptr;
+    P.g64 = (double *)ar.alloc(sizeof(double) * (size_t)bs * ng);
+    P.g32 = rule.mixed ? (float *)ar.alloc(sizeof(float) * 2 * (size_t)bs * ng) : nullptr;
+    P.gtc = rule.tensor ? (float *)ar.alloc(sizeof(float) * P.tx * ng) : nullptr;
     int *hs = (int *)ar.halloc(sizeof(int) * (8 * (size_t)NN + 1));
     {
         StreamSwap fast(ctx, ctx.fast);
@@ -793,10 +815,10 @@ void screen_level_gpu(Ctx &ctx, Arena &ar, DevScreen &ds, const std::vector<JobS
             st.launches += 3;
             st.generated += ngen;
             if (rule.mixed) {
-                k_to_fp32_cube(P.g64, const_cast<float *>(P.g32), (size_t)ngen, K, ctx.stream);
+                k_to_fp32_cube(P.g64, P.g32, (size_t)ngen, K, ctx.stream);
                 st.launches++;
                 if (rule.tensor) {
-                    k_to_tc_x(P.g32, const_cast<float *>(P.gtc), (size_t)ngen, K, ctx.stream);
+                    k_to_tc_x(P.g32, P.gtc, (size_t)ngen, K, ctx.stream);
                     st.launches++;
                 }
             }
@@ -868,7 +890,8 @@ void check_status(const int *hs) {
 
 }  // namespace
 
-void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st) {
+void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st,
+                 const HostInputs *hin) {
     if (jobs.empty()) return;
     Ctx &ctx = *jobs[0].out->ctx;
     const Basis &b = ctx.basis;
@@ -888,6 +911,23 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     for (auto &e : ev_span) MWG_CUDA(cudaEventCreate(&e));
     MWG_CUDA(cudaEventRecord(ev_span[0], ctx.stream));
 
+    // the reduced tiers' copies of an input tree's blocks (FP32 cube-order shadows, and the TF32
+    // tier's x-pass operand), on the context's current stream
+    auto convert_input = [&](Tree &in) {
+        k_to_fp32_cube(in.d_coefs, in.d_coefs32, (size_t)in.nn(), b.K, ctx.stream);
+        st.launches++;
+        if (tensor) {
+            k_to_tc_x(in.d_coefs32, in.d_coefs_tc, (size_t)in.nn(), b.K, ctx.stream);
+            st.launches++;
+        }
+    };
+    // host inputs: the input trees' structures now (host work), their blocks per job group below
+    std::vector<std::vector<int>> in_maps;
+    if (hin) {
+        std::vector<Tree *> itrees;
+        for (ApplyJob &job : jobs) itrees.push_back(job.inp);
+        in_maps = upload_structures(itrees, hin->nnodes.data(), hin->keys.data());
+    }
     std::vector<JobState> js(jobs.size());
     int max_levels = 0;
     for (size_t j = 0; j < jobs.size(); j++) {
@@ -896,7 +936,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         s.job = &job;
         if (job.inp->ctx != &ctx || job.out->ctx != &ctx || job.op->ctx != &ctx)
             throw Error(MW_ERR_ARG, "apply: trees and operator must belong to one context");
-        s.set_fmax(*job.inp, b.n0);
+        if (!hin) s.set_fmax(*job.inp, b.n0);  // with host inputs: when the job's group has them
         if (!fixed_grid && job.out->nn() != job.out->nroots)
             throw Error(MW_ERR_STATE, "apply: output tree must be empty");
         // every tier adds into the output blocks: they start at zero (on a fixed grid too, whose
@@ -909,17 +949,12 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                 MWG_CUDA(cudaMalloc(&in.d_coefs32, sizeof(float) * 2 * (size_t)bs * in.cap));
                 in.cap32 = in.cap;
             }
-            k_to_fp32_cube(in.d_coefs, in.d_coefs32, (size_t)in.nn(), b.K, ctx.stream);
-            st.launches++;
-            if (tensor) {
-                if (in.cap_tc < (size_t)in.nn()) {
-                    if (in.d_coefs_tc) cudaFree(in.d_coefs_tc);
-                    MWG_CUDA(cudaMalloc(&in.d_coefs_tc, sizeof(float) * tc5_x_floats(b.K) * in.cap));
-                    in.cap_tc = in.cap;
-                }
-                k_to_tc_x(in.d_coefs32, in.d_coefs_tc, (size_t)in.nn(), b.K, ctx.stream);
-                st.launches++;
+            if (tensor && in.cap_tc < (size_t)in.nn()) {
+                if (in.d_coefs_tc) cudaFree(in.d_coefs_tc);
+                MWG_CUDA(cudaMalloc(&in.d_coefs_tc, sizeof(float) * tc5_x_floats(b.K) * in.cap));
+                in.cap_tc = in.cap;
             }
+            if (!hin) convert_input(in);
         }
         for (int i = 0; i < job.out->nroots; i++) s.work.push_back(i);
         if (fixed_grid) max_levels = std::max(max_levels, job.out->max_scale() - b.n0 + 1);
@@ -930,7 +965,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     DevScreen ds;
     if (ctx.screening == 1) {
         ctx.sarena.reset();
-        screen_setup(ctx, jobs, ds);
+        screen_setup(ctx, jobs, ds, hin == nullptr);
     }
     // fixed grid: per level, the output's nodes at that scale
     auto fixed_level_nodes = [&](JobState &s, int n) {
@@ -953,6 +988,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         cudaEvent_t ev[NTIER + 1];
         std::vector<int *> status;  // pinned copies of the launches' status words
         std::vector<double *> h_cn;  // pinned staging of each job's component norms
+        cudaEvent_t ev_in = nullptr;  // host inputs: the group's input blocks and norms have landed
+        double *in_cn = nullptr;      // ... their norms, staged for the host
     };
     // launch settings: the autotuner's for this (order, jobs, mode) if it ran, else the context's
     Ctx::Tuning tune;
@@ -1004,6 +1041,23 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     }
     for (auto &g : groups)
         for (auto &e : g.ev) MWG_CUDA(cudaEventCreate(&e));
+    // host inputs: each group's input blocks go up on the group's stream, in group order, so that
+    // the first groups compute while the copy engine still moves the later groups' blocks
+    if (hin)
+        for (auto &G : groups) {
+            StreamSwap swap(ctx, G.stream);
+            std::vector<Tree *> trees;
+            std::vector<const int *> maps;
+            std::vector<const double *> coefs;
+            for (int j : G.jobs) {
+                trees.push_back(jobs[j].inp);
+                maps.push_back(in_maps[j].data());
+                coefs.push_back(hin->coefs[j]);
+            }
+            G.in_cn = upload_enqueue(trees, maps, coefs, *G.arena);
+            MWG_CUDA(cudaEventCreateWithFlags(&G.ev_in, cudaEventDisableTiming));
+            MWG_CUDA(cudaEventRecord(G.ev_in, ctx.stream));
+        }
 
     // host phases of the group's next level and its launches; false when the group has no work left
     auto launch_level = [&](Group &G) -> bool {
@@ -1016,6 +1070,23 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         if (fixed_grid) {
             if (level >= max_levels) return false;
             for (JobState *sp : jp) fixed_level_nodes(*sp, n);
+        }
+        if (hin && level == 0) {
+            // the group's inputs have landed: their norms to the host, then what the apply derives
+            // from them (pruning norms per level, reduced-precision copies, screening tables)
+            MWG_CUDA(cudaEventSynchronize(G.ev_in));
+            size_t off = 0;
+            for (int j : G.jobs) {
+                Tree &in = *jobs[j].inp;
+                std::copy(G.in_cn + off, G.in_cn + off + 8 * (size_t)in.nn(), in.cn.begin());
+                off += 8 * (size_t)in.nn();
+                js[j].set_fmax(in, b.n0);
+                if (mixed) convert_input(in);
+            }
+            if (ds.on) screen_setup_inputs(ctx, jobs, G.jobs, ds);
+            // the screening and generation kernels run on the high-priority stream and read what
+            // was just written on the group's stream (input blocks, norms, reduced copies, tables)
+            MWG_CUDA(cudaStreamSynchronize(ctx.stream));
         }
         bool any = false;
         for (JobState *sp : jp) any |= !sp->work.empty();
@@ -1465,6 +1536,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         }
     }
     for (auto &e : ev_post) cudaEventDestroy(e);
+    for (auto &G : groups)
+        if (G.ev_in) cudaEventDestroy(G.ev_in);
     for (auto &e : ev_span) cudaEventDestroy(e);
     if (ds.ev_counts) cudaEventDestroy(ds.ev_counts);
     st.kernel_ms += kernel_ms;

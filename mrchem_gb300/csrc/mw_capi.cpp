@@ -538,6 +538,49 @@ int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tre
     });
 }
 
+int mw_apply_batch_host(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *in_nnodes,
+                        const int *const *in_keys, const double *const *in_coefs, int max_iter, int abs_prec,
+                        int precision_mode) {
+    if (n < 1 || !precs || !outs || !ops || !inps || !in_nnodes || !in_keys || !in_coefs) return MW_ERR_ARG;
+    if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_DF) return MW_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (!outs[i] || !ops[i] || !inps[i] || !(precs[i] > 0.0) || outs[i] == inps[i] || in_nnodes[i] < 1 ||
+            !in_keys[i] || !in_coefs[i])
+            return MW_ERR_ARG;
+    mwg::Ctx *ctx = ctx_of(outs[0]);
+    return guard(ctx, [&] {
+        std::vector<mwg::ApplyJob> jobs(n);
+        std::vector<mwg::Tree *> itrees(n);
+        for (int i = 0; i < n; i++) {
+            check_same(outs[i]->tree, inps[i]->tree);
+            jobs[i] = mwg::ApplyJob{&outs[i]->tree, &ops[i]->op, &inps[i]->tree, precs[i], abs_prec != 0, max_iter, {}};
+            itrees[i] = &inps[i]->tree;
+        }
+        // the per-group upload needs distinct input trees, not among the outputs, and pinned blocks;
+        // otherwise the inputs go up first and the apply follows (the same results)
+        bool overlap = true;
+        std::vector<mwg::Tree *> sorted = itrees;
+        std::sort(sorted.begin(), sorted.end());
+        overlap &= std::adjacent_find(sorted.begin(), sorted.end()) == sorted.end();
+        for (int i = 0; i < n && overlap; i++) {
+            overlap &= !std::binary_search(sorted.begin(), sorted.end(), &outs[i]->tree);
+            overlap &= mwg::host_is_pinned(in_coefs[i]);
+        }
+        mw_stats st{};
+        if (overlap) {
+            mwg::HostInputs hin;
+            hin.nnodes.assign(in_nnodes, in_nnodes + n);
+            hin.keys.assign(in_keys, in_keys + n);
+            hin.coefs.assign(in_coefs, in_coefs + n);
+            mwg::apply_batch(jobs, precision_mode, false, st, &hin);
+        } else {
+            mwg::tree_upload_batch(itrees, in_nnodes, in_keys, in_coefs, ctx->arena);
+            mwg::apply_batch(jobs, precision_mode, false, st);
+        }
+        ctx->last = st;
+    });
+}
+
 int mw_apply_batch_autotune(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, int abs_prec,
                             int precision_mode, int repeats, int *groups, long long *chunks, double *ms) {
     if (n < 1 || !precs || !outs || !ops || !inps || repeats < 1 || repeats > 20) return MW_ERR_ARG;

@@ -433,8 +433,8 @@ struct ScreenLevel {
     long long *tier_tot;        // [4]
     const void **in, **ax, **ay, **az;  // item arrays, the tiers one after the other
     double *coef;
-    const double *g64;          // generated blocks and their shadows
-    const float *g32, *gtc;
+    double *g64;                // generated blocks and their shadows
+    float *g32, *gtc;
     size_t tx, tb;              // floats per block in the TF32 layouts (input, operator)
 };
 // shared memory of the walk kernels: maxT = most terms of an operator, zmax = most (t, lz) rows of

@@ -69,7 +69,24 @@ struct MulJob {
     bool abs_prec, use_max_norms;
 };
 
-void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st);
+// host inputs of a batched apply: per job, the input tree's keys and the caller's pinned
+// coefficient blocks (in the keys' order); the input trees must be distinct
+struct HostInputs {
+    std::vector<int> nnodes;
+    std::vector<const int *> keys;
+    std::vector<const double *> coefs;
+};
+void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st,
+                 const HostInputs *hin = nullptr);
+// the trees' structures from their keys, all trees in parallel (host work; the device arrays are
+// sized first); per tree, the caller's block index of each tree node
+std::vector<std::vector<int>> upload_structures(const std::vector<Tree *> &trees, const int *nnodes,
+                                                const int *const *keys);
+// on the context's current stream: the caller's pinned blocks into the trees (permuted into tree
+// order), the trees' norms, and the norms' download into pinned staging, returned (8 per node,
+// tree after tree); read it after the stream has passed this point
+double *upload_enqueue(const std::vector<Tree *> &trees, const std::vector<const int *> &maps,
+                       const std::vector<const double *> &coefs, Arena &arena);
 void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st);
 void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats &st);
 void multiply_adjoint(double prec, Tree &out, double coef, const Tree &a, Tree &b, Tree &seed, mw_stats &st);

@@ -536,7 +536,7 @@ __global__ void gen_tasks_kernel(ScreenLevel P, GenTask *tasks, int ngen) {
     const int an = gi[2];
     GenTask tk;
     tk.anc = J.in64 + (size_t)gi[1] * P.bs;
-    tk.out = const_cast<double *>(P.g64) + (size_t)i * P.bs;
+    tk.out = P.g64 + (size_t)i * P.bs;
     tk.cn = P.gcn + 8 * (size_t)i;
     tk.steps = P.n - an;
     tk.path = 0;

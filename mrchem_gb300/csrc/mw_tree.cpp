@@ -620,6 +620,66 @@ bool host_is_pinned(const void *p) {
     return a.type == cudaMemoryTypeHost;
 }
 
+std::vector<std::vector<int>> upload_structures(const std::vector<Tree *> &trees, const int *nnodes,
+                                                const int *const *keys) {
+    const int n = (int)trees.size();
+    std::vector<std::vector<int>> from(n);
+    if (n == 0) return from;
+    // sized first, so that building the structures is host work only and runs in parallel
+    for (int i = 0; i < n; i++) trees[i]->reserve((size_t)nnodes[i]);
+    trees[0]->ctx->sync();
+    std::vector<std::string> err(n);
+    std::vector<int> code(n, MW_OK);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < n; i++) {
+        try {
+            from[i] = upload_structure(*trees[i], nnodes[i], keys[i]);
+        } catch (const Error &e) {
+            code[i] = e.code;
+            err[i] = e.what();
+        }
+    }
+    for (int i = 0; i < n; i++)
+        if (code[i] != MW_OK) throw Error(code[i], err[i]);
+    return from;
+}
+
+double *upload_enqueue(const std::vector<Tree *> &trees, const std::vector<const int *> &maps,
+                       const std::vector<const double *> &coefs, Arena &arena) {
+    Ctx &ctx = *trees[0]->ctx;
+    const int bs = ctx.basis.bs, n = (int)trees.size();
+    std::vector<size_t> first(n + 1, 0);
+    for (int i = 0; i < n; i++) first[i + 1] = first[i] + (size_t)trees[i]->nn();
+    double *scratch = (double *)arena.alloc(sizeof(double) * (size_t)bs * first[n]);
+    for (int i = 0; i < n; i++)
+        MWG_CUDA(cudaMemcpyAsync(scratch + first[i] * bs, coefs[i], sizeof(double) * (size_t)bs * trees[i]->nn(),
+                                 cudaMemcpyHostToDevice, ctx.stream));
+    std::vector<int> m;
+    std::vector<double *> bl, cnp;
+    m.reserve(first[n]);
+    for (int i = 0; i < n; i++) {
+        m.insert(m.end(), maps[i], maps[i] + trees[i]->nn());
+        for (int j = 0; j < trees[i]->nn(); j++) {
+            bl.push_back(trees[i]->block(j));
+            cnp.push_back(trees[i]->d_cn + (size_t)8 * j);
+        }
+    }
+    Packer pk;
+    pk.add(m.data(), m.size() * sizeof(int));
+    pk.add(bl.data(), bl.size() * sizeof(double *));
+    pk.add(cnp.data(), cnp.size() * sizeof(double *));
+    pk.ship(ctx, arena);
+    const int *dmap = (const int *)pk.ptr(0);
+    for (int i = 0; i < n; i++)
+        k_permute_blocks(trees[i]->d_coefs, scratch + first[i] * bs, dmap + first[i], trees[i]->nn(), bs, ctx.stream);
+    k_norms(ctx.dbasis, (double *const *)pk.ptr(1), (double *const *)pk.ptr(2), (int)bl.size(), ctx.stream);
+    double *h = (double *)arena.halloc(sizeof(double) * 8 * first[n]);
+    for (int i = 0; i < n; i++)
+        MWG_CUDA(cudaMemcpyAsync(h + 8 * first[i], trees[i]->d_cn, sizeof(double) * 8 * trees[i]->nn(),
+                                 cudaMemcpyDeviceToHost, ctx.stream));
+    return h;
+}
+
 void tree_upload_batch(const std::vector<Tree *> &trees, const int *nnodes, const int *const *keys,
                        const double *const *coefs, Arena &arena) {
     if (trees.empty()) return;

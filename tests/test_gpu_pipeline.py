@@ -157,3 +157,50 @@ def test_batched_upload_download_match_single(engine):
         engine.unpin_host(mra, c)
     for o in outs:
         engine.unpin_host(mra, o[1])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_apply_batch_host_matches_upload_then_apply(engine, precision):
+    # mw_apply_batch_host (inputs uploaded per job group, overlapped with the first groups'
+    # levels) against mw_tree_upload_batch + mw_apply_batch: the same input trees, bit-identical
+    # outputs, with pinned and with pageable input buffers
+    prec = 1e-6
+    rng = np.random.default_rng(20261203)
+    mra = engine.MultiResolutionAnalysis(9)
+    mons = [(a, b, c) for a in range(4) for b in range(4) for c in range(4) if a + b + c <= 3]
+    srcs, mus = [], []
+    for _ in range(6):
+        alpha = float(np.exp(rng.uniform(np.log(0.3), np.log(20.0))))
+        R = tuple(rng.uniform(-2.0, 2.0, 3))
+        terms = [(float(c), alpha, R, m) for c, m in zip(rng.standard_normal(len(mons)), mons)]
+        f = engine.project(prec, engine.FunctionTree(mra), terms, abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        srcs.append(f)
+        mus.append(math.sqrt(-2.0 * rng.uniform(-2.0, -0.1)))
+    ops = [engine.HelmholtzOperator(mra, mu, prec) for mu in mus]
+    host = [s.download() for s in srcs]
+
+    inps_a = engine.upload_batch([engine.FunctionTree(mra) for _ in srcs], host)
+    outs_a = [engine.FunctionTree(mra) for _ in srcs]
+    engine.apply_batch([prec] * len(srcs), outs_a, ops, inps_a, abs_prec=True, precision=precision)
+    ref = engine.download_batch(outs_a)
+    ref_in = engine.download_batch(inps_a)
+    for pinned in (True, False):
+        buffers = [(k, c.copy(), l) for k, c, l in host]
+        if pinned:
+            for _, c, _ in buffers:
+                engine.pin_host(mra, c)
+        inps_b = [engine.FunctionTree(mra) for _ in srcs]
+        outs_b = [engine.FunctionTree(mra) for _ in srcs]
+        st = engine.apply_batch_host([prec] * len(srcs), outs_b, ops, inps_b, buffers, abs_prec=True,
+                                     precision=precision)
+        assert st["items"] > 0
+        for (k1, c1, l1), (k2, c2, l2) in zip(engine.download_batch(outs_b), ref):
+            assert np.array_equal(k1, k2) and np.array_equal(c1, c2) and np.array_equal(l1, l2)
+        for (k1, c1, _), (k2, c2, _) in zip(engine.download_batch(inps_b), ref_in):
+            assert np.array_equal(k1, k2) and np.array_equal(c1, c2)
+        # the input trees' host norms are those of an upload
+        assert [t.norm() for t in inps_b] == [t.norm() for t in inps_a]
+        if pinned:
+            for _, c, _ in buffers:
+                engine.unpin_host(mra, c)
