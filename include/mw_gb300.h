@@ -202,17 +202,22 @@ int mw_apply(double prec, mw_tree out, mw_op op, mw_tree inp, int nprec, const m
 int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *nprec,
                    const mw_tree *prec_trees, int max_iter, int abs_prec, int precision_mode);
 /* apply on a fixed output grid (the output's current grid, no refinement) */
-/* mw_tree_upload_batch of the inputs followed by mw_apply_batch (no precision trees), with the
- * upload overlapped: each job group's input blocks go up on the group's stream, and a group starts
- * computing as soon as its own inputs have landed, while the copy engine still moves the later
- * groups' blocks.  in_keys / in_coefs as in mw_tree_upload_batch.  The overlap needs distinct input
- * trees that are not outputs, and coefficient buffers pinned with mw_pin_host; otherwise the inputs
- * go up first.  Results are bit-identical to the two calls.  The reference has no counterpart
+/* mw_tree_upload_batch of the inputs, mw_apply_batch (no precision trees) and, optionally,
+ * mw_tree_download_batch of the outputs, with the transfers overlapped: each job group's input
+ * blocks go up on the group's stream and the group starts computing once they have landed; each
+ * group's outputs go down as soon as its post-processing is queued, beside the other groups' work.
+ * in_keys / in_coefs as in mw_tree_upload_batch.  Outputs (out_cap may be NULL for none): per job,
+ * buffers for out_cap[i] nodes as mw_tree_download_batch fills them; out_nnodes[i] is the output's
+ * node count when they were filled, minus it when the output did not fit or out_coefs[i] is not
+ * pinned (then download it with mw_tree_download_batch).  The overlap needs distinct input trees
+ * that are not outputs, and input buffers pinned with mw_pin_host; otherwise the inputs go up
+ * first.  Results are bit-identical to the separate calls.  The reference has no counterpart
  * (HelmholtzVector::operator(), src/scf_solver/HelmholtzVector.cpp:70-91, applies orbitals that
  * already live in memory). */
 int mw_apply_batch_host(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *in_nnodes,
                         const int *const *in_keys, const double *const *in_coefs, int max_iter, int abs_prec,
-                        int precision_mode);
+                        int precision_mode, const int *out_cap, int *const *out_keys, double *const *out_coefs,
+                        unsigned char *const *out_leaf, int *out_nnodes);
 /* Autotuner of the batched apply's launch settings (no counterpart in the reference): runs the
  * batch (as mw_apply_batch with no precision trees and max_iter = -1) `repeats` times for each
  * candidate -- job groups 2..6, then the chunk size of the TF32, FP32 and double-FP32 tiers, one

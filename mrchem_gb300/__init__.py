@@ -139,7 +139,7 @@ def load_library(path=None):
         "mw_apply_fixed": [D, P, P, P, I, I],
         "mw_apply_adjoint": [D, P, P, P, P, I],
         "mw_multiply_adjoint": [D, P, D, P, P, P],
-        "mw_apply_batch_host": [I, P, P, P, P, P, P, P, I, I, I],
+        "mw_apply_batch_host": [I, P, P, P, P, P, P, P, I, I, I, P, P, P, P, P],
         "mw_multiply": [D, P, D, P, P, I, I, I],
         "mw_square": [D, P, P, I, I],
         "mw_add": [D, P, I, dp, pp, I],
@@ -529,10 +529,13 @@ def autotune_batch(precs, outs, opers, inps, abs_prec=False, precision="mixed", 
             "ms": float(ms[0])}
 
 
-def apply_batch_host(precs, outs, opers, inps, inputs, max_iter=-1, abs_prec=False, precision="fp64"):
-    """upload_batch(inps, inputs) then apply_batch(...) as one call (mw_apply_batch_host): each job
-    group's inputs go up on its own stream and the group starts once they have landed.  inputs:
-    (keys, coefs, ...) per job, coefs pinned with pin_host for the overlap."""
+def apply_batch_host(precs, outs, opers, inps, inputs, max_iter=-1, abs_prec=False, precision="fp64", outputs=None):
+    """upload_batch(inps, inputs), apply_batch(...) and, with `outputs`, download_batch(outs) as one
+    call (mw_apply_batch_host): each job group's inputs go up on its own stream and the group
+    starts once they have landed; its outputs go down as soon as its post-processing is queued.
+    inputs: (keys, coefs, ...) per job, coefs pinned with pin_host for the overlap.  outputs: per
+    job (keys, coefs, leaf) arrays as download_batch returns them (coefs pinned), filled in place
+    where the output fits; the returned stats hold "outputs_filled" (one bool per job)."""
     n = len(outs)
     p = np.ascontiguousarray(precs if np.ndim(precs) else [precs] * n, dtype=np.float64)
     ks = [np.ascontiguousarray(x[0], dtype=np.int32) for x in inputs]
@@ -540,9 +543,27 @@ def apply_batch_host(precs, outs, opers, inps, inputs, max_iter=-1, abs_prec=Fal
     nn = np.ascontiguousarray([k.shape[0] for k in ks], dtype=np.int32)
     kp = (C.c_void_p * n)(*[k.ctypes.data for k in ks])
     cp = (C.c_void_p * n)(*[c.ctypes.data for c in cs])
+    ocap = okp = ocp = olp = onn = None
+    if outputs is not None:
+        bs = 8 * outs[0].mra.K ** 3
+        for k, c, l in outputs:
+            if not (k.dtype == np.int32 and c.dtype == np.float64 and l.dtype == np.uint8 and k.flags.c_contiguous
+                    and c.flags.c_contiguous and l.flags.c_contiguous and k.ndim == 2 and k.shape[1] == 4
+                    and c.ndim == 2 and c.shape[1] == bs and l.ndim == 1):
+                raise ValueError("outputs: (n, 4) int32 keys, (n, 8K^3) float64 coefs and (n,) uint8 leaf "
+                                 "arrays, C-contiguous")
+        ocap = np.ascontiguousarray([min(k.shape[0], c.shape[0], l.shape[0]) for k, c, l in outputs], dtype=np.int32)
+        okp = (C.c_void_p * n)(*[o[0].ctypes.data for o in outputs])
+        ocp = (C.c_void_p * n)(*[o[1].ctypes.data for o in outputs])
+        olp = (C.c_void_p * n)(*[o[2].ctypes.data for o in outputs])
+        onn = np.zeros(n, dtype=np.int32)
     _check(_lib.mw_apply_batch_host(n, _dp(p), _ptrs(outs), _ptrs(opers), _ptrs(inps), _ip(nn), kp, cp, max_iter,
-                                    int(abs_prec), _PREC[precision]), outs[0].mra.ptr)
-    return outs[0].mra.last_stats()
+                                    int(abs_prec), _PREC[precision], _ip(ocap) if ocap is not None else None, okp,
+                                    ocp, olp, _ip(onn) if onn is not None else None), outs[0].mra.ptr)
+    st = outs[0].mra.last_stats()
+    if onn is not None:
+        st["outputs_filled"] = [bool(v > 0) for v in onn]
+    return st
 
 
 def multiply_batch(precs, outs, coefs, as_, bs_, max_iter=-1, abs_prec=False, use_max_norms=False):

@@ -1497,6 +1497,24 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     MWG_CUDA(cudaEventRecord(ev_post[2 * g], ctx.stream));
                     post_process(jset, *G.arena);
                     MWG_CUDA(cudaEventRecord(ev_post[2 * g + 1], ctx.stream));
+                    if (hin && hin->out_nnodes) {
+                        // the group's outputs that fit go down now, beside the other groups' levels
+                        std::vector<Tree *> trees;
+                        std::vector<int *> k;
+                        std::vector<double *> c;
+                        std::vector<unsigned char *> l;
+                        for (int j : G.jobs) {
+                            Tree &out = *jobs[j].out;
+                            const bool fits = out.nn() <= hin->out_cap[j] && hin->out_coefs[j];
+                            hin->out_nnodes[j] = fits ? out.nn() : -out.nn();
+                            if (!fits) continue;
+                            trees.push_back(&out);
+                            k.push_back(hin->out_keys[j]);
+                            c.push_back(hin->out_coefs[j]);
+                            l.push_back(hin->out_leaf[j]);
+                        }
+                        download_enqueue(trees, k.data(), c.data(), l.data(), *G.arena);
+                    }
                 }
             }
             if (!G.done) {

@@ -540,7 +540,9 @@ int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tre
 
 int mw_apply_batch_host(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tree *inps, const int *in_nnodes,
                         const int *const *in_keys, const double *const *in_coefs, int max_iter, int abs_prec,
-                        int precision_mode) {
+                        int precision_mode, const int *out_cap, int *const *out_keys, double *const *out_coefs,
+                        unsigned char *const *out_leaf, int *out_nnodes) {
+    if (out_cap && (!out_keys || !out_coefs || !out_leaf || !out_nnodes)) return MW_ERR_ARG;
     if (n < 1 || !precs || !outs || !ops || !inps || !in_nnodes || !in_keys || !in_coefs) return MW_ERR_ARG;
     if (precision_mode < MW_PREC_FP64 || precision_mode > MW_PREC_DF) return MW_ERR_ARG;
     for (int i = 0; i < n; i++)
@@ -566,17 +568,47 @@ int mw_apply_batch_host(int n, const double *precs, mw_tree *outs, mw_op *ops, m
             overlap &= !std::binary_search(sorted.begin(), sorted.end(), &outs[i]->tree);
             overlap &= mwg::host_is_pinned(in_coefs[i]);
         }
+        // outputs are written where they fit and their coefficient buffer is pinned
+        std::vector<double *> oc(n, nullptr);
+        if (out_cap)
+            for (int i = 0; i < n; i++)
+                if (out_coefs[i] && mwg::host_is_pinned(out_coefs[i])) oc[i] = out_coefs[i];
         mw_stats st{};
         if (overlap) {
             mwg::HostInputs hin;
             hin.nnodes.assign(in_nnodes, in_nnodes + n);
             hin.keys.assign(in_keys, in_keys + n);
             hin.coefs.assign(in_coefs, in_coefs + n);
+            if (out_cap) {
+                hin.out_keys.assign(out_keys, out_keys + n);
+                hin.out_coefs = oc;
+                hin.out_leaf.assign(out_leaf, out_leaf + n);
+                hin.out_cap.assign(out_cap, out_cap + n);
+                hin.out_nnodes = out_nnodes;
+            }
             mwg::apply_batch(jobs, precision_mode, false, st, &hin);
         } else {
             mwg::tree_upload_batch(itrees, in_nnodes, in_keys, in_coefs, ctx->arena);
             mwg::apply_batch(jobs, precision_mode, false, st);
+            if (out_cap) {
+                std::vector<mwg::Tree *> ts;
+                std::vector<int *> k;
+                std::vector<double *> c;
+                std::vector<unsigned char *> l;
+                for (int i = 0; i < n; i++) {
+                    const int m = outs[i]->tree.nn();
+                    const bool fits = m <= out_cap[i] && oc[i];
+                    out_nnodes[i] = fits ? m : -m;
+                    if (!fits) continue;
+                    ts.push_back(&outs[i]->tree);
+                    k.push_back(out_keys[i]);
+                    c.push_back(oc[i]);
+                    l.push_back(out_leaf[i]);
+                }
+                if (!ts.empty()) mwg::tree_download_batch(ts, k.data(), c.data(), l.data());
+            }
         }
+        ctx->sync();
         ctx->last = st;
     });
 }

@@ -75,6 +75,14 @@ struct HostInputs {
     std::vector<int> nnodes;
     std::vector<const int *> keys;
     std::vector<const double *> coefs;
+    // optional host outputs, per job: buffers for out_cap nodes (coefficients pinned).  When a job
+    // group's post-processing is queued, each of its outputs that fits goes down in canonical
+    // order on the group's stream; out_nnodes gets the node count, negative when it did not fit.
+    std::vector<int *> out_keys;
+    std::vector<double *> out_coefs;
+    std::vector<unsigned char *> out_leaf;
+    std::vector<int> out_cap;
+    int *out_nnodes = nullptr;
 };
 void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_grid, mw_stats &st,
                  const HostInputs *hin = nullptr);
@@ -87,6 +95,10 @@ std::vector<std::vector<int>> upload_structures(const std::vector<Tree *> &trees
 // tree after tree); read it after the stream has passed this point
 double *upload_enqueue(const std::vector<Tree *> &trees, const std::vector<const int *> &maps,
                        const std::vector<const double *> &coefs, Arena &arena);
+// on the context's current stream: the trees' blocks in canonical order into the caller's pinned
+// buffers; keys and leaf flags (host data, either may be null) are written before it returns
+void download_enqueue(const std::vector<Tree *> &trees, int *const *keys, double *const *coefs,
+                      unsigned char *const *leaf, Arena &arena);
 void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st);
 void apply_adjoint(double prec, Tree &res, Oper &op, Tree &x, Tree &y, mw_stats &st);
 void multiply_adjoint(double prec, Tree &out, double coef, const Tree &a, Tree &b, Tree &seed, mw_stats &st);

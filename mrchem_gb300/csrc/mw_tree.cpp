@@ -680,6 +680,43 @@ double *upload_enqueue(const std::vector<Tree *> &trees, const std::vector<const
     return h;
 }
 
+void download_enqueue(const std::vector<Tree *> &trees, int *const *keys, double *const *coefs,
+                      unsigned char *const *leaf, Arena &arena) {
+    const int n = (int)trees.size();
+    if (n == 0) return;
+    Ctx &ctx = *trees[0]->ctx;
+    const int bs = ctx.basis.bs;
+    std::vector<std::vector<int>> idx(n);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < n; i++) idx[i] = canonical_order(*trees[i]);
+    std::vector<size_t> first(n + 1, 0);
+    for (int i = 0; i < n; i++) first[i + 1] = first[i] + (size_t)trees[i]->nn();
+    double *scratch = (double *)arena.alloc(sizeof(double) * (size_t)bs * first[n]);
+    std::vector<int> maps;
+    maps.reserve(first[n]);
+    for (int i = 0; i < n; i++) maps.insert(maps.end(), idx[i].begin(), idx[i].end());
+    Packer pk;
+    pk.add(maps.data(), maps.size() * sizeof(int));
+    pk.ship(ctx, arena);
+    const int *dmap = (const int *)pk.ptr(0);
+    for (int i = 0; i < n; i++) {
+        k_permute_blocks(scratch + first[i] * bs, trees[i]->d_coefs, dmap + first[i], trees[i]->nn(), bs, ctx.stream);
+        MWG_CUDA(cudaMemcpyAsync(coefs[i], scratch + first[i] * bs, sizeof(double) * (size_t)bs * trees[i]->nn(),
+                                 cudaMemcpyDeviceToHost, ctx.stream));
+    }
+    // keys and leaf flags are host data: written now
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < trees[i]->nn(); j++) {
+            const NodeInfo &nd = trees[i]->nodes[idx[i][j]];
+            if (keys[i]) {
+                keys[i][4 * j] = nd.n;
+                for (int d = 0; d < 3; d++) keys[i][4 * j + 1 + d] = nd.l[d];
+            }
+            if (leaf[i]) leaf[i][j] = nd.child0 < 0;
+        }
+}
+
 void tree_upload_batch(const std::vector<Tree *> &trees, const int *nnodes, const int *const *keys,
                        const double *const *coefs, Arena &arena) {
     if (trees.empty()) return;

@@ -204,3 +204,48 @@ def test_apply_batch_host_matches_upload_then_apply(engine, precision):
         if pinned:
             for _, c, _ in buffers:
                 engine.unpin_host(mra, c)
+
+
+def test_apply_batch_host_outputs(engine):
+    # the outputs of mw_apply_batch_host go down per job group into the caller's pinned buffers:
+    # equal to a download_batch afterwards; an output whose buffer is too small is left for
+    # download_batch (its count comes back negative)
+    prec = 1e-6
+    rng = np.random.default_rng(20261204)
+    mra = engine.MultiResolutionAnalysis(9)
+    srcs, ops = [], []
+    for _ in range(5):
+        R = tuple(rng.uniform(-2.0, 2.0, 3))
+        alpha = float(np.exp(rng.uniform(np.log(0.5), np.log(10.0))))
+        f = engine.project(prec, engine.FunctionTree(mra), [(1.0, alpha, R, (1, 0, 0)), (0.5, 2 * alpha, R, (0, 0, 0))],
+                           abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        srcs.append(f)
+        ops.append(engine.HelmholtzOperator(mra, float(rng.uniform(0.5, 2.0)), prec))
+    host = [s.download() for s in srcs]
+    for _, c, _ in host:
+        engine.pin_host(mra, c)
+    inps = [engine.FunctionTree(mra) for _ in srcs]
+    outs = [engine.FunctionTree(mra) for _ in srcs]
+    engine.apply_batch_host([prec] * 5, outs, ops, inps, host, abs_prec=True, precision="mixed")
+    ref = engine.download_batch(outs)
+    bufs = []
+    for i, (k, c, l) in enumerate(ref):
+        m = k.shape[0] - (1 if i == 2 else 0)  # job 2's buffer is one node short
+        b = (np.zeros((m, 4), np.int32), np.zeros((m, c.shape[1])), np.zeros(m, np.uint8))
+        engine.pin_host(mra, b[1])
+        bufs.append(b)
+    outs2 = [engine.FunctionTree(mra) for _ in srcs]
+    st = engine.apply_batch_host([prec] * 5, outs2, ops, [engine.FunctionTree(mra) for _ in srcs], host,
+                                 abs_prec=True, precision="mixed", outputs=bufs)
+    assert st["outputs_filled"] == [True, True, False, True, True]
+    for i, ((k1, c1, l1), (k2, c2, l2)) in enumerate(zip(bufs, ref)):
+        if i == 2:
+            continue
+        assert np.array_equal(k1, k2) and np.array_equal(c1, c2) and np.array_equal(l1, l2)
+    k3, c3, l3 = engine.download_batch([outs2[2]])[0]
+    assert np.array_equal(k3, ref[2][0]) and np.array_equal(c3, ref[2][1])
+    for b in bufs:
+        engine.unpin_host(mra, b[1])
+    for _, c, _ in host:
+        engine.unpin_host(mra, c)
