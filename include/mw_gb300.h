@@ -231,7 +231,7 @@ int mw_apply_fixed(double prec, mw_tree out, mw_op op, mw_tree inp, int abs_prec
 /* L2-adjoint of the fixed-grid FP64 apply y = A x (output grid = seed's grid, absolute precision):
  * out <- A^T seed on x's grid, with the forward's item set (screened with x's norms).  Transposed
  * operator blocks, contraction grouped by input node (gather), then the forward's post-processing.
- * No MRCPP counterpart: it serves the gradient of J = 1/2 <rho, P rho> (pattern 3 of the plan). */
+ * No MRCPP counterpart: it serves the gradient of the Coulomb energy J = 1/2 <rho, P rho>. */
 int mw_apply_adjoint(double prec, mw_tree out, mw_op op, mw_tree x, mw_tree seed, int abs_prec);
 
 /* mrcpp::multiply(prec, out, coef, a, b, maxIter, absPrec, useMaxNorms)

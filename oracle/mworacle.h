@@ -6,8 +6,8 @@
  * reaches through MRCPP (commit 0e5b32003eed8e1abb22a44ba4e1a2ce9fd9ddb1,
  * fetched by external/upstream/fetch_mrcpp.cmake:39-42; MRCPP itself is not
  * vendored in the reference tree).  It is used by the tests, by the smoke
- * check and by bench.py's CPU-baseline leg as the checker; the product
- * (mrchem_gb300) never links or calls it.
+ * check and by bench.py's CPU-baseline leg, as the CPU result the GPU path is
+ * compared with; the product (mrchem_gb300) never links or calls it.
  *
  * Published methods restated here:
  *   - Alpert multiwavelets (SIAM J. Math. Anal. 24 (1993) 246) with the

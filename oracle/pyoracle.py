@@ -1,8 +1,8 @@
 """ctypes wrapper of the CPU oracle (oracle/_build/libmworacle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by
-bench.py's CPU-baseline leg as the checker.  The product package never
-imports this module.
+bench.py's CPU-baseline leg, as the CPU result the GPU path is compared
+with.  The product package never imports this module.
 """
 import ctypes as C
 import os
