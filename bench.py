@@ -401,8 +401,10 @@ def run(args):
                               "wait_level": st["host_wait_ms"], "kernel_fp64": st_ser["kernel_ms_fp64"],
                               "kernel_fp32": st_ser["kernel_ms_fp32"], "kernel_tf32": st_ser["kernel_ms_tf32"],
                               "kernel_df32": st_ser["kernel_ms_df"],
-                              "note": "host phases from the timed (overlapped) steps; exclusive kernel times "
-                                      "from one step without overlap"},
+                              "note": "host phases from the timed (overlapped) steps, with the screening on the "
+                                      "GPU: enumerate = waiting for the walk's candidate counts, generate = "
+                                      "queueing the generation, items = the tiers' node lists from the GPU's "
+                                      "counts; exclusive kernel times from one step without overlap"},
         "no_overlap": {"value": st_ser["out_nodes"] * world / (serial_ms / 1e3), "unit": "nodes/s",
                        "ms_per_step": serial_ms, "policy": "job groups not pipelined (mw_ctx_set_overlap 0)"},
         "host_screening": {"value": st_hs["out_nodes"] * world / (host_scr_ms / 1e3), "unit": "nodes/s",
