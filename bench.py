@@ -415,6 +415,15 @@ def run(args):
                 "ms_per_step": e2e_ms, **{k: v / args.e2e_steps for k, v in e2e_parts.items()}},
         "roofline": dict(roofs[dominant], tier=dominant),
         "roofline_tiers": roofs,
+        # the whole step against HBM: algorithmic bytes (FP64 blocks of every input and output
+        # node, operator blocks used) over the step time; the step is compute-bound, so this
+        # fraction is small by construction
+        "hbm": {"achieved_gbs": st["bytes"] / (ms / 1e3) / 1e9,
+                "peak_gbs": measured_peaks().get("hbm_gbs"),
+                "frac": (st["bytes"] / (ms / 1e3) / 1e9 / measured_peaks()["hbm_gbs"])
+                if measured_peaks().get("hbm_gbs") else None,
+                "bytes_per_step": st["bytes"],
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"},
         "clocks": clk.summary(),
     }
     line["speedup_mixed_vs_fp64"] = (nodes / (ms / 1e3)) / (st64["out_nodes"] / fp64_s)
