@@ -174,7 +174,9 @@ int mw_dot(mw_tree a, mw_tree b, double *out);
  * node-pair lists and partial sums live in a fixed 1 MiB device array that every GPU loading this
  * library holds until exit, so at most 32768 nodes common to both trees (MW_ERR_ARG beyond that).
  * All calls share that array: calls that overlap on the GPU or across host threads race.  The
- * first call on each device looks up the array's address; make it before any stream capture. */
+ * array is reserved, and its address looked up, by mw_ctx_create on the context's device, not by
+ * this call.  The call blocks until the result is on the host (it synchronises the context's
+ * stream), so it must not be called while that stream is being captured. */
 int mw_dot_noalloc(mw_tree a, mw_tree b, double *out);
 
 /* ---- operators (src/driver.cpp:1131,1283; src/scf_solver/HelmholtzVector.cpp:144) ---- */

@@ -26,6 +26,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libmwgb300.so")
 
 MW_OK = 0
+MW_ERR_ARG, MW_ERR_OOM, MW_ERR_CUDA, MW_ERR_TIMEOUT, MW_ERR_STATE = 1, 2, 3, 4, 5
 PREC_FP64 = 0
 PREC_MIXED = 1
 PREC_MIXED_NEARFP64 = 2
@@ -679,8 +680,9 @@ def dot(a, b):
 def dot_noalloc(a, b):
     """<a|b> without allocating anything, for callers that cannot allocate GPU memory at that point.
 
-    Uses a fixed 1 MiB device array held for the life of the process: at most 32768 nodes common
-    to both trees; calls that overlap race on that array.
+    Uses a fixed 1 MiB device array, reserved when the context was created and held for the life
+    of the process: at most 32768 nodes common to both trees; calls that overlap race on that
+    array.  Blocks until the result is on the host, so not callable during stream capture.
     """
     v = C.c_double()
     _check(_lib.mw_dot_noalloc(a.ptr, b.ptr, C.byref(v)), a.mra.ptr)

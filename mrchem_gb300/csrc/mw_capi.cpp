@@ -98,6 +98,9 @@ int mw_ctx_create(int device, int root_scale, const int corner[3], const int box
         c->ctx.dbasis = mwg::DevBasis{K, basis, d, d + K2 * K2, d + 2 * K2 * K2, d + 2 * K2 * K2 + K * K,
                                       d + 2 * K2 * K2 + 2 * K * K, d + 2 * K2 * K2 + 2 * K * K + K,
                                       d + 2 * K2 * K2 + 2 * K * K + 2 * K};
+        // mw_dot_noalloc's fixed device array: its address is taken here, with the device current,
+        // so that its module is loaded (and the array reserved) while the caller may still allocate
+        mwg::noalloc_setup(device);
     });
     if (rc != MW_OK) {
         if (c->ctx.stream) cudaStreamDestroy(c->ctx.stream);

@@ -106,6 +106,8 @@ void density(double prec, Tree &rho, const std::vector<Tree *> &orbs, const std:
              mw_stats &st);
 void rotate(const std::vector<Tree *> &outs, const std::vector<const Tree *> &ins, const double *U, mw_stats &st);
 double dot_noalloc(const Tree &a, const Tree &b);
+// looks up the no-allocation scratch array's address on `device` (current), loading its module
+void noalloc_setup(int device);
 void tree_save(Tree &t, const char *path);
 void tree_load(Tree &t, const char *path);
 void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st);

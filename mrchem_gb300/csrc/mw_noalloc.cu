@@ -16,12 +16,17 @@
 // array, and host staging is file-scope too: calls that overlap, on the GPU or
 // from several host threads, race and must be serialised by the caller.
 // Nothing needs clearing between calls, since each call writes every entry it
-// later reads.  On each device, the first call looks up the array's device
-// address (cudaGetSymbolAddress) with that device current; that first call
-// should come before any stream capture.
+// later reads.  The array's device address is looked up (cudaGetSymbolAddress)
+// when a context is created on a device, with that device current: with lazy
+// module loading that lookup is what loads this file's module and reserves the
+// 1 MiB, so it happens at mw_ctx_create, where the caller may still allocate,
+// and never inside mw_dot_noalloc itself.  Each call copies its pair lists from
+// host arrays and waits for its result on the host (a stream synchronisation),
+// so it must not be called while the context's stream is being captured.
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <string>
 
 #include "mw_internal.h"
 
@@ -62,6 +67,8 @@ char *scratch_on(int device) {
 
 }  // namespace
 
+void noalloc_setup(int device) { scratch_on(device); }
+
 double dot_noalloc(const Tree &a, const Tree &b) {
     Ctx &ctx = *a.ctx;
     const int K3 = ctx.basis.K * ctx.basis.K * ctx.basis.K;
@@ -71,8 +78,8 @@ double dot_noalloc(const Tree &a, const Tree &b) {
         int j = b.find(nd.n, nd.l);
         if (j < 0) continue;
         if (n == NOALLOC_MAX_PAIRS)
-            throw Error(MW_ERR_ARG, "mw_dot_noalloc: the trees share more than 32768 nodes, the most its fixed "
-                                    "scratch holds; use mw_dot");
+            throw Error(MW_ERR_ARG, "mw_dot_noalloc: the trees share more than " + std::to_string(NOALLOC_MAX_PAIRS) +
+                                        " nodes, the most its fixed scratch holds; use mw_dot");
         h_pa[n] = a.block(i);
         h_pb[n] = b.block(j);
         h_start[n] = nd.n == ctx.basis.n0 ? 0 : K3;
