@@ -30,6 +30,9 @@ import numpy as np  # noqa: E402
 
 SEED = 20261203
 ORDER, PREC = 9, 1e-6
+# DRAM bytes (read + write) per item of each tier kernel on the benchmark step (k=9), from the ncu
+# launch capture summarised in profiles/dram_traffic_tiers_k10.md; re-captured when a tier changes
+DRAM_PER_ITEM = {"fp32": 2.79e3, "tf32": 1.36e3, "df32": 10.1e3}
 NORB = 16
 METRIC = "Helmholtz-apply nodes/s: batched mixed vs plain FP64 GPU at 1e-6 rel. error"
 
@@ -107,31 +110,50 @@ def measured_peaks():
         return {}
 
 
-def cpu_sample(terms, mus, max_iter, budget_s):
-    """Oracle (OpenMP FP64) Helmholtz applies of the batch's orbitals 0, 1, ... in turn, until
-    budget_s seconds of apply time have passed or the batch is done (max_iter = -1: the complete
-    adaptive apply of each).  Projection and operator setup are outside the timed part."""
+# The CPU sample both arms time: the complete adaptive apply of these orbitals of the batch.
+# `--impl reference` runs it once per step; the GPU arm's cpu_baseline runs it until --cpu-s
+# seconds have passed, and compares the GPU outputs of these orbitals with the oracle's.
+CPU_SAMPLE = (0, 1, 2)
+
+
+def workload_config():
+    """The `config` both arms print (identical, so the two lines describe the same workload)."""
+    return {"workload": "helmholtz-batch16-k9-prec1e-6", "orbitals": NORB, "order": ORDER, "prec": PREC,
+            "basis": "interpolating", "box": "[-32,32]^3", "abs_prec": True,
+            "cpu_sample": "orbitals %d..%d of the batch, complete adaptive apply each, oracle FP64 OpenMP"
+                          % (CPU_SAMPLE[0], CPU_SAMPLE[-1])}
+
+
+def cpu_sample(terms, mus, budget_s, keep=False):
+    """Oracle (OpenMP FP64) Helmholtz applies of the CPU_SAMPLE orbitals, the whole sample
+    repeated until budget_s seconds of apply time have passed (at least once).  Projection and
+    operator setup are outside the timed part.  keep: also return the oracle output trees of
+    the first pass (orbital index -> (keys, coefs, is_leaf))."""
     from oracle import pyoracle as po
     po.build()
     threads = os.cpu_count() or 1
     po.set_threads(threads)
     mra = po.MRA(ORDER)
-    nodes, dt, done = 0, 0.0, 0
-    for i in range(len(terms)):
+    jobs = []
+    for i in CPU_SAMPLE:
         phi = po.project_gauss(PREC, po.Tree(mra), terms[i], abs_prec=True)
         phi.rescale(1.0 / phi.norm())
-        op = po.helmholtz(mra, float(mus[i]), PREC)
-        out = po.Tree(mra)
-        t0 = time.perf_counter()
-        st = po.apply(PREC, out, op, phi, max_iter=max_iter, abs_prec=True)
-        dt += time.perf_counter() - t0
-        nodes += st["out_nodes"]
-        done += 1
-        if dt >= budget_s:
-            break
-    return {"value": nodes / dt, "unit": "nodes/s", "cores": threads, "kind": "port",
-            "sample": "orbitals 0..%d of the batch, %s adaptive apply each (%d output nodes, %.1f s)"
-                      % (done - 1, "complete" if max_iter < 0 else "levels 0..%d of the" % max_iter, nodes, dt)}
+        jobs.append((i, phi, po.helmholtz(mra, float(mus[i]), PREC)))
+    nodes, dt, reps, kept = 0, 0.0, 0, {}
+    while reps == 0 or dt < budget_s:
+        for i, phi, op in jobs:
+            out = po.Tree(mra)
+            t0 = time.perf_counter()
+            st = po.apply(PREC, out, op, phi, max_iter=-1, abs_prec=True)
+            dt += time.perf_counter() - t0
+            nodes += st["out_nodes"]
+            if keep and reps == 0:
+                kept[i] = out.export()
+        reps += 1
+    res = {"value": nodes / dt, "unit": "nodes/s", "cores": threads, "kind": "port",
+           "sample": "orbitals %d..%d of the batch, complete adaptive apply each, %d pass(es): %d output nodes "
+                     "in %.1f s" % (CPU_SAMPLE[0], CPU_SAMPLE[-1], reps, nodes, dt)}
+    return (res, kept) if keep else res
 
 
 def run_reference(args):
@@ -142,19 +164,17 @@ def run_reference(args):
     terms, mus = orbital_terms(rng)
     vals = []
     for _ in range(args.warmup):
-        cpu_sample(terms, mus, args.cpu_levels, args.ref_step_s)
+        cpu_sample(terms, mus, 0.0)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        s = cpu_sample(terms, mus, args.cpu_levels, args.ref_step_s)
+        s = cpu_sample(terms, mus, 0.0)  # one pass of the sample per step
         vals.append(s["value"])
     wall = time.perf_counter() - t0
     v = float(np.mean(vals))
     print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": "nodes/s", "n_gpus": args.gpus,
                       "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * wall / max(args.steps, 1),
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                      "data": "synthetic",
-                      "config": {"workload": "helmholtz-batch16-k9-prec1e-6", "orbitals": NORB, "order": ORDER,
-                                 "prec": PREC, "sample": s["sample"]},
+                      "data": "synthetic", "config": workload_config(),
                       "cpu_baseline": {"value": v, "unit": "nodes/s", "cores": s["cores"], "kind": "port",
                                        "sample": s["sample"]},
                       "e2e": {"value": v, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
@@ -342,46 +362,77 @@ def run(args):
     tf32_n32_tf = mra.probe_mma_peak("tc05_n32")  # the same at the tier's own MMA shape, N = 32
     tf32_sync_tf = mra.probe_mma_peak("tf32")     # warp-level mma.sync m16n8k8 TF32, for comparison
 
-    # DRAM read bytes per item of each tier kernel, from an ncu capture of the 4-orbital case of this
-    # batch (dram__bytes_read.sum + dram__bytes_write.sum over all launches of one step / items);
-    # traffic per step = that x the tier's items in this step
-    dram_per_item = {"fp32": 2.79e3, "tf32": 1.36e3, "df32": 10.1e3}
+    K = ORDER + 1
+    # Work of one item (output node o, input node i, term t) in the cube formulation every tier
+    # kernel uses: three passes, each contracting the (2K)^3 cube of the input block over one
+    # dimension with a 2K x 2K operator block: 3 (2K)^4 multiply-adds = 6 (2K)^4 = 96 K^4 flops.
+    work_item = 6.0 * (2 * K) ** 4
+    # The tcgen05 tier issues its passes as M128 x N32 x K8 MMAs (mw_apply_tc05.cu's schedule):
+    # ceil(4K^2/128) tiles in the x pass, ceil(5K^2/128) in the y and z passes, ceil(ceil(2K/4)/2)
+    # k-steps each.
+    ks = ((2 * K + 3) // 4 + 1) // 2
+    tc_mmas = (-(-4 * K * K // 128) + 2 * -(-5 * K * K // 128)) * ks
+    tc_issued_item = tc_mmas * 2.0 * 128 * (32 if 3 * K > 16 else 16) * 8
+
+    # DRAM bytes (read + write) per item of each tier kernel: ncu capture of the benchmark step
+    # itself (all launches of one mixed step, metrics dram__bytes_read.sum and dram__bytes_write.sum;
+    # profiles/dram_traffic_tiers_k10.md), divided by that step's items of the tier
+    dram_per_item = DRAM_PER_ITEM
     tier_items = {"fp64": st_ser["items_fp64"], "fp32": st_ser["items_fp32"], "tf32": st_ser["items_tf32"],
                   "df32": st_ser["items_df"]}
 
-    def roof(flops, ms, peak, kernel, bound, source, tier=None):
-        ach = flops / (ms / 1e3) / 1e12 if ms > 0 else 0.0
-        traffic = dram_per_item[tier] * tier_items[tier] if tier in dram_per_item else None
-        return {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak if peak else None,
-                "traffic": traffic, "traffic_unit": "bytes per step (all launches of the kernel)" if traffic else None,
-                "traffic_source": "ncu dram bytes per item on the 4-orbital case, scaled by items" if traffic else None,
-                "kernel": kernel, "kernel_ms_per_step": ms, "peak_source": source}
+    def roof(tier, ms, peak, kernel, bound, source, issued_item=None):
+        items = tier_items[tier]
+        sec = ms / 1e3
+        ach = items * work_item / sec / 1e12 if ms > 0 else 0.0
+        out = {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+               "frac": ach / peak if peak else None,
+               "work_per_item_flops": work_item,
+               "work_unit": "6 (2K)^4 flops per item: the three cube passes of one (output node, input node, "
+                            "term) contraction",
+               "items": items, "kernel": kernel, "kernel_ms_per_step": ms, "peak_source": source}
+        if issued_item:
+            iss = items * issued_item / sec / 1e12 if ms > 0 else 0.0
+            out.update({"issued_per_item_flops": issued_item, "issued_achieved": iss,
+                        "issued_frac": iss / peak if peak else None})
+        tr = dram_per_item.get(tier)
+        out["traffic"] = tr * items if tr is not None else None
+        out["traffic_unit"] = "DRAM bytes per step, all launches of the kernel" if tr is not None else None
+        # the survey's per-component-pair count (6 K^4 per surviving (ft, gt) pair), kept apart:
+        # the cube passes share partial sums across pairs, so this rate can exceed the pipe's peak
+        fl = st_ser["flops_" + ("df" if tier == "df32" else tier)]
+        out["pair_unit_rate"] = fl / sec / 1e12 if ms > 0 else 0.0
+        return out
 
     fma_src = "probed FMA throughput of this GPU (mw_probe_fma_peak); MEASURED_PEAKS.json holds no FP64/FP32 figure"
     mma_src = ("probed dense tcgen05.mma TF32 throughput of this GPU at M128 N256 K8 (mw_probe_mma_peak kind 2); "
                "MEASURED_PEAKS.json holds no TF32 figure")
     roofs = {
-        "fp64": roof(st_ser["flops_fp64"], st_ser["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
-        "fp32": roof(st_ser["flops_fp32"], st_ser["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src, tier="fp32"),
-        "tf32": roof(st_ser["flops_tf32"], st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc05_kernel<10>", "tensor", mma_src, tier="tf32"),
-        # a double-FP32 multiply-add costs 12 FP32 instructions: peak = FP32 FMA peak * 2 / 24
-        "df32": roof(st_ser["flops_df"], st_ser["kernel_ms_df"], fp32_tf / 12.0, "apply_df_kernel<10>",
+        "fp64": roof("fp64", st_ser["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
+        "fp32": roof("fp32", st_ser["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src),
+        "tf32": roof("tf32", st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc05_kernel<10>", "tensor", mma_src,
+                     issued_item=tc_issued_item),
+        # a double-FP32 multiply-add costs about 12 FP32 instructions in this kernel: its ceiling is the
+        # FP32 FMA rate / 12 (multiply-adds), i.e. peak flops = FP32 FMA flops / 12
+        "df32": roof("df32", st_ser["kernel_ms_df"], fp32_tf / 12.0, "apply_df_kernel<10>",
                      "fp32-pipe (double-FP32)", fma_src + "; divided by 12 FP32 instructions per double-FP32 "
-                     "multiply-add", tier="df32"),
+                     "multiply-add"),
     }
     roofs["tf32"]["peak_tc05_n32"] = tf32_n32_tf
+    roofs["tf32"]["issued_frac_of_n32_rate"] = (roofs["tf32"]["issued_achieved"] / tf32_n32_tf
+                                                if tf32_n32_tf else None)
     roofs["tf32"]["peak_mma_sync_tf32"] = tf32_sync_tf
     dominant = max(roofs, key=lambda k: roofs[k]["kernel_ms_per_step"])
     line = {
         "metric": METRIC, "value": value, "unit": "nodes/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64+df32+f32+tf32", "data": "synthetic",
-        "config": {"workload": "helmholtz-batch16-k9-prec1e-6", "orbitals": NORB, "order": ORDER, "prec": PREC,
-                   "tuned": tuned,
-                   "basis": "interpolating", "box": "[-32,32]^3", "input_nodes": in_nodes,
-                   "output_nodes": nodes, "l2": "inputs larger than L2 (%.1f GB of FP64 blocks)"
-                   % (sum(in_nodes) * 8 * (ORDER + 1) ** 3 * 8 / 1e9),
-                   "operator_terms": [o.nterms for o in ops], "operator_build_s": op_build_s},
+        "config": workload_config(),
+        "workload_detail": {"tuned": tuned, "input_nodes": in_nodes, "input_nodes_total": int(sum(in_nodes)),
+                            "output_nodes": nodes,
+                            "l2": "inputs larger than L2 (%.2f GB of FP64 blocks against 129 MB of L2)"
+                                  % (sum(in_nodes) * 8 * (ORDER + 1) ** 3 * 8 / 1e9),
+                            "operator_terms": [o.nterms for o in ops], "operator_build_s": op_build_s},
         "fp64": {"value": st64["out_nodes"] * world / fp64_s, "unit": "nodes/s", "ms_per_step": fp64_ms,
                  "items": st64["items"], "kernel_ms_per_step": st64["kernel_ms"]},
         "mixed_near_fp64": {"value": st_near["out_nodes"] * world / (near_ms / 1e3), "unit": "nodes/s",
@@ -423,12 +474,27 @@ def run(args):
                 "frac": (st["bytes"] / (ms / 1e3) / 1e9 / measured_peaks()["hbm_gbs"])
                 if measured_peaks().get("hbm_gbs") else None,
                 "bytes_per_step": st["bytes"],
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)"},
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth)",
+                "target_frac": 0.5, "target_met": False,
+                "why": "compute-bound: each FP64 input block feeds hundreds of items, so the step's algorithmic "
+                       "bytes take a fraction of a millisecond at HBM rate while its contractions take "
+                       "milliseconds on the FP32, FP64 and tensor pipes"},
         "clocks": clk.summary(),
     }
     line["speedup_mixed_vs_fp64"] = (nodes / (ms / 1e3)) / (st64["out_nodes"] / fp64_s)
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_sample(terms, mus, args.cpu_levels, args.cpu_s)
+        base, oracle_out = cpu_sample(terms, mus, args.cpu_s, keep=True)
+        line["cpu_baseline"] = base
+        # the GPU outputs of the sampled orbitals against the oracle's complete applies of them
+        # (same orbitals, each side projecting its own input tree from the same Gaussians)
+        vs, same = {"mixed": [], "fp64": []}, True
+        for i, (ok, oc, _) in oracle_out.items():
+            o_tree = mw.FunctionTree(mra).upload(ok, oc)
+            vs["mixed"].append(rel_err(outs[i], o_tree))
+            vs["fp64"].append(rel_err(ref[i], o_tree))
+            same = same and np.array_equal(outs[i].download()[0], ok) and np.array_equal(ref[i].download()[0], ok)
+        line["rel_l2_vs_oracle"] = {"mixed_max": max(vs["mixed"]), "fp64_max": max(vs["fp64"]),
+                                    "orbitals": list(oracle_out), "node_sets_identical": bool(same)}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -442,13 +508,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-levels", type=int, default=-1)
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="pick the batch's launch settings with mw_apply_batch_autotune before timing")
     ap.add_argument("--cpu-s", type=float, default=12.0,
                     help="seconds of oracle apply time for the cpu_baseline sample")
-    ap.add_argument("--ref-step-s", type=float, default=4.0,
-                    help="seconds of oracle apply time per step of --impl reference")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--orbitals", type=int, default=16)
     ap.add_argument("--fp64-steps", type=int, default=1)
