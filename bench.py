@@ -180,6 +180,235 @@ def run_reference(args):
                       "e2e": {"value": v, "unit": "nodes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def poly_orbitals(rng, n, lo, hi):
+    """n orbitals p(r - R) exp(-a |r - R|^2): random cubic p (20 N(0,1) coefficients), a
+    log-uniform in [lo, hi], R uniform in [-2, 2]^3."""
+    mons = cubic_monomials()
+    out = []
+    for _ in range(n):
+        alpha = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        R = rng.uniform(-2.0, 2.0, 3)
+        out.append([(float(c), alpha, tuple(R), m) for c, m in zip(rng.standard_normal(len(mons)), mons)])
+    return out
+
+
+def other_configs(mw, device, world, sync, steps):
+    """The other workloads of the benchmark definition, each timed on the GPU (CUDA events around
+    `steps` repetitions after one untimed) beside its error against FP64 and the oracle, and the
+    oracle's own rate on the host cores (cpu_baseline: OpenMP FP64, the same inputs).
+
+    poisson_k7:   plain FP64 Poisson apply of 4 normalized Gaussians (k=7, prec 1e-5, relative)
+    helmholtz_prec1e-5 / _prec1e-7: the 16-orbital batch at those precisions, mixed vs FP64
+    exchange_528: 32 orbitals, all 528 pair products rho_ij = phi_i phi_j (multiply at prec/10,
+                  absolute, max-norm estimates) then the Poisson apply of each (prec*10, absolute,
+                  steered by phi_i, phi_j; ExchangePotential.cpp:166-204), mixed precision."""
+    import math
+    import torch
+
+    from oracle import pyoracle as po
+    po.build()
+    po.set_threads(os.cpu_count() or 1)
+    out = {}
+
+    def timed(fn, n):
+        fn()
+        sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            r = fn()
+        e1.record()
+        sync()
+        return e0.elapsed_time(e1) / n, r
+
+    def rel_vs_oracle(mra, t, otree):
+        k2, c2, _ = otree.export()
+        o = mw.FunctionTree(mra).upload(k2, c2)
+        d = mw.FunctionTree(mra)
+        mw.add(-1.0, d, [(1.0, t), (-1.0, o)])
+        return d.norm() / max(o.norm(), 1e-300), bool(np.array_equal(t.download()[0], k2))
+
+    def rel_err(mra, a, r):
+        d = mw.FunctionTree(mra)
+        mw.add(-1.0, d, [(1.0, a), (-1.0, r)])
+        return d.norm() / max(r.norm(), 1e-300)
+
+    # ---- Poisson, one density, plain FP64 ----
+    prec, rng = 1e-5, np.random.default_rng(SEED)
+    alphas = np.exp(rng.uniform(np.log(0.5), np.log(50.0), 4))
+    centres = rng.uniform(-2, 2, (4, 3))
+    terms = [((a / math.pi) ** 1.5, float(a), tuple(c), (0, 0, 0)) for a, c in zip(alphas, centres)]
+    mra, omra = mw.MultiResolutionAnalysis(7, device=device), po.MRA(7)
+    orho = po.project_gauss(prec, po.Tree(omra), terms)
+    rho = mw.FunctionTree(mra).upload(*orho.export()[:2])
+    P = mw.PoissonOperator(mra, prec)
+    V = mw.FunctionTree(mra)
+
+    def step1():
+        V.clear()
+        return mw.apply(prec, V, P, rho, precision="fp64")
+
+    ms, st = timed(step1, steps)
+    oV = po.Tree(omra)
+    t0 = time.perf_counter()
+    ost = po.apply(prec, oV, po.poisson(omra, prec), orho)
+    cpu_s = time.perf_counter() - t0
+    e_or, same = rel_vs_oracle(mra, V, oV)
+    pts = np.random.default_rng(SEED + 1).uniform(-4, 4, (300, 3))
+    exact = np.array([sum(math.erf(math.sqrt(a) * np.linalg.norm(p - r)) / np.linalg.norm(p - r)
+                          for a, r in zip(alphas, centres)) for p in pts])
+    out["poisson_k7"] = {
+        "value": st["out_nodes"] * world / (ms / 1e3), "unit": "nodes/s", "ms_per_step": ms, "dtype": "f64",
+        "input_nodes": rho.nnodes, "output_nodes": st["out_nodes"], "items": st["items"],
+        "rel_l2_vs_oracle": e_or, "node_set_identical_to_oracle": same,
+        "erf_max_abs_err_rel": float(np.abs(V.evalf(pts) - exact).max() / np.abs(exact).max()),
+        "cpu_baseline": {"value": ost["out_nodes"] / cpu_s, "unit": "nodes/s", "cores": po.get_threads(),
+                         "kind": "port", "sample": "the same apply, complete (%.2f s)" % cpu_s}}
+
+    # ---- the 16-orbital Helmholtz batch at prec 1e-5 and 1e-7 ----
+    for prec in (1e-5, 1e-7):
+        rng = np.random.default_rng(SEED)
+        terms, mus = orbital_terms(rng)
+        mra, omra = mw.MultiResolutionAnalysis(ORDER, device=device), po.MRA(ORDER)
+        ophis, phis = [], []
+        for t in terms:
+            f = po.project_gauss(prec, po.Tree(omra), t, abs_prec=True)
+            f.rescale(1.0 / f.norm())
+            ophis.append(f)
+            phis.append(mw.FunctionTree(mra).upload(*f.export()[:2]))
+        ops = mw.HelmholtzOperator.batch(mra, mus, prec)
+        o64 = [mw.FunctionTree(mra) for _ in phis]
+        omx = [mw.FunctionTree(mra) for _ in phis]
+
+        def stepb(outs, mode):
+            for o in outs:
+                o.clear()
+            return mw.apply_batch([prec] * NORB, outs, ops, phis, abs_prec=True, precision=mode)
+
+        ms64, st64 = timed(lambda: stepb(o64, "fp64"), 1)
+        msmx, stmx = timed(lambda: stepb(omx, "mixed"), steps)
+        oout = po.Tree(omra)
+        t0 = time.perf_counter()
+        ost = po.apply(prec, oout, po.helmholtz(omra, float(mus[0]), prec), ophis[0], abs_prec=True)
+        cpu_s = time.perf_counter() - t0
+        e_mx, same_mx = rel_vs_oracle(mra, omx[0], oout)
+        e_64, same_64 = rel_vs_oracle(mra, o64[0], oout)
+        out["helmholtz_prec%g" % prec] = {
+            "value": stmx["out_nodes"] * world / (msmx / 1e3), "unit": "nodes/s", "ms_per_step": msmx,
+            "dtype": "f64+df32+f32+tf32", "fp64": {"value": st64["out_nodes"] * world / (ms64 / 1e3),
+                                                  "ms_per_step": ms64},
+            "speedup_mixed_vs_fp64": ms64 / msmx,
+            "input_nodes_total": int(sum(p.nnodes for p in phis)), "output_nodes": stmx["out_nodes"],
+            "items": {"fp64": stmx["items_fp64"], "df32": stmx["items_df"], "fp32": stmx["items_fp32"],
+                      "tf32": stmx["items_tf32"]},
+            "rel_l2_vs_fp64_per_orbital_max": max(rel_err(mra, a, r) for a, r in zip(omx, o64)),
+            "rel_l2_vs_oracle_orbital0": {"mixed": e_mx, "fp64": e_64, "node_sets_identical": same_mx and same_64},
+            "cpu_baseline": {"value": ost["out_nodes"] / cpu_s, "unit": "nodes/s", "cores": po.get_threads(),
+                             "kind": "port", "sample": "orbital 0, complete adaptive apply (%.2f s)" % cpu_s}}
+
+    # ---- exchange-like: 528 pair products, then their Poisson applies ----
+    prec = 1e-5
+    rng = np.random.default_rng(SEED)
+    orbs = poly_orbitals(rng, 32, 0.5, 10.0)
+    mra, omra = mw.MultiResolutionAnalysis(7, device=device), po.MRA(7)
+    phis = []
+    for t in orbs:
+        f = mw.project(prec, mw.FunctionTree(mra), t, abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        phis.append(f)
+    pairs = [(i, j) for i in range(32) for j in range(i, 32)]
+    P = mw.PoissonOperator(mra, prec)
+    pt = [[phis[i], phis[j]] if i != j else [phis[i]] for i, j in pairs]
+    rhos = [mw.FunctionTree(mra) for _ in pairs]
+    vmx = [mw.FunctionTree(mra) for _ in pairs]
+    parts = {}
+
+    def step4():
+        for t in rhos + vmx:
+            t.clear()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        sm = mw.multiply_batch(prec / 10, rhos, 1.0, [phis[i] for i, _ in pairs], [phis[j] for _, j in pairs],
+                               abs_prec=True, use_max_norms=True)
+        e[1].record()
+        sa = mw.apply_batch(prec * 10, vmx, [P] * len(pairs), rhos, prec_trees=pt, abs_prec=True, precision="mixed")
+        e[2].record()
+        parts["e"] = e
+        return sm, sa
+
+    ms4, (sm, sa) = timed(step4, max(1, steps // 3))
+    e = parts["e"]
+    mul_ms, app_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    v64 = [mw.FunctionTree(mra) for _ in pairs]
+    mw.apply_batch(prec * 10, v64, [P] * len(pairs), rhos, prec_trees=pt, abs_prec=True, precision="fp64")
+    worst = 0.0
+    for a, b in zip(vmx, v64):
+        d = mw.FunctionTree(mra)
+        mw.add(-1.0, d, [(1.0, a), (-1.0, b)])
+        worst = max(worst, d.norm() / max(b.norm(), 1.0))
+    # four pairs against the oracle (multiply and FP64 apply from the same input trees), timed
+    sample = [pairs[k] for k in (0, 37, 300, 527)]
+    oP = po.poisson(omra, prec)
+    orac = {"rho": 0.0, "V": 0.0}
+    same = True
+    cpu_s, cpu_nodes = 0.0, 0
+    for (i, j) in sample:
+        k = pairs.index((i, j))
+        oa = po.Tree.from_arrays(omra, *phis[i].download()[:2])
+        ob = po.Tree.from_arrays(omra, *phis[j].download()[:2])
+        t0 = time.perf_counter()
+        orho = po.Tree(omra)
+        po.multiply(prec / 10, orho, 1.0, oa, ob, -1, True, True)
+        oV = po.Tree(omra)
+        ost = po.apply(prec * 10, oV, oP, orho, abs_prec=True, prec_trees=[oa, ob] if i != j else [oa])
+        cpu_s += time.perf_counter() - t0
+        cpu_nodes += orho.nnodes + ost["out_nodes"]
+        er, s1 = rel_vs_oracle(mra, rhos[k], orho)
+        ev, s2 = rel_vs_oracle(mra, v64[k], oV)
+        orac["rho"], orac["V"] = max(orac["rho"], er), max(orac["V"], ev)
+        same = same and s1 and s2
+    out["exchange_528"] = {
+        "value": len(pairs) * world / (ms4 / 1e3), "unit": "pairs/s", "ms_per_step": ms4,
+        "multiply_ms": mul_ms, "apply_ms": app_ms, "dtype": "df32 multiply + mixed apply",
+        "nodes_per_s": (sm["out_nodes"] + sa["out_nodes"]) * world / (ms4 / 1e3),
+        "input_nodes_total": int(sum(p.nnodes for p in phis)), "product_nodes": int(sum(r.nnodes for r in rhos)),
+        "multiply_nodes_computed": sm["out_nodes"], "apply_output_nodes": sa["out_nodes"],
+        "potential_err_vs_fp64_max": worst,
+        "potential_err_unit": "|V_mixed - V_fp64| / max(|V_fp64|, 1): absolute precision",
+        "rel_l2_vs_oracle_4_pairs": {"products": orac["rho"], "potentials_fp64": orac["V"],
+                                     "pairs": sample, "node_sets_identical": same},
+        "graph_captured": False,
+        "cpu_baseline": {"value": len(sample) / cpu_s, "unit": "pairs/s", "cores": po.get_threads(), "kind": "port",
+                         "sample": "pairs %s: multiply + FP64 apply each (%d nodes, %.1f s)" % (sample, cpu_nodes, cpu_s)}}
+    return out
+
+
+def exchange_profile(mw, device, norb, reps):
+    """The exchange-like workload of other_configs() on its first `norb` orbitals, `reps` times."""
+    prec = 1e-5
+    rng = np.random.default_rng(SEED)
+    orbs = poly_orbitals(rng, 32, 0.5, 10.0)[:norb]
+    mra = mw.MultiResolutionAnalysis(7, device=device)
+    phis = []
+    for t in orbs:
+        f = mw.project(prec, mw.FunctionTree(mra), t, abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        phis.append(f)
+    pairs = [(i, j) for i in range(norb) for j in range(i, norb)]
+    P = mw.PoissonOperator(mra, prec)
+    pt = [[phis[i], phis[j]] if i != j else [phis[i]] for i, j in pairs]
+    rhos = [mw.FunctionTree(mra) for _ in pairs]
+    vmx = [mw.FunctionTree(mra) for _ in pairs]
+    for _ in range(reps):
+        for t in rhos + vmx:
+            t.clear()
+        sm = mw.multiply_batch(prec / 10, rhos, 1.0, [phis[i] for i, _ in pairs], [phis[j] for _, j in pairs],
+                               abs_prec=True, use_max_norms=True)
+        sa = mw.apply_batch(prec * 10, vmx, [P] * len(pairs), rhos, prec_trees=pt, abs_prec=True, precision="mixed")
+    mra.synchronize()
+    return {"pairs": len(pairs), "multiply": sm, "apply": sa}
+
+
 def max_over_ranks(ms, device):
     """The slowest rank's time: every rank's timed region ends at a barrier, the job at its last rank."""
     import torch
@@ -249,6 +478,12 @@ def run(args):
         barrier()
         return e0.elapsed_time(e1) / steps, st_
 
+    if args.profile_exchange:
+        # profiling mode: only the exchange-like workload on its first N orbitals (N(N+1)/2 pair
+        # products and their Poisson applies), W + K times, for ncu captures of the multiply
+        prof = exchange_profile(mw, local, args.profile_exchange, args.warmup + args.steps)
+        print(json.dumps({"profile_exchange": True, **prof}))
+        return
     if args.profile_mixed:
         # profiling mode: only the W + K mixed steps run (for a launch list of the headline step)
         for _ in range(args.warmup + args.steps):
@@ -495,6 +730,8 @@ def run(args):
             same = same and np.array_equal(outs[i].download()[0], ok) and np.array_equal(ref[i].download()[0], ok)
         line["rel_l2_vs_oracle"] = {"mixed_max": max(vs["mixed"]), "fp64_max": max(vs["fp64"]),
                                     "orbitals": list(oracle_out), "node_sets_identical": bool(same)}
+    if args.configs:
+        line["configs"] = other_configs(mw, local, world, barrier, max(3, args.steps // 2))
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -513,9 +750,13 @@ def main():
     ap.add_argument("--cpu-s", type=float, default=12.0,
                     help="seconds of oracle apply time for the cpu_baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--configs", action=argparse.BooleanOptionalAction, default=True,
+                    help="also time the other workloads (Poisson k=7, the batch at prec 1e-5 / 1e-7, exchange-like)")
     ap.add_argument("--orbitals", type=int, default=16)
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--profile-mixed", action="store_true")
+    ap.add_argument("--profile-exchange", type=int, default=0, metavar="N",
+                    help="run only the exchange-like workload on its first N orbitals (for ncu)")
     args = ap.parse_args()
     global NORB
     NORB = args.orbitals

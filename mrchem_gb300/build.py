@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libmwgb300.so")
 SOURCES = ["mw_kernels.cu", "mw_basis.cpp", "mw_tree.cpp", "mw_apply.cpp", "mw_capi.cpp", "mw_noalloc.cu", "mw_apply_df.cu", "mw_screen.cu",
-           "mw_post_df.cu", "mw_apply_tc05.cu", "mw_opbuild.cu"]
+           "mw_post_df.cu", "mw_apply_tc05.cu", "mw_opbuild.cu", "mw_multiply_df.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

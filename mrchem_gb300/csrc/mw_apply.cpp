@@ -281,7 +281,7 @@ struct DevItems {
 };
 
 int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, int tier, long long chunk,
-                 mw_stats &st, const DevItems *dv = nullptr) {
+                 mw_stats &st, const DevItems *dv = nullptr, bool split_tc = false) {
     const int nn = (int)li.nodes;
     const size_t ni = (size_t)li.items;
     if (nn == 0) return nullptr;
@@ -389,14 +389,17 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     }
     st.launches++;
     int *hs = nullptr;
+    // tier 1 in the tensor-core modes: the split-TF32 tcgen05 kernel (FP32 accuracy); else the
+    // FP32 CUDA-core kernel
+    const bool tc = tier == 2 || (tier == 1 && split_tc);
     if (tier == 3) {
         k_apply_df(ctx.dbasis, L, ctx.nsm, ctx.stream);
     } else {
-        if (tier == 2)
-            k_apply_tc05(ctx.dbasis, L, ctx.stream);
+        if (tc)
+            k_apply_tc05(ctx.dbasis, L, tier == 1, ctx.stream);
         else
             k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
-        if (tier == 2) {  // the TF32 kernel waits for bulk copies with a bound
+        if (tc) {  // the tensor-core kernels wait for bulk copies with a bound
             hs = (int *)arena.halloc(sizeof(int));
             *hs = 0;
             MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
@@ -723,8 +726,8 @@ void screen_level_gpu(Ctx &ctx, Arena &ar, DevScreen &ds, const std::vector<JobS
     P.tier_fp64 = TIER_FP64;
     P.tier_tf32 = TIER_TF32;
     P.tier_df = TIER_DF;
-    P.tx = tc5_x_floats(K);
-    P.tb = tc5_b_floats(K);
+    P.tx = tc5_x_stride(K);
+    P.tb = tc5_b_stride(K);
     // walk 1: candidate counts and generation requests (tables grown and the walk repeated if a
     // job's generation table fills up)
     int *hc = nullptr;
@@ -951,7 +954,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             }
             if (tensor && in.cap_tc < (size_t)in.nn()) {
                 if (in.d_coefs_tc) cudaFree(in.d_coefs_tc);
-                MWG_CUDA(cudaMalloc(&in.d_coefs_tc, sizeof(float) * tc5_x_floats(b.K) * in.cap));
+                MWG_CUDA(cudaMalloc(&in.d_coefs_tc, sizeof(float) * tc5_x_stride(b.K) * in.cap));
                 in.cap_tc = in.cap;
             }
             if (!hin) convert_input(in);
@@ -1171,7 +1174,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     k_to_fp32_cube(first, first32, total, b.K, ctx.stream);
                     st.launches++;
                     if (tensor) {
-                        firsttc = (float *)ar.alloc(sizeof(float) * tc5_x_floats(b.K) * total);
+                        firsttc = (float *)ar.alloc(sizeof(float) * tc5_x_stride(b.K) * total);
                         k_to_tc_x(first32, firsttc, total, b.K, ctx.stream);
                         st.launches++;
                     }
@@ -1181,7 +1184,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     s.gbase = s.gens.base;
                     s.gcn.swap(s.gens.cn);
                     s.gbase32 = (first32 && s.gbase) ? first32 + 2 * (s.gbase - first) : nullptr;
-                    s.gbase_tc = (firsttc && s.gbase) ? firsttc + tc5_x_floats(b.K) * (size_t)((s.gbase - first) / bs) : nullptr;
+                    s.gbase_tc = (firsttc && s.gbase) ? firsttc + tc5_x_stride(b.K) * (size_t)((s.gbase - first) / bs) : nullptr;
                 }
             }
             auto tC = std::chrono::steady_clock::now();
@@ -1283,9 +1286,9 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                         T.ax[pi] = op.d_blocks + (size_t)bxi * bsz;
                         T.ay[pi] = op.d_blocks + (size_t)byi * bsz;
                         T.az[pi] = op.d_blocks + (size_t)bzi * bsz;
-                    } else if (cd.tier == 2) {
-                        // the tensor-core tier reads its own operand layouts (mw_tc05_layout.h)
-                        const size_t tx = tc5_x_floats(b.K), tb = tc5_b_floats(b.K);
+                    } else if (cd.tier == 2 || (cd.tier == 1 && tensor)) {
+                        // the tensor-core tiers read their own operand layouts (mw_tc05_layout.h)
+                        const size_t tx = tc5_x_stride(b.K), tb = tc5_b_stride(b.K);
                         T.in[pi] = cd.gen ? (const void *)(s.gbase_tc + tx * (size_t)cd.src)
                                           : (const void *)(inp.d_coefs_tc + tx * (size_t)cd.src);
                         T.ax[pi] = op.d_blocks_tc + tb * (size_t)bxi;
@@ -1322,7 +1325,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         MWG_CUDA(cudaEventRecord(G.ev[0], ctx.stream));
         G.status.clear();
         for (int k = 0; k < NTIER; k++) {
-            int *hs = launch_tier(ctx, ar, lt[k], root, false, k, tune.chunk[k], st, dscreen ? &dv : nullptr);
+            int *hs = launch_tier(ctx, ar, lt[k], root, false, k, tune.chunk[k], st, dscreen ? &dv : nullptr,
+                                  tensor && k == 1);
             if (hs) G.status.push_back(hs);
             MWG_CUDA(cudaEventRecord(G.ev[k + 1], ctx.stream));
         }
@@ -1564,7 +1568,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
 
 // ------------------------------------------------------------------ multiply
 // bottom-up compression of several trees, one launch per scale
-void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st) {
+void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st, bool df) {
     if (trees.empty()) return;
     Ctx &ctx = *trees[0]->ctx;
     int maxn = ctx.basis.n0;
@@ -1583,7 +1587,12 @@ void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st
         pk.add(tasks.data(), tasks.size() * sizeof(PairTask));
         pk.add(cnp.data(), cnp.size() * sizeof(double *));
         pk.ship(ctx, arena);
-        k_compress(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(), ctx.stream);
+        if (df)
+            k_compress_df(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(),
+                          ctx.stream);
+        else
+            k_compress(ctx.dbasis, (const PairTask *)pk.ptr(0), (double *const *)pk.ptr(1), (int)tasks.size(),
+                       ctx.stream);
         if (st) st->launches++;
     }
     for (Tree *t : trees)
@@ -1615,10 +1624,12 @@ std::vector<double> detail_tails(const Tree &t) {
 
 struct MulState {
     MulJob *job;
-    std::vector<double> ta, tb;
+    const std::vector<double> *ta = nullptr, *tb = nullptr;  // the inputs' detail tails (useMaxNorms)
     std::vector<int> work;
     int iter = 0;
     GenSet ga, gb;
+    std::vector<MulTask> tasks;  // this level's node tasks
+    std::vector<double> crit;    // ... and their max-norm criteria
 };
 
 }  // namespace
@@ -1635,15 +1646,32 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
     const Basis &bsis = ctx.basis;
     Arena &arena = ctx.arena;
     auto t_start = std::chrono::steady_clock::now();
+    using clk = std::chrono::steady_clock;
+    auto since = [](clk::time_point t0) { return std::chrono::duration<double, std::milli>(clk::now() - t0).count(); };
     std::vector<MulState> ms(jobs.size());
+    // the inputs' unresolved detail, once per distinct input tree (the exchange products share
+    // their 32 orbitals among 528 jobs)
+    std::vector<std::pair<const Tree *, std::vector<double>>> tails;
+    {
+        std::unordered_map<const Tree *, int> idx;
+        for (auto &j : jobs)
+            if (j.use_max_norms)
+                for (const Tree *t : {j.a, j.b})
+                    if (idx.emplace(t, (int)tails.size()).second) tails.push_back({t, {}});
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long i = 0; i < (long)tails.size(); i++) tails[i].second = detail_tails(*tails[i].first);
+        for (size_t j = 0; j < jobs.size(); j++)
+            if (jobs[j].use_max_norms) {
+                ms[j].ta = &tails[idx.at(jobs[j].a)].second;
+                ms[j].tb = &tails[idx.at(jobs[j].b)].second;
+            }
+    }
     for (size_t j = 0; j < jobs.size(); j++) {
         MulState &s = ms[j];
         s.job = &jobs[j];
-        if (jobs[j].use_max_norms) {
-            s.ta = detail_tails(*jobs[j].a);
-            s.tb = detail_tails(*jobs[j].b);
-        }
         Tree &out = *jobs[j].out;
+        // a product's grid rarely outgrows the smaller input's: sized once for that
+        out.reserve(std::max((size_t)out.nn(), (size_t)std::min(jobs[j].a->nn(), jobs[j].b->nn())));
         for (int i = 0; i < out.nn(); i++)
             if (out.nodes[i].child0 < 0) s.work.push_back(i);
     }
@@ -1652,8 +1680,12 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
         for (auto &s : ms) any |= !s.work.empty();
         if (!any) break;
         arena.reset();
-        std::vector<std::pair<GenSet *, const Tree *>> sets;
-        for (auto &s : ms) {
+        auto tA = clk::now();
+        // input blocks to generate at this level's output nodes (jobs in parallel: each has its own
+        // sets and reads its shared input trees only)
+#pragma omp parallel for schedule(dynamic, 4)
+        for (long j = 0; j < (long)ms.size(); j++) {
+            MulState &s = ms[j];
             s.ga.clear();
             s.gb.clear();
             Tree &out = *s.job->out, &a = *s.job->a, &b = *s.job->b;
@@ -1662,51 +1694,73 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
                 if (a.find(o.n, o.l) < 0) s.ga.request(a, o.n, o.l, find_ancestor(a, o.n, o.l, nullptr));
                 if (b.find(o.n, o.l) < 0) s.gb.request(b, o.n, o.l, find_ancestor(b, o.n, o.l, nullptr));
             }
-            sets.push_back({&s.ga, &a});
-            sets.push_back({&s.gb, &b});
         }
-        generate_all(sets, arena, &st);
-        std::vector<MulTask> tasks;
-        std::vector<std::vector<double>> crit(ms.size());
+        std::vector<std::pair<GenSet *, const Tree *>> sets;
         for (auto &s : ms) {
+            sets.push_back({&s.ga, s.job->a});
+            sets.push_back({&s.gb, s.job->b});
+        }
+        st.host_enum_ms += since(tA);
+        auto tB = clk::now();
+        generate_all(sets, arena, &st);
+        st.host_gen_ms += since(tB);
+        auto tC = clk::now();
+        // node tasks and max-norm criteria, jobs in parallel, then concatenated in job order
+#pragma omp parallel for schedule(dynamic, 4)
+        for (long j = 0; j < (long)ms.size(); j++) {
+            MulState &s = ms[j];
             Tree &out = *s.job->out, &a = *s.job->a, &b = *s.job->b;
-            std::vector<double> &cr = crit[&s - &ms[0]];
-            cr.assign(s.work.size(), 0.0);
+            s.tasks.resize(s.work.size());
+            s.crit.assign(s.work.size(), 0.0);
             for (size_t w = 0; w < s.work.size(); w++) {
                 const NodeInfo &o = out.nodes[s.work[w]];
                 int ia = a.find(o.n, o.l), ib = b.find(o.n, o.l);
-                MulTask tk;
+                MulTask &tk = s.tasks[w];
                 tk.a = block_at(a, s.ga, s.ga.base, o.n, o.l);
                 tk.b = block_at(b, s.gb, s.gb.base, o.n, o.l);
                 tk.out = out.block(s.work[w]);
                 tk.cn = out.d_cn + (size_t)8 * s.work[w];
                 tk.scale = s.job->coef * std::pow(2.0, 1.5 * (o.n + 1));
-                tasks.push_back(tk);
                 if (s.job->use_max_norms) {
                     Key k{o.n, {o.l[0], o.l[1], o.l[2]}};
                     const double *cna = ia >= 0 ? &a.cn[8 * (size_t)ia] : &s.ga.cn[8 * (size_t)s.ga.slot.at(k)];
                     const double *cnb = ib >= 0 ? &b.cn[8 * (size_t)ib] : &s.gb.cn[8 * (size_t)s.gb.slot.at(k)];
                     double sc = std::pow(2.0, 1.5 * o.n);
-                    cr[w] = (ia >= 0 ? s.ta[ia] : 0.0) * block_norm8(cnb) * sc +
-                            (ib >= 0 ? s.tb[ib] : 0.0) * block_norm8(cna) * sc;
+                    s.crit[w] = (ia >= 0 ? (*s.ta)[ia] : 0.0) * block_norm8(cnb) * sc +
+                                (ib >= 0 ? (*s.tb)[ib] : 0.0) * block_norm8(cna) * sc;
                 }
             }
         }
+        std::vector<MulTask> tasks;
+        for (auto &s : ms) tasks.insert(tasks.end(), s.tasks.begin(), s.tasks.end());
+        st.host_items_ms += since(tC);
+        auto tD = clk::now();
         Packer pk;
         pk.add(tasks.data(), tasks.size() * sizeof(MulTask));
         pk.ship(ctx, arena);
-        k_multiply(ctx.dbasis, (const MulTask *)pk.ptr(0), (int)tasks.size(), ctx.stream);
+        k_multiply_df(ctx.dbasis, (const MulTask *)pk.ptr(0), (int)tasks.size(), ctx.nsm, ctx.stream);
         st.launches++;
         st.out_nodes += (long long)tasks.size();
+        // the norms of the nodes computed at this level: one copy of their index range when it is
+        // contiguous (the children appended by the last refinement), else the whole array
         for (auto &s : ms) {
             Tree &out = *s.job->out;
-            MWG_CUDA(cudaMemcpyAsync(out.cn.data(), out.d_cn, sizeof(double) * 8 * out.nn(), cudaMemcpyDeviceToHost,
-                                     ctx.stream));
+            if (s.work.empty()) continue;
+            const auto mm = std::minmax_element(s.work.begin(), s.work.end());
+            size_t first = 0, count = (size_t)out.nn();
+            if ((size_t)(*mm.second - *mm.first + 1) == s.work.size()) {
+                first = (size_t)*mm.first;
+                count = s.work.size();
+            }
+            MWG_CUDA(cudaMemcpyAsync(out.cn.data() + 8 * first, out.d_cn + 8 * first, sizeof(double) * 8 * count,
+                                     cudaMemcpyDeviceToHost, ctx.stream));
         }
         ctx.sync();
+        st.host_wait_ms += since(tD);
+        auto tE = clk::now();
+        // refinement; the new children need no zeroing: the next level's kernel writes their blocks
         for (auto &s : ms) {
             Tree &out = *s.job->out;
-            const std::vector<double> &cr = crit[&s - &ms[0]];
             double R = s.job->abs_prec ? 1.0 : std::sqrt(out.sqnorm_leaves());
             std::vector<int> next;
             if (s.job->max_iter < 0 || s.iter < s.job->max_iter) {
@@ -1715,23 +1769,24 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
                     int n = out.nodes[oi].n;
                     if (n >= bsis.max_scale()) continue;
                     double thr = split_thr(s.job->prec, R, n);
-                    if (wavelet_norm8(&out.cn[8 * (size_t)oi]) > thr || cr[w] > thr) {
+                    if (wavelet_norm8(&out.cn[8 * (size_t)oi]) > thr || s.crit[w] > thr) {
                         int c0 = out.split(oi);
                         for (int c = 0; c < 8; c++) next.push_back(c0 + c);
                     }
                 }
-                if (!next.empty()) tree_zero(out, out.nn() - (int)next.size(), (int)next.size());
             }
             s.work.swap(next);
             s.iter++;
         }
+        st.host_refine_ms += since(tE);
         st.levels++;
     }
     std::vector<Tree *> outs;
     for (auto &j : jobs) outs.push_back(j.out);
     arena.reset();
-    compress_batch(outs, arena, &st);
-    arena.reset();
+    auto tF = clk::now();
+    compress_batch(outs, arena, &st, true);
+    st.gpu_post_ms += since(tF);
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }
 

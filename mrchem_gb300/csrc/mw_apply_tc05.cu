@@ -104,6 +104,28 @@ struct T5Geo {
     static_assert(SMEM <= 113 * 1024, "two CTAs per SM");
 };
 
+// Shared-memory layout of the kernel: SPLIT = 0 is the TF32 tier, SPLIT = 1 the split-TF32 tier,
+// whose operands are stored twice (hi, then lo): S_hi S_lo | R_hi R_lo | zero pad | two sets of
+// (B_x hi lo, B_y hi lo, B_z hi lo).  An MMA pass reads past its operand's end (last k-step):
+// S_hi into S_lo, S_lo into R_hi, R_hi into R_lo, R_lo into the pad, all finite and not written
+// while those MMAs run; the B operands are zero there.
+template <int K, int SPLIT>
+struct T5Mem {
+    using G = T5Geo<K>;
+    static constexpr int NP = SPLIT ? 2 : 1;  // stored parts per operand
+    static constexpr int OR = NP * G::SX;      // R (hi) starts here; R lo at OR + RSZ
+    static constexpr int OB = OR + NP * G::RSZ + G::ZPAD;
+    static constexpr int BSET = 3 * NP * G::BSZ;  // one set of B operands
+    static constexpr int SMEM = OB + 2 * BSET;
+    static constexpr uint32_t STAGE_BYTES = (uint32_t)(NP * (G::SX + 3 * G::BSZ));
+    static constexpr int MAX_CTAS = SPLIT ? 1 : G::MAX_CTAS;
+    static constexpr int SMEM_LAUNCH = SPLIT ? SMEM : G::SMEM_LAUNCH;
+    static_assert(SPLIT || (OR == G::OR && OB == G::OB && SMEM == G::SMEM && STAGE_BYTES == G::STAGE_BYTES),
+                  "the TF32 tier's layout");
+    static_assert(OR % 16 == 0 && OB % 16 == 0 && BSET % 16 == 0 && G::RSZ % 16 == 0, "alignment");
+    static_assert(SMEM <= 227 * 1024, "shared memory");
+};
+
 __device__ __forceinline__ float tf32r(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -195,12 +217,20 @@ __device__ __forceinline__ void t5_epilogue(uint32_t tcol, int tiles, int q, int
     }
 }
 
-template <int K>
-__global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyLaunch L) {
+template <int K, int SPLIT>
+__global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_kernel(ApplyLaunch L) {
     using G = T5Geo<K>;
+    using M = T5Mem<K, SPLIT>;
     constexpr int N2 = G::N2, NN = G::NN, KK = G::KK, K3 = G::K3, N = G::N;
     extern __shared__ __align__(1024) uint8_t smem5[];
-    uint8_t *sS = smem5, *sR = smem5 + G::OR, *sB = smem5 + G::OB;
+    uint8_t *sS = smem5, *sR = smem5 + M::OR, *sB = smem5 + M::OB;
+    // an epilogue value into the next pass's A operand: rounded to TF32, and for the split tier
+    // the remainder rounded to TF32 in the lo copy of R
+    auto put = [&](float *dst, float v) {
+        const float h = tf32r(v);
+        dst[0] = h;
+        if (SPLIT) dst[G::RSZ / 4] = tf32r(__fsub_rn(v, h));
+    };
     // barriers: 0 staging copies, 1 x MMAs, 2 y MMAs, 3 end of a node, 4 draining after a failed wait
     __shared__ __align__(8) uint64_t bar[5];
     __shared__ uint32_t s_tmem;
@@ -213,7 +243,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
     const bool excl = !L.root;
 
     // zero everything once: padding rows, columns and k-groups are read by the MMAs
-    for (int i = tid; i < G::SMEM / 16; i += blockDim.x) reinterpret_cast<float4 *>(smem5)[i] = make_float4(0, 0, 0, 0);
+    for (int i = tid; i < M::SMEM / 16; i += blockDim.x) reinterpret_cast<float4 *>(smem5)[i] = make_float4(0, 0, 0, 0);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
                      "r"(G::TMEM_COLS));
@@ -239,12 +269,13 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
     auto stage = [&](const void *in, const void *ax, const void *ay, const void *az, uint32_t set) {
         if (s_fail) return;  // the issuing thread: the item's input block and B operands
         async_fence();
-        mbar_expect_tx(&bar[0], G::STAGE_BYTES);
-        uint8_t *B = sB + set * 3 * G::BSZ;
-        bulk_copy(sS, in, G::SX, &bar[0]);
-        bulk_copy(B, ax, G::BSZ, &bar[0]);
-        bulk_copy(B + G::BSZ, ay, G::BSZ, &bar[0]);
-        bulk_copy(B + 2 * G::BSZ, az, G::BSZ, &bar[0]);
+        mbar_expect_tx(&bar[0], M::STAGE_BYTES);
+        uint8_t *B = sB + set * M::BSET;
+        // each stored operand is hi, then lo (mw_tc05_layout.h): one copy of hi, or of hi and lo
+        bulk_copy(sS, in, M::NP * G::SX, &bar[0]);
+        bulk_copy(B, ax, M::NP * G::BSZ, &bar[0]);
+        bulk_copy(B + M::NP * G::BSZ, ay, M::NP * G::BSZ, &bar[0]);
+        bulk_copy(B + 2 * M::NP * G::BSZ, az, M::NP * G::BSZ, &bar[0]);
     };
     // status on a wait that runs out: 1 + barrier + 8 * (parity) + 16 * (items this CTA had started)
     auto wait = [&](int b) {
@@ -260,15 +291,27 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
         t5_after_sync();
     };
     // the issuing thread: tiles x k-steps of one pass, then a commit to barrier b (none if b < 0)
-    auto issue_pass = [&](uint64_t da, int lbo_a, uint64_t db, int tiles, uint32_t dcol, bool accumulate, int b) {
+    // split tier: hi * hi, then hi * lo and lo * hi into the same accumulator (lo * lo dropped);
+    // a_lo / b_lo: the descriptor offsets of the operands' lo copies
+    auto issue_pass = [&](uint64_t da, int lbo_a, uint32_t a_lo, uint64_t db, int tiles, uint32_t dcol,
+                          bool accumulate, int b) {
         if (s_fail) return;
+        const uint32_t b_lo = (uint32_t)(G::BSZ >> 4);
         for (int i = 0; i < tiles; i++)
 #pragma unroll
-            for (int s = 0; s < G::KS; s++)
-                t5_mma(dcol + (uint32_t)(i * N), da + (uint64_t)((2 * s * lbo_a + i * 2048) >> 4),
-                       db + (uint64_t)((2 * s * G::LBO_B) >> 4), idesc, (accumulate || s > 0) ? 1u : 0u);
+            for (int s = 0; s < G::KS; s++) {
+                const uint64_t a = da + (uint64_t)((2 * s * lbo_a + i * 2048) >> 4);
+                const uint64_t bb = db + (uint64_t)((2 * s * G::LBO_B) >> 4);
+                const uint32_t d = dcol + (uint32_t)(i * N);
+                t5_mma(d, a, bb, idesc, (accumulate || s > 0) ? 1u : 0u);
+                if (SPLIT) {
+                    t5_mma(d, a, bb + b_lo, idesc, 1u);
+                    t5_mma(d, a + a_lo, bb, idesc, 1u);
+                }
+            }
         if (b >= 0) t5_commit(&bar[b]);
     };
+    constexpr uint32_t S_LO = (uint32_t)(G::SX >> 4), R_LO = (uint32_t)(G::RSZ >> 4);
 
     while (true) {
         if (tid == 0) s_node = atomicAdd(L.counter, 1);
@@ -279,7 +322,8 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
         if (issuer && b0 < b1) stage(L.in[b0], L.ax[b0], L.ay[b0], L.az[b0], nitem & 1u);
         for (long long j = b0; j < b1; j++, nitem++) {
             const uint32_t set = nitem & 1u;
-            const uint64_t dBs = dB + (uint64_t)((set * 3 * G::BSZ) >> 4);
+            const uint64_t dBs = dB + (uint64_t)((set * M::BSET) >> 4);
+            constexpr uint32_t BPASS = (uint32_t)((M::NP * G::BSZ) >> 4);  // B_x -> B_y -> B_z
             if (producer) {
                 if (lane == 0) {
                     const bool more = j + 1 < b1;
@@ -291,7 +335,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
                         naz = L.az[j + 1];
                     }
                     wait(0);  // item j's input block and B operands are in S and B set `set`
-                    issue_pass(dS, G::LBO_S, dBs, G::MTX, tD, false, 1);
+                    issue_pass(dS, G::LBO_S, S_LO, dBs, G::MTX, tD, false, 1);
                     // the x MMAs, and every earlier MMA (the previous item's z pass), are done:
                     // S and the other B set are free for item j+1
                     wait(1);
@@ -307,16 +351,16 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
                     const int Z = r / N2, Y = r - Z * N2;
                     float *base = r_at<K>(sR, 0, Y);
 #pragma unroll
-                    for (int xp = 0; xp < N2; xp++) base[4 * (xp * N2 + Z)] = tf32r(__uint_as_float(v[xp]));
+                    for (int xp = 0; xp < N2; xp++) put(base + 4 * (xp * N2 + Z), __uint_as_float(v[xp]));
                     if (Z < K) {
 #pragma unroll
                         for (int xp = 0; xp < K; xp++)
-                            base[4 * (NN + xp * K + Z)] = tf32r(__uint_as_float(Y < K ? v[N2 + xp] : v[xp]));
+                            put(base + 4 * (NN + xp * K + Z), __uint_as_float(Y < K ? v[N2 + xp] : v[xp]));
                     }
                 });
             }
             publish();
-            if (issuer) issue_pass(dR, G::LBO_R, dBs + (uint64_t)(G::BSZ >> 4), G::MT, tD, false, 2);
+            if (issuer) issue_pass(dR, G::LBO_R, R_LO, dBs + BPASS, G::MT, tD, false, 2);
             if (!producer) {
                 // ---- y epilogue: D row (X', Z) -> c * A_z rows (Y', X') with k = Z; extra rows (Y', X' < K)
                 const float cf = float(L.coef[j]);
@@ -327,22 +371,21 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
                         const int xp = r / N2, Z = r - xp * N2;
                         float *base = r_at<K>(sR, 0, Z);
 #pragma unroll
-                        for (int yp = 0; yp < N2; yp++) base[4 * (yp * N2 + xp)] = tf32r(cf * __uint_as_float(v[yp]));
+                        for (int yp = 0; yp < N2; yp++) put(base + 4 * (yp * N2 + xp), cf * __uint_as_float(v[yp]));
                         if (Z >= K && xp < K) {
 #pragma unroll
-                            for (int yp = 0; yp < K; yp++)
-                                base[4 * (NN + yp * K + xp)] = tf32r(cf * __uint_as_float(v[yp]));
+                            for (int yp = 0; yp < K; yp++) put(base + 4 * (NN + yp * K + xp), cf * __uint_as_float(v[yp]));
                         }
                     } else if (r < G::RE) {
                         const int e = r - NN, xp = e / K, Z = e - xp * K;
                         float *base = r_at<K>(sR, 0, Z);
 #pragma unroll
-                        for (int yp = 0; yp < K; yp++) base[4 * (NN + yp * K + xp)] = tf32r(cf * __uint_as_float(v[yp]));
+                        for (int yp = 0; yp < K; yp++) put(base + 4 * (NN + yp * K + xp), cf * __uint_as_float(v[yp]));
                     }
                 });
             }
             publish();
-            if (issuer) issue_pass(dR, G::LBO_R, dBs + (uint64_t)((2 * G::BSZ) >> 4), G::MT, tACC, j != b0, -1);
+            if (issuer) issue_pass(dR, G::LBO_R, R_LO, dBs + 2 * BPASS, G::MT, tACC, j != b0, -1);
         }
         // ---- node epilogue: accumulator rows (Y', X'), columns Z' -> component-major FP64 block
         if (b0 < b1 && issuer && !s_fail) t5_commit(&bar[3]);
@@ -404,17 +447,21 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, 2) apply_tc05_kernel(ApplyL
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(G::TMEM_COLS));
 }
 
-template <int K>
+template <int K, int SPLIT>
 void launch_tc05(const ApplyLaunch &L, cudaStream_t s) {
     using G = T5Geo<K>;
-    MWG_CUDA(cudaFuncSetAttribute(apply_tc05_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM_LAUNCH));
+    using M = T5Mem<K, SPLIT>;
+    MWG_CUDA(cudaFuncSetAttribute(apply_tc05_kernel<K, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  M::SMEM_LAUNCH));
     const int grid = L.nnodes;
     if (grid < 1) return;
-    apply_tc05_kernel<K><<<grid, G::THREADS, G::SMEM_LAUNCH, s>>>(L);
+    apply_tc05_kernel<K, SPLIT><<<grid, G::THREADS, M::SMEM_LAUNCH, s>>>(L);
     MWG_CUDA(cudaGetLastError());
 }
 
-// FP32 cube-order shadow (high cube) -> x-pass operand: float4 (g, r) = row r = Z * 2K + Y, X = 4g .. 4g+3
+// FP32 cube-order shadow -> x-pass operand: float4 (g, r) = row r = Z * 2K + Y, X = 4g .. 4g+3, per
+// block the value rounded to TF32 (hi), then the remainder (the shadow's high cube minus hi, plus its
+// low cube) rounded to TF32 (lo)
 __global__ void to_tc_x_kernel(const float *cube32, float *out, size_t nblocks, int K) {
     const int N2 = 2 * K, NN = N2 * N2, KG = tc5_kg(K), C = NN * N2;
     const size_t per = (size_t)KG * NN, total = nblocks * per;
@@ -422,12 +469,18 @@ __global__ void to_tc_x_kernel(const float *cube32, float *out, size_t nblocks, 
         const size_t blk = i / per;
         const int rem = (int)(i - blk * per), g = rem / NN, r = rem - g * NN;
         const float *src = cube32 + blk * 2 * (size_t)C + (size_t)r * N2 + 4 * g;
-        float4 v;
-        v.x = 4 * g + 0 < N2 ? tf32r(src[0]) : 0.0f;
-        v.y = 4 * g + 1 < N2 ? tf32r(src[1]) : 0.0f;
-        v.z = 4 * g + 2 < N2 ? tf32r(src[2]) : 0.0f;
-        v.w = 4 * g + 3 < N2 ? tf32r(src[3]) : 0.0f;
-        reinterpret_cast<float4 *>(out)[i] = v;
+        const float *srl = src + C;  // the low cube
+        float h[4], l[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const bool in = 4 * g + c < N2;
+            const float v = in ? src[c] : 0.0f;
+            h[c] = tf32r(v);
+            l[c] = tf32r(in ? __fadd_rn(__fsub_rn(v, h[c]), srl[c]) : 0.0f);
+        }
+        float4 *o4 = reinterpret_cast<float4 *>(out);
+        o4[2 * blk * per + rem] = make_float4(h[0], h[1], h[2], h[3]);
+        o4[2 * blk * per + per + rem] = make_float4(l[0], l[1], l[2], l[3]);
     }
 }
 
@@ -511,18 +564,26 @@ void k_to_tc_x(const float *cube32, float *out, size_t nblocks, int K, cudaStrea
     MWG_CUDA(cudaGetLastError());
 }
 
-void k_apply_tc05(const DevBasis &b, const ApplyLaunch &L, cudaStream_t s) {
-    if (L.nnodes <= 0) return;
-    switch (b.K) {
-        case 4: launch_tc05<4>(L, s); break;
-        case 5: launch_tc05<5>(L, s); break;
-        case 6: launch_tc05<6>(L, s); break;
-        case 7: launch_tc05<7>(L, s); break;
-        case 8: launch_tc05<8>(L, s); break;
-        case 9: launch_tc05<9>(L, s); break;
-        case 10: launch_tc05<10>(L, s); break;
+template <int SPLIT>
+void k_apply_tc05_t(int K, const ApplyLaunch &L, cudaStream_t s) {
+    switch (K) {
+        case 4: launch_tc05<4, SPLIT>(L, s); break;
+        case 5: launch_tc05<5, SPLIT>(L, s); break;
+        case 6: launch_tc05<6, SPLIT>(L, s); break;
+        case 7: launch_tc05<7, SPLIT>(L, s); break;
+        case 8: launch_tc05<8, SPLIT>(L, s); break;
+        case 9: launch_tc05<9, SPLIT>(L, s); break;
+        case 10: launch_tc05<10, SPLIT>(L, s); break;
         default: throw Error(MW_ERR_ARG, "no tensor-core apply kernel for this order");
     }
+}
+
+void k_apply_tc05(const DevBasis &b, const ApplyLaunch &L, bool split, cudaStream_t s) {
+    if (L.nnodes <= 0) return;
+    if (split)
+        k_apply_tc05_t<1>(b.K, L, s);
+    else
+        k_apply_tc05_t<0>(b.K, L, s);
 }
 
 }  // namespace mwg

@@ -398,7 +398,7 @@ void build_operators(const std::vector<Oper *> &ops, const Basis &b) {
     for (Oper *op : ops) {
         const long nb = std::max<long>(op->nblocks, 1);
         MWG_CUDA(cudaMalloc(&op->d_blocks32, sizeof(float) * 2 * (size_t)nb * bsz));
-        if (tc) MWG_CUDA(cudaMalloc(&op->d_blocks_tc, sizeof(float) * tc5_b_floats(K) * (size_t)nb));
+        if (tc) MWG_CUDA(cudaMalloc(&op->d_blocks_tc, sizeof(float) * tc5_b_stride(K) * (size_t)nb));
         k_op_convert(op->d_blocks, op->d_blocks32, tc ? op->d_blocks_tc : nullptr, nb, K, tc5_n(K), 2 * tc5_ks(K),
                      st);
     }

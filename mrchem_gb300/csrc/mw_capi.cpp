@@ -27,20 +27,23 @@ thread_local std::string g_noctx_err;
 
 template <typename F>
 int guard(mwg::Ctx *ctx, F &&f) {
+    int rc = MW_OK;
     try {
         if (ctx) MWG_CUDA(cudaSetDevice(ctx->device));
         f();
-        return MW_OK;
     } catch (const mwg::Error &e) {
         (ctx ? ctx->err : g_noctx_err) = e.what();
-        return e.code;
+        rc = e.code;
     } catch (const std::bad_alloc &) {
         (ctx ? ctx->err : g_noctx_err) = "host allocation failed";
-        return MW_ERR_OOM;
+        rc = MW_ERR_OOM;
     } catch (const std::exception &e) {
         (ctx ? ctx->err : g_noctx_err) = e.what();
-        return MW_ERR_STATE;
+        rc = MW_ERR_STATE;
     }
+    // device arrays that trees outgrew during the call, released once the call's work is done
+    if (ctx) ctx->release_retired();
+    return rc;
 }
 
 mwg::Ctx *ctx_of(mw_tree t) { return t ? t->tree.ctx : nullptr; }
@@ -98,6 +101,12 @@ int mw_ctx_create(int device, int root_scale, const int corner[3], const int box
         c->ctx.dbasis = mwg::DevBasis{K, basis, d, d + K2 * K2, d + 2 * K2 * K2, d + 2 * K2 * K2 + K * K,
                                       d + 2 * K2 * K2 + 2 * K * K, d + 2 * K2 * K2 + 2 * K * K + K,
                                       d + 2 * K2 * K2 + 2 * K * K + 2 * K};
+        // tree growth allocates from the device's stream-ordered pool (Tree::reserve); the pool keeps
+        // what is returned to it instead of handing it back to the driver at every synchronisation
+        cudaMemPool_t pool = nullptr;
+        MWG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+        uint64_t keep = UINT64_MAX;
+        MWG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
         // mw_dot_noalloc's fixed device array: its address is taken here, with the device current,
         // so that its module is loaded (and the array reserved) while the caller may still allocate
         mwg::noalloc_setup(device);
@@ -117,6 +126,7 @@ int mw_ctx_create(int device, int root_scale, const int corner[3], const int box
 // alive, so handles may be destroyed in any order (e.g. by a garbage collector).
 static void ctx_free(mw_ctx c) {
     cudaSetDevice(c->ctx.device);
+    c->ctx.release_retired();
     cudaStreamSynchronize(c->ctx.stream);
     for (auto &xs : c->ctx.xstream)
         if (xs) cudaStreamSynchronize(xs);

@@ -208,6 +208,11 @@ struct Ctx {
     size_t pinned_bytes = 0;
     void *pinned(size_t bytes);
     void sync();
+    // Device buffers a tree outgrew during the current call (Tree::reserve).  Kernels queued
+    // earlier, on any of the context's streams, may still read them, so they are released only
+    // when the call has ended and every stream of the context is idle (release_retired).
+    std::vector<void *> retired;
+    void release_retired();
 };
 
 // Packs host arrays into the context's pinned buffer and ships them to the
@@ -304,7 +309,10 @@ inline size_t generate_scratch_doubles(int K) {
 void k_apply(const DevBasis &b, const ApplyLaunch &L, int fp32, int nsm, cudaStream_t s);
 // TF32 tensor-core tier on the 5th-generation tensor cores (tcgen05.mma, accumulators in tensor
 // memory); items point at the operand layouts of mw_tc05_layout.h
-void k_apply_tc05(const DevBasis &b, const ApplyLaunch &L, cudaStream_t s);
+// split = false: the TF32 tier; split = true: the split-TF32 tier (hi * hi + hi * lo + lo * hi of
+// the TF32-rounded operands and their remainders, FP32 accumulation), the tensor-core form of the
+// FP32 tier.  Item pointers point at the hi copies of mw_tc05_layout.h's operand layouts.
+void k_apply_tc05(const DevBasis &b, const ApplyLaunch &L, bool split, cudaStream_t s);
 // FP32 cube-order shadows (high cube read) -> the tensor-core tier's x-pass operand layout
 void k_to_tc_x(const float *cube32, float *out, size_t nblocks, int K, cudaStream_t s);
 // round to TF32: nearest, ties away from zero (as cvt.rna.tf32.f32)
@@ -324,7 +332,8 @@ void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int
 // the same two passes with double-FP32 arithmetic on the FP32 pipe (mw_post_df.cu); FP64 blocks and norms
 void k_topdown_df(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s);
 void k_compress_df(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s);
-void k_multiply(const DevBasis &b, const MulTask *tasks, int n, cudaStream_t s);
+// the multiply's node kernel (mw_multiply_df.cu): double-FP32 transforms, FP64 blocks in and out
+void k_multiply_df(const DevBasis &b, const MulTask *tasks, int n, int nsm, cudaStream_t s);
 void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
            cudaStream_t s);
 void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);

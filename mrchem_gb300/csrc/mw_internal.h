@@ -110,7 +110,8 @@ double dot_noalloc(const Tree &a, const Tree &b);
 void noalloc_setup(int device);
 void tree_save(Tree &t, const char *path);
 void tree_load(Tree &t, const char *path);
-void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st);
+// bottom-up compression of several trees, one launch per scale; df: double-FP32 transforms
+void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st, bool df = false);
 void add(Tree &out, const std::vector<const Tree *> &trees, const std::vector<double> &coefs, mw_stats &st);
 
 }  // namespace mwg

@@ -660,28 +660,6 @@ __global__ void compress_kernel(DevBasis b, const PairTask *tasks, double *const
     }
 }
 
-__global__ void multiply_kernel(DevBasis b, const MulTask *tasks, int n) {
-    extern __shared__ double sm[];
-    int K = b.K, N2 = 2 * K, C = N2 * N2 * N2;
-    double *ca = sm, *cb = sm + C, *tmp = sm + 2 * C, *red = sm + 3 * C;
-    for (int t = blockIdx.x; t < n; t += gridDim.x) {
-        MulTask task = tasks[t];
-        load_block(ca, task.a, K);
-        load_block(cb, task.b, K);
-        cube_transform(ca, tmp, b.WT, K);
-        cube_map_halves(ca, tmp, b.c2v, K);
-        cube_transform(cb, tmp, b.WT, K);
-        cube_map_halves(cb, tmp, b.c2v, K);
-        for (int i = threadIdx.x; i < C; i += blockDim.x) ca[i] = ca[i] * cb[i] * task.scale;
-        __syncthreads();
-        cube_map_halves(ca, tmp, b.v2c, K);
-        cube_transform(ca, tmp, b.W, K);
-        store_block(task.out, ca, K);
-        __syncthreads();
-        block_norms(task.out, task.cn, K, red);
-    }
-}
-
 __global__ void add_kernel(DevBasis b, const AddTask *tasks, const double *const *src, const double *coefs, int n,
                            int bs) {
     extern __shared__ double sm[];
@@ -827,14 +805,6 @@ void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int
     size_t smem = 2 * cube_bytes(b.K) + 8 * 256 * sizeof(double);
     MWG_CUDA(cudaFuncSetAttribute(compress_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     compress_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, cn, n);
-    MWG_CUDA(cudaGetLastError());
-}
-
-void k_multiply(const DevBasis &b, const MulTask *tasks, int n, cudaStream_t s) {
-    if (n <= 0) return;
-    size_t smem = 3 * cube_bytes(b.K) + 8 * 256 * sizeof(double);
-    MWG_CUDA(cudaFuncSetAttribute(multiply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    multiply_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, n);
     MWG_CUDA(cudaGetLastError());
 }
 

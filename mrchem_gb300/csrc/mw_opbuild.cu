@@ -213,6 +213,13 @@ __global__ void __launch_bounds__(OB_THREADS) op_block_kernel(int K, const doubl
 }
 
 // FP32 high and low parts of every block, and the tensor-core tier's B operand (mw_tc05_layout.h)
+// round to TF32: nearest, ties away from zero (infinities and NaNs unchanged)
+__device__ __forceinline__ float tf32_round(float v) {
+    uint32_t u = __float_as_uint(v);
+    if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & ~0x1fffu;
+    return __uint_as_float(u);
+}
+
 __global__ void op_convert_kernel(const double *blocks, float *b32, float *btc, long nblocks, int K, int NB,
                                   int groups) {
     const int N2 = 2 * K, bsz = N2 * N2;
@@ -226,21 +233,22 @@ __global__ void op_convert_kernel(const double *blocks, float *b32, float *btc, 
         b32[2 * blk * bsz + bsz + r] = __double2float_rn(d - (double)h);
     }
     if (!btc) return;
+    // per block: the B operand rounded to TF32 (hi), then the remainder rounded to TF32 (lo)
     const size_t per = (size_t)groups * NB * 4, ttot = (size_t)nblocks * per;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < ttot; i += (size_t)gridDim.x * blockDim.x) {
         const size_t blk = i / per;
         const int rem = (int)(i - blk * per), g = rem / (NB * 4), n = (rem / 4) % NB, c = rem % 4, k = 4 * g + c;
-        float v = 0.0f;
+        double d = 0.0;
         if (k < N2) {
             const size_t base = blk * bsz;
             if (n < N2)
-                v = __double2float_rn(blocks[base + (size_t)n * N2 + k]);
+                d = blocks[base + (size_t)n * N2 + k];
             else if (n < N2 + K && k >= K)
-                v = __double2float_rn(blocks[base + (size_t)(n - N2) * N2 + k]);
+                d = blocks[base + (size_t)(n - N2) * N2 + k];
         }
-        uint32_t u = __float_as_uint(v);  // round to TF32: nearest, ties away from zero
-        if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & ~0x1fffu;
-        btc[i] = __uint_as_float(u);
+        const float h = tf32_round(__double2float_rn(d));
+        btc[2 * blk * per + rem] = h;
+        btc[2 * blk * per + per + rem] = tf32_round(__double2float_rn(d - (double)h));
     }
 }
 

@@ -627,7 +627,8 @@ __global__ void __launch_bounds__(ST) fill_kernel(ScreenLevel P) {
                 P.ax[dst] = op.b64 + bx * P.bsz;
                 P.ay[dst] = op.b64 + by * P.bsz;
                 P.az[dst] = op.b64 + bz * P.bsz;
-            } else if (tier == 2) {
+            } else if (tier == 2 || (tier == 1 && P.tensor)) {
+                // the tensor-core tiers (TF32, and split-TF32 for tier 1 in the tensor modes)
                 P.in[dst] = cd.gen ? (const void *)(P.gtc + P.tx * src) : (const void *)(J.intc + P.tx * src);
                 P.ax[dst] = op.btc + P.tb * bx;
                 P.ay[dst] = op.btc + P.tb * by;

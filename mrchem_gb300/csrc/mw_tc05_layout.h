@@ -12,6 +12,11 @@
 //                                  rows 2K .. 3K-1 repeat rows 0 .. K-1 with the columns k < K
 //                                  zeroed (the wavelet-in-x part the x pass needs); 2 KS groups
 //                                  of N rows, the groups and rows past the data zero
+//
+// Every block is stored twice in a row: the value rounded to TF32 (hi), then the rounded
+// remainder, value - hi, rounded to TF32 (lo).  The TF32 tier reads hi only; the split-TF32 tier
+// (hi * hi + hi * lo + lo * hi on the tensor cores, the FP32-accuracy tier) reads both, lo at a
+// fixed offset from hi.  Blocks are tc5_x_stride / tc5_b_stride floats apart.
 #pragma once
 
 #include <cstddef>
@@ -29,5 +34,8 @@ MWG_HD constexpr int tc5_kg(int K) { return (2 * K + 3) / 4; }          // k-gro
 MWG_HD constexpr int tc5_ks(int K) { return (tc5_kg(K) + 1) / 2; }      // MMA k-steps of 8
 MWG_HD constexpr size_t tc5_x_floats(int K) { return (size_t)tc5_kg(K) * 4 * (size_t)(2 * K) * (size_t)(2 * K); }
 MWG_HD constexpr size_t tc5_b_floats(int K) { return (size_t)2 * tc5_ks(K) * tc5_n(K) * 4; }
+// per-block strides of the stored layouts: hi, then lo
+MWG_HD constexpr size_t tc5_x_stride(int K) { return 2 * tc5_x_floats(K); }
+MWG_HD constexpr size_t tc5_b_stride(int K) { return 2 * tc5_b_floats(K); }
 
 }  // namespace mwg

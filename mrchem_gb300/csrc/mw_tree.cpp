@@ -105,6 +105,16 @@ void *Ctx::pinned(size_t bytes) {
 
 void Ctx::sync() { MWG_CUDA(cudaStreamSynchronize(stream)); }
 
+void Ctx::release_retired() {
+    if (retired.empty()) return;
+    cudaStreamSynchronize(stream);
+    for (auto &xs : xstream)
+        if (xs) cudaStreamSynchronize(xs);
+    if (fast) cudaStreamSynchronize(fast);
+    for (void *p : retired) cudaFreeAsync(p, stream);  // back to the pool, which keeps it for reuse
+    retired.clear();
+}
+
 // Packs several host arrays into one pinned buffer and ships them with one copy.
 void *Packer::add(const void *src, size_t bytes) {
     size_t o = (size.size() ? offs.back() + size.back() : 0);
@@ -143,21 +153,25 @@ void Packer::ship(Ctx &ctx, Arena &arena) {
 // ------------------------------------------------------------------ tree
 double *Tree::block(int i) const { return d_coefs + (size_t)i * ctx->basis.bs; }
 
+// Grows the device arrays geometrically.  The new arrays come from the device's stream-ordered
+// pool on the context's current stream, which also copies the old contents, so a growth neither
+// waits for the GPU nor synchronises the device (as cudaMalloc / cudaFree may): the refinement of
+// hundreds of trees per call (the exchange pair products) grows each a few times.  The old arrays
+// are retired, not freed: kernels queued before the growth may still read them.
 void Tree::reserve(size_t n) {
     if (n <= cap) return;
     size_t nc = std::max(n, std::max(cap * 2, (size_t)64));
     int bs = ctx->basis.bs;
     double *nd = nullptr, *ncn = nullptr;
-    MWG_CUDA(cudaMalloc(&nd, sizeof(double) * bs * nc));
-    MWG_CUDA(cudaMalloc(&ncn, sizeof(double) * 8 * nc));
+    MWG_CUDA(cudaMallocAsync(&nd, sizeof(double) * bs * nc, ctx->stream));
+    MWG_CUDA(cudaMallocAsync(&ncn, sizeof(double) * 8 * nc, ctx->stream));
     if (d_coefs) {
         MWG_CUDA(cudaMemcpyAsync(nd, d_coefs, sizeof(double) * bs * nodes.size(), cudaMemcpyDeviceToDevice,
                                  ctx->stream));
         MWG_CUDA(cudaMemcpyAsync(ncn, d_cn, sizeof(double) * 8 * nodes.size(), cudaMemcpyDeviceToDevice,
                                  ctx->stream));
-        ctx->sync();
-        cudaFree(d_coefs);
-        cudaFree(d_cn);
+        ctx->retired.push_back(d_coefs);
+        ctx->retired.push_back(d_cn);
     }
     d_coefs = nd;
     d_cn = ncn;

@@ -130,7 +130,9 @@ def test_job_group_count_bit_identical(engine):
 
 def test_autotune_batch(engine):
     # the autotuner keeps one of its candidates, and the tuned apply agrees with the default one far
-    # below the requested (absolute) precision: chunk sizes change only the order of the sums
+    # below the requested (absolute) precision: chunk sizes change only the order of the sums.  The
+    # FP32-accuracy tier accumulates in FP32 on the tensor cores, items up to 2e6 x the screening
+    # threshold: regrouping them moves the sum by a few 1e-3 of prec (5.4e-3 measured)
     prec = 1e-5
     mra = engine.MultiResolutionAnalysis(9)
     rng = np.random.default_rng(13)
@@ -153,7 +155,7 @@ def test_autotune_batch(engine):
         for x in (a, b):
             d = engine.FunctionTree(mra)
             engine.add(-1.0, d, [(1.0, x), (-1.0, r)])
-            assert d.norm() <= 1e-3 * prec
+            assert d.norm() <= 2e-2 * prec
     mra.set_overlap(False)
     with pytest.raises(engine.MWError):
         engine.autotune_batch([prec] * 5, outs, ops, phis, abs_prec=True, precision="mixed", repeats=1)
