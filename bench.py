@@ -30,9 +30,11 @@ import numpy as np  # noqa: E402
 
 SEED = 20261203
 ORDER, PREC = 9, 1e-6
-# DRAM bytes (read + write) per item of each tier kernel on the benchmark step (k=9), from the ncu
-# launch capture summarised in profiles/dram_traffic_tiers_k10.md; re-captured when a tier changes
-DRAM_PER_ITEM = {"fp32": 2.79e3, "tf32": 1.36e3, "df32": 10.1e3}
+# DRAM bytes (read + write) per item of each tier kernel in the mixed step (k=9): ncu capture of every
+# tier launch of two mixed steps of the first 8 orbitals of the batch with the caches left warm
+# (--cache-control none), divided by those launches' items; summarised with its command in
+# profiles/dram_traffic_tiers_k10.md and re-captured whenever a tier kernel changes
+DRAM_PER_ITEM = {"fp32": 2.45e3, "tf32": 0.43e3, "df32": 4.58e3}
 NORB = 16
 METRIC = "Helmholtz-apply nodes/s: batched mixed vs plain FP64 GPU at 1e-6 rel. error"
 
@@ -609,9 +611,6 @@ def run(args):
     tc_mmas = (-(-4 * K * K // 128) + 2 * -(-5 * K * K // 128)) * ks
     tc_issued_item = tc_mmas * 2.0 * 128 * (32 if 3 * K > 16 else 16) * 8
 
-    # DRAM bytes (read + write) per item of each tier kernel: ncu capture of the benchmark step
-    # itself (all launches of one mixed step, metrics dram__bytes_read.sum and dram__bytes_write.sum;
-    # profiles/dram_traffic_tiers_k10.md), divided by that step's items of the tier
     dram_per_item = DRAM_PER_ITEM
     tier_items = {"fp64": st_ser["items_fp64"], "fp32": st_ser["items_fp32"], "tf32": st_ser["items_tf32"],
                   "df32": st_ser["items_df"]}
@@ -644,8 +643,11 @@ def run(args):
                "MEASURED_PEAKS.json holds no TF32 figure")
     roofs = {
         "fp64": roof("fp64", st_ser["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
-        "fp32": roof("fp32", st_ser["kernel_ms_fp32"], fp32_tf, "apply32_kernel<10>", "fp32-pipe", fma_src),
-        "tf32": roof("tf32", st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc05_kernel<10>", "tensor", mma_src,
+        # the FP32-accuracy tier of the mixed step runs on the tensor cores as split TF32: three
+        # MMAs (hi*hi, hi*lo, lo*hi) per tile and k-step, 3 x the TF32 tier's issued work
+        "fp32": roof("fp32", st_ser["kernel_ms_fp32"], tf32_tf, "apply_tc05_kernel<10,1> (split TF32)", "tensor",
+                     mma_src, issued_item=3 * tc_issued_item),
+        "tf32": roof("tf32", st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc05_kernel<10,0>", "tensor", mma_src,
                      issued_item=tc_issued_item),
         # a double-FP32 multiply-add costs about 12 FP32 instructions in this kernel: its ceiling is the
         # FP32 FMA rate / 12 (multiply-adds), i.e. peak flops = FP32 FMA flops / 12
@@ -653,9 +655,9 @@ def run(args):
                      "fp32-pipe (double-FP32)", fma_src + "; divided by 12 FP32 instructions per double-FP32 "
                      "multiply-add"),
     }
-    roofs["tf32"]["peak_tc05_n32"] = tf32_n32_tf
-    roofs["tf32"]["issued_frac_of_n32_rate"] = (roofs["tf32"]["issued_achieved"] / tf32_n32_tf
-                                                if tf32_n32_tf else None)
+    for t in ("tf32", "fp32"):
+        roofs[t]["peak_tc05_n32"] = tf32_n32_tf
+        roofs[t]["issued_frac_of_n32_rate"] = (roofs[t]["issued_achieved"] / tf32_n32_tf if tf32_n32_tf else None)
     roofs["tf32"]["peak_mma_sync_tf32"] = tf32_sync_tf
     dominant = max(roofs, key=lambda k: roofs[k]["kernel_ms_per_step"])
     line = {
