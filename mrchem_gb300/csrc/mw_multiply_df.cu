@@ -15,12 +15,15 @@
 // Arithmetic: every value is an unevaluated FP32 pair (hi + lo) and every multiply-add is the
 // error-free double-FP32 update of the apply's double-FP32 tier, as in the post-processing
 // transforms (mw_post_df.cu): about (2K + 4) 2^-48 of sum |M| |x| per pass, 1e-14 relative, at
-// about 8x GB300's FP64 rate.  Blocks in global memory stay FP64; norms are summed in FP64.
+// about 8x GB300's FP64 rate.  Blocks in global memory stay FP64; norms are summed in FP64.  The
+// FP64 blocks are split into FP32 pairs and joined back with integer operations (mw_dfconv.cuh),
+// which keeps the conversions off GB300's slow FP64 pipe.
 //
 // Layout: one CTA per node, one thread per line of the cube, the two cubes in shared memory
 // (rows padded to 2K + 1 pairs, conflict-free row stores).  The x pass of each input reads its
 // row straight from the FP64 block; the product is formed in b's z pass by the thread that owns
 // the same line of a's cube; the last (z) pass of the backward transform writes the FP64 block.
+#include "mw_dfconv.cuh"
 #include "mw_host.h"
 
 namespace mwg {
@@ -146,7 +149,7 @@ __global__ void __launch_bounds__(MulGeo<K>::THREADS) multiply_df_kernel(DevBasi
                 const int cyz = (p >= K ? 2 : 0) | (q >= K ? 4 : 0);
                 const int r = (q % K) * K * K + (p % K) * K;
 #pragma unroll
-                for (int X = 0; X < N2; X++) mdf_split(g[(size_t)(cyz | (X >= K ? 1 : 0)) * K3 + r + X % K], vh[X], vl[X]);
+                for (int X = 0; X < N2; X++) df_split(g[(size_t)(cyz | (X >= K ? 1 : 0)) * K3 + r + X % K], vh[X], vl[X]);
             } else {
 #pragma unroll
                 for (int i = 0; i < N2; i++) {
@@ -165,7 +168,7 @@ __global__ void __launch_bounds__(MulGeo<K>::THREADS) multiply_df_kernel(DevBasi
                     s_a[base + j * stride] = mdf_mul(as.x, as.y, h, l);
                 } else if (pass == 8) {
                     const int c = cxy | (j >= K ? 4 : 0);
-                    const double v = (double)h + (double)l;
+                    const double v = df_widen(h) + df_widen(l);
                     task.out[(size_t)c * K3 + (size_t)(j % K) * K * K + r8] = v;
                     if (j < K)
                         s0 = fma(v, v, s0);

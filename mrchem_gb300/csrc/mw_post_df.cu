@@ -13,7 +13,8 @@
 // error-free double-FP32 update of the double-FP32 apply tier, so a pass is
 // accurate to about (2K + 4) 2^-48 of sum |W| |x| -- 1e-14 relative, far below
 // any precision an apply is asked for -- at ~8x the FP64 rate.  The blocks in
-// global memory stay FP64; the norms are summed in FP64.
+// global memory stay FP64; the norms are summed in FP64.  The FP64 values are split into FP32
+// pairs with integer operations (mw_dfconv.cuh), off GB300's slow FP64 pipe.
 //
 // One CTA per node, one thread per line of the cube: the x pass reads its row
 // straight from the FP64 block(s) in global memory into registers and writes
@@ -21,6 +22,7 @@
 // registers and write it back (y) or out to global memory (z).  The shared cube
 // rows are padded to 2K + 1 pairs, which makes the row-wise x-pass stores free
 // of bank conflicts.
+#include "mw_dfconv.cuh"
 #include "mw_host.h"
 
 namespace mwg {
@@ -106,78 +108,73 @@ __global__ void __launch_bounds__(PostGeo<K>::THREADS, 1)
 
     for (int t = blockIdx.x; t < n; t += gridDim.x) {
         const PairTask task = tasks[t];
-        __syncthreads();  // M^T ready; the previous node's cube and partials are no longer read
-        float vh[N2], vl[N2];
-        if (active) {  // x pass: thread (Y = a, Z = bq) holds row X = 0 .. 2K-1
-            const int Y = a, Z = bq;
-            const int cyz = (Y >= K ? 2 : 0) | (Z >= K ? 4 : 0);
-            const int r = (Z % K) * K * K + (Y % K) * K;
+        double s0 = 0.0, s1 = 0.0;  // MODE 1, z pass: this line's squared norms (Z < K, Z >= K)
+        // The three passes run through one instance of the line transform (an instance per pass
+        // overflowed the instruction cache): x reads the thread's row from the FP64 block(s), y and
+        // z read a line of the shared cube; every pass writes back into the cube, except the
+        // compression's z pass, which writes the parent's FP64 block.  Thread mapping: x (Y, Z) =
+        // (a, bq), y (X, Z) = (a, bq), z (X, Y) = (a, bq).
+#pragma unroll 1
+        for (int dim = 0; dim < 3; dim++) {
+            __syncthreads();  // x: M^T ready, the previous node's cube and partials no longer read;
+                              // y, z: the previous pass's stores are visible
+            if (!active) continue;
+            const int base = dim == 0 ? (bq * N2 + a) * RS : (dim == 1 ? bq * N2 * RS + a : a + bq * RS);
+            const int stride = dim == 0 ? 1 : (dim == 1 ? RS : N2 * RS);
+            float vh[N2], vl[N2];
+            if (dim == 0) {
+                const int cyz = (a >= K ? 2 : 0) | (bq >= K ? 4 : 0);
+                const int r = (bq % K) * K * K + (a % K) * K;
 #pragma unroll
-            for (int X = 0; X < N2; X++) {
-                const int c = cyz | (X >= K ? 1 : 0);
-                const double d = MODE == 0 ? task.parent[(size_t)c * K3 + r + X % K]
-                                           : task.child0[(size_t)c * 8 * K3 + r + X % K];
-                pdf_split(d, vh[X], vl[X]);
-            }
-            float2 *row = s_cube + (size_t)(Z * N2 + Y) * RS;
-            pdf_line<K>(vh, vl, s_mth, s_mtl, [&](int X, float h, float l) { row[X] = make_float2(h, l); });
-        }
-        __syncthreads();
-        if (active) {  // y pass: thread (X = a, Z = bq) holds column Y = 0 .. 2K-1
-            const int X = a, Z = bq;
-            float2 *col = s_cube + (size_t)Z * N2 * RS + X;
-#pragma unroll
-            for (int Y = 0; Y < N2; Y++) {
-                const float2 v = col[Y * RS];
-                vh[Y] = v.x;
-                vl[Y] = v.y;
-            }
-            // the whole column is in registers before the first store
-            pdf_line<K>(vh, vl, s_mth, s_mtl, [&](int Y, float h, float l) { col[Y * RS] = make_float2(h, l); });
-        }
-        __syncthreads();
-        if (active) {  // z pass: thread (X = a, Y = bq) holds line Z = 0 .. 2K-1
-            const int X = a, Y = bq;
-            const float2 *col = s_cube + (size_t)Y * RS + X;
-#pragma unroll
-            for (int Z = 0; Z < N2; Z++) {
-                const float2 v = col[(size_t)Z * N2 * RS];
-                vh[Z] = v.x;
-                vl[Z] = v.y;
-            }
-            if (MODE == 0) {  // back into the cube; the children are updated below, coalesced
-                pdf_line<K>(vh, vl, s_mth, s_mtl,
-                            [&](int Z, float h, float l) { s_cube[(size_t)Z * N2 * RS + Y * RS + X] = make_float2(h, l); });
+                for (int X = 0; X < N2; X++) {
+                    const int c = cyz | (X >= K ? 1 : 0);
+                    const double d = MODE == 0 ? task.parent[(size_t)c * K3 + r + X % K]
+                                               : task.child0[(size_t)c * 8 * K3 + r + X % K];
+                    df_split(d, vh[X], vl[X]);
+                }
             } else {
-                const int cxy = (X >= K ? 1 : 0) | (Y >= K ? 2 : 0);
-                const int r = (Y % K) * K + X % K;
-                double s0 = 0.0, s1 = 0.0;
-                pdf_line<K>(vh, vl, s_mth, s_mtl, [&](int Z, float h, float l) {
-                    const int c = cxy | (Z >= K ? 4 : 0);
+                // the whole line is in registers before the first store
+#pragma unroll
+                for (int i = 0; i < N2; i++) {
+                    const float2 v = s_cube[base + i * stride];
+                    vh[i] = v.x;
+                    vl[i] = v.y;
+                }
+            }
+            const bool to_parent = MODE == 1 && dim == 2;
+            const int cxy = (a >= K ? 1 : 0) | (bq >= K ? 2 : 0);  // z pass: (X, Y) = (a, bq)
+            const int r2 = (bq % K) * K + a % K;
+            pdf_line<K>(vh, vl, s_mth, s_mtl, [&](int j, float h, float l) {
+                if (to_parent) {
+                    const int c = cxy | (j >= K ? 4 : 0);
+                    // CUDA conversions here: the integer join made this pass spill at K = 9, 10
                     const double v = (double)h + (double)l;
-                    task.parent[(size_t)c * K3 + (size_t)(Z % K) * K * K + r] = v;
-                    if (Z < K)
+                    task.parent[(size_t)c * K3 + (size_t)(j % K) * K * K + r2] = v;
+                    if (j < K)
                         s0 = fma(v, v, s0);
                     else
                         s1 = fma(v, v, s1);
-                });
-                s_red[cxy * K * K + r] = s0;
-                s_red[(cxy | 4) * K * K + r] = s1;
+                } else {
+                    s_cube[base + j * stride] = make_float2(h, l);
+                }
+            });
+            if (to_parent) {
+                s_red[cxy * K * K + r2] = s0;
+                s_red[(cxy | 4) * K * K + r2] = s1;
             }
         }
+        __syncthreads();
         if (MODE == 0) {
-            __syncthreads();
             // child c's scaling part += octant c of the cube
             for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
                 const int c = gi / K3, r = gi - c * K3;
                 const int ix = r % K, iy = (r / K) % K, iz = r / (K * K);
                 const int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
                 const float2 v = s_cube[(size_t)(Z * N2 + Y) * RS + X];
-                task.child0[(size_t)c * 8 * K3 + r] += (double)v.x + (double)v.y;
+                task.child0[(size_t)c * 8 * K3 + r] += df_widen(v.x) + df_widen(v.y);
             }
         }
         if (MODE == 1) {
-            __syncthreads();
             // component c summed by one warp: lane-strided, then a fixed butterfly (deterministic)
             const int warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
             for (int c = warp; c < 8; c += nw) {
