@@ -17,10 +17,13 @@
 // this tier the items with 2e6 < b / tau <= 1e11.
 //
 // Inputs: FP32 shadows in cube order, hi cube followed by lo cube; operator
-// blocks hi followed by lo.  Layout per CTA (one output node at a time, one
-// thread per output column (Y', X')): the input cube, T1 and the node
-// accumulator as (hi, lo) float2 in shared memory, the operator rows of the
-// x and y passes in registers.
+// blocks hi followed by lo.  Layout per CTA (one output node or chunk at a
+// time, one thread per output column (Y', X')): the node accumulator in the
+// thread's registers, one half (in Z) of the input cube, T1 and u as (hi, lo)
+// float2 in shared memory, the y and z passes fused so that T2 is never
+// stored.  113.6 KB of shared memory and at most 112 registers a thread at
+// K = 10, so that a CTA of this tier (FP32 pipe) and one of the TF32 tier
+// (tensor pipe) can run on the same SM.
 #include "mw_chunks.cuh"
 #include "mw_host.h"
 
@@ -56,27 +59,44 @@ __device__ __forceinline__ float2 df_norm(float h, float l) {
     return make_float2(t, __fsub_rn(l, __fsub_rn(t, h)));
 }
 
-template <int K>
-struct DfGeo {
-    static constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K;
-    static constexpr int THREADS = ((NC + 31) / 32) * 32;
-    // float2 units: IN (later T2), T1, ACC (C each), U and T2X (K^3 each); then floats: A hi (3 NC),
-    // A lo (3 NC)
-    static constexpr size_t SMEM = sizeof(float2) * (3 * (size_t)C + 2 * K3) + sizeof(float) * 6 * (size_t)NC;
-};
+// (ah + al) * (bh + bl) as a renormalised pair
+__device__ __forceinline__ float2 df_mul(float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    return df_norm(p, e);
+}
+
+// Registers a thread may hold: with 416 threads at this cap, a CTA of this kernel and one CTA of
+// the TF32 tier (288 threads x 64 registers) fit in an SM's 64K registers together.
+constexpr int DF_MAXREG = 112;
 
 template <int K>
-__global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLaunch L) {
+struct DfGeo {
+    static constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K, HALF = K * NC;
+    static constexpr int THREADS = ((NC + 31) / 32) * 32;
+    // float2 units: IN (one half in Z: K x N2 x N2), T1 (C), U (K^3); then floats: A_x, A_y and
+    // c A_z, high parts (3 NC), then low parts (3 NC).  113.6 KB at K = 10: a CTA of this kernel
+    // and one of the TF32 tier (98.7 KB) share an SM.
+    static constexpr size_t SMEM = sizeof(float2) * ((size_t)HALF + C + K3) + sizeof(float) * 6 * (size_t)NC;
+    static_assert(SMEM <= 127 * 1024, "shares an SM with a TF32-tier CTA");
+};
+
+// One CTA per task (output node or chunk), thread (Y', X') owns the output column (Y', X', Z' =
+// 0 .. 2K-1): its node accumulator stays in registers for all of the task's items.  Per item:
+//   x pass, in two halves of Z (the input cube is staged half by half): T1[Z][Y][X'] and u;
+//   y and z passes fused: for each Z the thread forms T2[Z][Y'][X'] (and t2x for Z < K) and adds
+//   c A_z[Z'][Z] T2 to its 2K accumulators at once, so T2 is never stored.
+template <int K>
+__global__ void __maxnreg__(DF_MAXREG) apply_df_kernel(ApplyLaunch L) {
     using G = DfGeo<K>;
-    constexpr int N2 = G::N2, NC = G::NC, C = G::C, K3 = G::K3;
+    constexpr int N2 = G::N2, NC = G::NC, C = G::C, K3 = G::K3, HALF = G::HALF;
     extern __shared__ __align__(16) float2 smem_df[];
-    float2 *s_in = smem_df;        // IN[Z][Y][X]
-    float2 *s_t1 = s_in + C;       // T1[Z][Y][X']
-    float2 *s_acc = s_t1 + C;      // node accumulator acc[Z'][Y'][X']
-    float2 *s_u = s_acc + C;       // u[Z][Y][X'], Z, Y, X' < K
-    float2 *s_t2 = s_in;           // T2[Z][Y'][X'] (the input is dead after the x pass)
-    float2 *s_t2x = s_u + K3;      // t2x[Z][Y'][X'], Z, Y', X' < K
-    float *s_Ah = reinterpret_cast<float *>(s_t2x + K3);  // A_x, A_y, A_z high parts
+    float2 *s_in = smem_df;        // IN[z][Y][X] of the current half (Z = h K + z)
+    float2 *s_t1 = s_in + HALF;    // T1[Z][Y][X']
+    float2 *s_u = s_t1 + C;        // u[Z][Y][X'], Z, Y, X' < K
+    float *s_Ah = reinterpret_cast<float *>(s_u + K3);  // A_x, A_y, c A_z high parts
     float *s_Al = s_Ah + 3 * NC;                        // low parts
     __shared__ int s_node, s_redf;
     const int tid = threadIdx.x;
@@ -89,71 +109,79 @@ __global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLau
         __syncthreads();
         const int w = s_node;
         if (w >= L.nnodes) break;
-        for (int i = tid; i < C; i += blockDim.x) s_acc[i] = make_float2(0.0f, 0.0f);
+        float acc_h[N2], acc_l[N2];  // acc[Z'] of the thread's column (Y', X')
+#pragma unroll
+        for (int z = 0; z < N2; z++) acc_h[z] = acc_l[z] = 0.0f;
         const long long b0 = L.begin[w], b1 = L.end[w];
         for (long long j = b0; j < b1; j++) {
-            __syncthreads();
-            {
-                // hi and lo cubes -> interleaved (hi, lo) pairs
-                const float4 *gh = reinterpret_cast<const float4 *>(L.in[j]);
-                const float4 *gl = gh + C / 4;
-                float4 *s4 = reinterpret_cast<float4 *>(s_in);
-                for (int i = tid; i < C / 4; i += blockDim.x) {
-                    const float4 h = __ldg(gh + i), l = __ldg(gl + i);
-                    s4[2 * i] = make_float4(h.x, l.x, h.y, l.y);
-                    s4[2 * i + 1] = make_float4(h.z, l.z, h.w, l.w);
+#pragma unroll 1
+            for (int h = 0; h < 2; h++) {
+                __syncthreads();  // the previous half's x pass, or the previous item, is done with smem
+                {
+                    // half h of the hi and lo cubes -> interleaved (hi, lo) pairs
+                    const float4 *gh = reinterpret_cast<const float4 *>(L.in[j]) + (size_t)h * (HALF / 4);
+                    const float4 *gl = gh + C / 4;
+                    float4 *s4 = reinterpret_cast<float4 *>(s_in);
+                    for (int i = tid; i < HALF / 4; i += blockDim.x) {
+                        const float4 hv = __ldg(gh + i), lv = __ldg(gl + i);
+                        s4[2 * i] = make_float4(hv.x, lv.x, hv.y, lv.y);
+                        s4[2 * i + 1] = make_float4(hv.z, lv.z, hv.w, lv.w);
+                    }
+                    if (h == 0) {
+                        const float *ax = reinterpret_cast<const float *>(L.ax[j]);
+                        const float *ay = reinterpret_cast<const float *>(L.ay[j]);
+                        const float *az = reinterpret_cast<const float *>(L.az[j]);
+                        const double cfd = L.coef[j];
+                        const float cfh = (float)cfd, cfl = (float)(cfd - (double)cfh);
+                        for (int i = tid; i < 3 * NC; i += blockDim.x) {
+                            const int d = i / NC, r = i - d * NC;
+                            const float *op = d == 0 ? ax : (d == 1 ? ay : az);
+                            float hv = __ldg(op + r), lv = __ldg(op + NC + r);
+                            if (d == 2) {  // c A_z
+                                const float2 m = df_mul(hv, lv, cfh, cfl);
+                                hv = m.x;
+                                lv = m.y;
+                            }
+                            s_Ah[i] = hv;
+                            s_Al[i] = lv;
+                        }
+                    }
                 }
-                const float *ax = reinterpret_cast<const float *>(L.ax[j]);
-                const float *ay = reinterpret_cast<const float *>(L.ay[j]);
-                const float *az = reinterpret_cast<const float *>(L.az[j]);
-                for (int i = tid; i < 3 * NC; i += blockDim.x) {
-                    const int d = i / NC, r = i - d * NC;
-                    const float *op = d == 0 ? ax : (d == 1 ? ay : az);
-                    s_Ah[i] = __ldg(op + r);
-                    s_Al[i] = __ldg(op + NC + r);
-                }
-            }
-            const double cfd = L.coef[j];
-            const float cfh = (float)cfd, cfl = (float)(cfd - (double)cfh);
-            __syncthreads();
-            if (active) {  // x pass, thread (Y = Yp, X' = Xp)
-                float ah[N2], al[N2];
+                __syncthreads();
+                if (active) {  // x pass of this half, thread (Y = Yp, X' = Xp)
+                    float ah[N2], al[N2];
 #pragma unroll
-                for (int X = 0; X < N2; X++) {
-                    ah[X] = s_Ah[Xp * N2 + X];
-                    al[X] = s_Al[Xp * N2 + X];
-                }
+                    for (int X = 0; X < N2; X++) {
+                        ah[X] = s_Ah[Xp * N2 + X];
+                        al[X] = s_Al[Xp * N2 + X];
+                    }
 #pragma unroll 2
-                for (int Z = 0; Z < N2; Z++) {
-                    const float2 *src = s_in + (Z * N2 + Yp) * N2;
-                    float s0h = 0.0f, s0l = 0.0f, s1h = 0.0f, s1l = 0.0f;
+                    for (int z = 0; z < K; z++) {
+                        const float2 *src = s_in + (z * N2 + Yp) * N2;
+                        float s0h = 0.0f, s0l = 0.0f, s1h = 0.0f, s1l = 0.0f;
 #pragma unroll
-                    for (int X = 0; X < K; X++) {
-                        const float2 v = src[X];
-                        df_fma(s0h, s0l, ah[X], al[X], v.x, v.y);
-                    }
+                        for (int X = 0; X < K; X++) {
+                            const float2 v = src[X];
+                            df_fma(s0h, s0l, ah[X], al[X], v.x, v.y);
+                        }
 #pragma unroll
-                    for (int X = K; X < N2; X++) {
-                        const float2 v = src[X];
-                        df_fma(s1h, s1l, ah[X], al[X], v.x, v.y);
+                        for (int X = K; X < N2; X++) {
+                            const float2 v = src[X];
+                            df_fma(s1h, s1l, ah[X], al[X], v.x, v.y);
+                        }
+                        float th = s0h, tl = s0l;
+                        df_add(th, tl, s1h, s1l);
+                        const int Z = h * K + z;
+                        s_t1[(Z * N2 + Yp) * N2 + Xp] = df_norm(th, tl);
+                        if (excl && h == 0) s_u[(z * K + Yp) * K + Xp] = df_norm(s1h, s1l);
                     }
-                    float th = s0h, tl = s0l;
-                    df_add(th, tl, s1h, s1l);
-                    s_t1[(Z * N2 + Yp) * N2 + Xp] = df_norm(th, tl);
-                    if (excl && Z < K) s_u[(Z * K + Yp) * K + Xp] = df_norm(s1h, s1l);
                 }
             }
             __syncthreads();
             if (active) {  // y and z passes, thread (Y' = Yp, X' = Xp)
-                float ayh[N2], ayl[N2];
-#pragma unroll
-                for (int Y = 0; Y < N2; Y++) {
-                    ayh[Y] = s_Ah[NC + Yp * N2 + Y];
-                    ayl[Y] = s_Al[NC + Yp * N2 + Y];
-                }
-                // rolled over Z (a fully unrolled pass overflows the instruction cache): each
-                // thread parks its own T2 column in shared memory and reads it back for the z pass
-#pragma unroll 2
+                const float *ayh = s_Ah + NC + Yp * N2, *ayl = s_Al + NC + Yp * N2;
+                const float *czh = s_Ah + 2 * NC, *czl = s_Al + 2 * NC;  // c A_z[Z'][Z] at Z' N2 + Z
+#pragma unroll 1
                 for (int Z = 0; Z < N2; Z++) {
                     float s0h = 0.0f, s0l = 0.0f, s1h = 0.0f, s1l = 0.0f;
 #pragma unroll
@@ -166,8 +194,9 @@ __global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLau
                         const float2 v = s_t1[(Z * N2 + Y) * N2 + Xp];
                         df_fma(s1h, s1l, ayh[Y], ayl[Y], v.x, v.y);
                     }
+                    // t2x: u replaces T1 for Y < K (the scaling-scaling path in x and y left out)
+                    float2 t2x = make_float2(0.0f, 0.0f);
                     if (Z < K) {
-                        // t2x: u replaces T1 for Y < K (the scaling-scaling path in x and y left out)
                         float xh = 0.0f, xl = 0.0f;
                         if (excl) {
 #pragma unroll
@@ -177,43 +206,32 @@ __global__ void __launch_bounds__(DfGeo<K>::THREADS, 1) apply_df_kernel(ApplyLau
                             }
                         }
                         df_add(xh, xl, s1h, s1l);
-                        if (excl) s_t2x[(Z * K + Yp) * K + Xp] = df_norm(xh, xl);
+                        t2x = df_norm(xh, xl);
                     }
                     df_add(s0h, s0l, s1h, s1l);
-                    s_t2[(Z * N2 + Yp) * N2 + Xp] = df_norm(s0h, s0l);
-                }
-                float2 t2[N2], t2x[K];
+                    const float2 t2 = df_norm(s0h, s0l);
+                    const bool use_x = excl && Z < K;
 #pragma unroll
-                for (int Z = 0; Z < N2; Z++) t2[Z] = s_t2[(Z * N2 + Yp) * N2 + Xp];
-#pragma unroll
-                for (int Z = 0; Z < K; Z++) t2x[Z] = excl ? s_t2x[(Z * K + Yp) * K + Xp] : make_float2(0.0f, 0.0f);
-#pragma unroll 2
-                for (int Zp = 0; Zp < N2; Zp++) {
-                    const float *azh = s_Ah + 2 * NC + Zp * N2, *azl = s_Al + 2 * NC + Zp * N2;
-                    float sh = 0.0f, sl = 0.0f;
-#pragma unroll
-                    for (int Z = 0; Z < N2; Z++) {
-                        float2 v = t2[Z];
-                        if (Zp < K && Z < K && excl) v = t2x[Z < K ? Z : 0];
-                        df_fma(sh, sl, azh[Z], azl[Z], v.x, v.y);
+                    for (int Zp = 0; Zp < N2; Zp++) {
+                        const float2 v = (use_x && Zp < K) ? t2x : t2;
+                        df_fma(acc_h[Zp], acc_l[Zp], czh[Zp * N2 + Z], czl[Zp * N2 + Z], v.x, v.y);
                     }
-                    const float2 sn = df_norm(sh, sl);
-                    float2 &a = s_acc[(Zp * N2 + Yp) * N2 + Xp];
-                    float ah_ = a.x, al_ = a.y;
-                    df_fma(ah_, al_, cfh, cfl, sn.x, sn.y);
-                    a = df_norm(ah_, al_);
+                }
+#pragma unroll
+                for (int Zp = 0; Zp < N2; Zp++) {
+                    const float2 a = df_norm(acc_h[Zp], acc_l[Zp]);
+                    acc_h[Zp] = a.x;
+                    acc_l[Zp] = a.y;
                 }
             }
         }
-        __syncthreads();
         if (active) {
             double *out = L.out[w];
-#pragma unroll 4
+#pragma unroll
             for (int Zp = 0; Zp < N2; Zp++) {
                 const int c = (Xp >= K ? 1 : 0) | (Yp >= K ? 2 : 0) | (Zp >= K ? 4 : 0);
                 const int gi = c * K3 + (Zp % K) * K * K + (Yp % K) * K + (Xp % K);
-                const float2 a = s_acc[(Zp * N2 + Yp) * N2 + Xp];
-                const double v = (double)a.x + (double)a.y;
+                const double v = (double)acc_h[Zp] + (double)acc_l[Zp];
                 if (L.set)
                     out[gi] = v;
                 else
