@@ -372,6 +372,10 @@ def other_configs(mw, device, world, sync, steps):
     out["exchange_528"] = {
         "value": len(pairs) * world / (ms4 / 1e3), "unit": "pairs/s", "ms_per_step": ms4,
         "multiply_ms": mul_ms, "apply_ms": app_ms, "dtype": "df32 multiply + mixed apply",
+        "multiply_host_split_ms": {"requests": sm["host_enum_ms"], "generation": sm["host_gen_ms"],
+                                   "tasks": sm["host_items_ms"], "kernel_and_norms": sm["host_wait_ms"],
+                                   "refinement": sm["host_refine_ms"], "compression": sm["gpu_post_ms"],
+                                   "levels": sm["levels"], "launches": sm["launches"]},
         "nodes_per_s": (sm["out_nodes"] + sa["out_nodes"]) * world / (ms4 / 1e3),
         "input_nodes_total": int(sum(p.nnodes for p in phis)), "product_nodes": int(sum(r.nnodes for r in rhos)),
         "multiply_nodes_computed": sm["out_nodes"], "apply_output_nodes": sa["out_nodes"],

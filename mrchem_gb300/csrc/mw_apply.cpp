@@ -1595,10 +1595,33 @@ void compress_batch(const std::vector<Tree *> &trees, Arena &arena, mw_stats *st
                        ctx.stream);
         if (st) st->launches++;
     }
-    for (Tree *t : trees)
-        MWG_CUDA(cudaMemcpyAsync(t->cn.data(), t->d_cn, sizeof(double) * 8 * t->nn(), cudaMemcpyDeviceToHost,
-                                 ctx.stream));
+    // every tree's norms in one download (gathered on the device into pinned memory)
+    std::vector<const double *> gsrc;
+    std::vector<long long> goff;
+    std::vector<int> glen;
+    long long gtot = 0;
+    for (Tree *t : trees) {
+        gsrc.push_back(t->d_cn);
+        goff.push_back(gtot);
+        glen.push_back(8 * t->nn());
+        gtot += 8LL * t->nn();
+    }
+    double *hnorm = nullptr;
+    if (gtot > 0) {
+        Packer pg;
+        pg.add(gsrc.data(), gsrc.size() * sizeof(const double *));
+        pg.add(goff.data(), goff.size() * sizeof(long long));
+        pg.add(glen.data(), glen.size() * sizeof(int));
+        pg.ship(ctx, arena);
+        double *dnorm = (double *)arena.alloc(sizeof(double) * (size_t)gtot);
+        k_gather_ranges((const double *const *)pg.ptr(0), (const long long *)pg.ptr(1), (const int *)pg.ptr(2),
+                        (int)gsrc.size(), dnorm, ctx.stream);
+        if (st) st->launches++;
+        hnorm = (double *)arena.halloc(sizeof(double) * (size_t)gtot);
+        MWG_CUDA(cudaMemcpyAsync(hnorm, dnorm, sizeof(double) * (size_t)gtot, cudaMemcpyDeviceToHost, ctx.stream));
+    }
     ctx.sync();
+    for (size_t r = 0; r < trees.size(); r++) std::copy(hnorm + goff[r], hnorm + goff[r] + glen[r], trees[r]->cn.data());
 }
 
 namespace {
@@ -1741,8 +1764,15 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
         k_multiply_df(ctx.dbasis, (const MulTask *)pk.ptr(0), (int)tasks.size(), ctx.nsm, ctx.stream);
         st.launches++;
         st.out_nodes += (long long)tasks.size();
-        // the norms of the nodes computed at this level: one copy of their index range when it is
-        // contiguous (the children appended by the last refinement), else the whole array
+        // the norms of the nodes computed at this level (each job's index range: the children
+        // appended by the last refinement, or the whole array when not contiguous), gathered on
+        // the device and downloaded with one copy into pinned memory: a copy per tree into its
+        // pageable norm array cost several microseconds each, hundreds of trees per level
+        std::vector<const double *> gsrc;
+        std::vector<long long> goff;
+        std::vector<int> glen;
+        std::vector<std::pair<Tree *, size_t>> gdst;  // (tree, first node)
+        long long gtot = 0;
         for (auto &s : ms) {
             Tree &out = *s.job->out;
             if (s.work.empty()) continue;
@@ -1752,14 +1782,36 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
                 first = (size_t)*mm.first;
                 count = s.work.size();
             }
-            MWG_CUDA(cudaMemcpyAsync(out.cn.data() + 8 * first, out.d_cn + 8 * first, sizeof(double) * 8 * count,
-                                     cudaMemcpyDeviceToHost, ctx.stream));
+            gsrc.push_back(out.d_cn + 8 * first);
+            goff.push_back(gtot);
+            glen.push_back((int)(8 * count));
+            gdst.push_back({&out, first});
+            gtot += (long long)(8 * count);
+        }
+        double *hnorm = nullptr;
+        if (gtot > 0) {
+            Packer pg;
+            pg.add(gsrc.data(), gsrc.size() * sizeof(const double *));
+            pg.add(goff.data(), goff.size() * sizeof(long long));
+            pg.add(glen.data(), glen.size() * sizeof(int));
+            pg.ship(ctx, arena);
+            double *dnorm = (double *)arena.alloc(sizeof(double) * (size_t)gtot);
+            k_gather_ranges((const double *const *)pg.ptr(0), (const long long *)pg.ptr(1), (const int *)pg.ptr(2),
+                            (int)gsrc.size(), dnorm, ctx.stream);
+            st.launches++;
+            hnorm = (double *)arena.halloc(sizeof(double) * (size_t)gtot);
+            MWG_CUDA(cudaMemcpyAsync(hnorm, dnorm, sizeof(double) * (size_t)gtot, cudaMemcpyDeviceToHost, ctx.stream));
         }
         ctx.sync();
+        for (size_t r = 0; r < gdst.size(); r++)
+            std::copy(hnorm + goff[r], hnorm + goff[r] + glen[r], gdst[r].first->cn.data() + 8 * gdst[r].second);
         st.host_wait_ms += since(tD);
         auto tE = clk::now();
-        // refinement; the new children need no zeroing: the next level's kernel writes their blocks
-        for (auto &s : ms) {
+        // refinement, jobs in parallel (each splits its own tree); the new children need no
+        // zeroing: the next level's kernel writes their blocks
+#pragma omp parallel for schedule(dynamic, 4)
+        for (long j = 0; j < (long)ms.size(); j++) {
+            MulState &s = ms[j];
             Tree &out = *s.job->out;
             double R = s.job->abs_prec ? 1.0 : std::sqrt(out.sqnorm_leaves());
             std::vector<int> next;

@@ -15,6 +15,7 @@
 #include <stdexcept>
 #include <tuple>
 #include <string>
+#include <mutex>
 #include <unordered_map>
 #include <vector>
 
@@ -212,6 +213,7 @@ struct Ctx {
     // earlier, on any of the context's streams, may still read them, so they are released only
     // when the call has ended and every stream of the context is idle (release_retired).
     std::vector<void *> retired;
+    std::mutex retired_mu;  // trees of one call may grow on several host threads
     void release_retired();
 };
 
@@ -334,6 +336,9 @@ void k_topdown_df(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t 
 void k_compress_df(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s);
 // the multiply's node kernel (mw_multiply_df.cu): double-FP32 transforms, FP64 blocks in and out
 void k_multiply_df(const DevBasis &b, const MulTask *tasks, int n, int nsm, cudaStream_t s);
+// dst[off[r] ..] = the len[r] doubles at src[r], for n ranges (one download of many small arrays)
+void k_gather_ranges(const double *const *src, const long long *off, const int *len, int n, double *dst,
+                     cudaStream_t s);
 void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
            cudaStream_t s);
 void k_to_fp32(const double *in, float *out, size_t n, cudaStream_t s);

@@ -808,6 +808,23 @@ void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int
     MWG_CUDA(cudaGetLastError());
 }
 
+// dst[off[r] .. off[r] + len[r]) = src[r][0 .. len[r]): one CTA per range
+__global__ void gather_ranges_kernel(const double *const *src, const long long *off, const int *len, int n,
+                                     double *dst) {
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        const double *s = src[r];
+        double *d = dst + off[r];
+        for (int i = threadIdx.x; i < len[r]; i += blockDim.x) d[i] = s[i];
+    }
+}
+
+void k_gather_ranges(const double *const *src, const long long *off, const int *len, int n, double *dst,
+                     cudaStream_t s) {
+    if (n <= 0) return;
+    gather_ranges_kernel<<<n < 4096 ? n : 4096, 128, 0, s>>>(src, off, len, n, dst);
+    MWG_CUDA(cudaGetLastError());
+}
+
 void k_add(const DevBasis &b, const AddTask *tasks, const double *const *src, const double *coefs, int n, int bs,
            cudaStream_t s) {
     if (n <= 0) return;

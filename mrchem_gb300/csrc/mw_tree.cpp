@@ -170,6 +170,7 @@ void Tree::reserve(size_t n) {
                                  ctx->stream));
         MWG_CUDA(cudaMemcpyAsync(ncn, d_cn, sizeof(double) * 8 * nodes.size(), cudaMemcpyDeviceToDevice,
                                  ctx->stream));
+        std::lock_guard<std::mutex> lock(ctx->retired_mu);
         ctx->retired.push_back(d_coefs);
         ctx->retired.push_back(d_cn);
     }
