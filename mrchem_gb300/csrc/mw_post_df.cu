@@ -16,12 +16,12 @@
 // global memory stay FP64; the norms are summed in FP64.  The FP64 values are split into FP32
 // pairs with integer operations (mw_dfconv.cuh), off GB300's slow FP64 pipe.
 //
-// One CTA per node, one thread per line of the cube: the x pass reads its row
-// straight from the FP64 block(s) in global memory into registers and writes
-// the transformed row to the shared cube, the y and z passes read a column into
-// registers and write it back (y) or out to global memory (z).  The shared cube
-// rows are padded to 2K + 1 pairs, which makes the row-wise x-pass stores free
-// of bank conflicts.
+// One CTA per node, one thread per line of the cube: the CTA stages the FP64
+// input as a cube of FP32 pairs in shared memory, then each pass transforms the
+// threads' lines from one shared cube into the other (the last pass of the
+// compression writes the parent's FP64 block and its norms).  Cube rows are
+// padded to 2K + 1 pairs, which keeps the row-wise accesses free of bank
+// conflicts.
 #include "mw_dfconv.cuh"
 #include "mw_host.h"
 
@@ -51,28 +51,32 @@ template <int K>
 struct PostGeo {
     static constexpr int N2 = 2 * K, NC = N2 * N2, K3 = K * K * K, RS = N2 + 1;
     static constexpr int THREADS = ((NC + 31) / 32) * 32;
-    // cube (N2 x N2 rows of RS pairs), M^T hi and lo (NC floats each), 8 K^2 norm partials
+    // two cubes (N2 x N2 rows of RS pairs: the y pass reads one and writes the other), M^T hi and lo
+    // (NC floats each), 8 K^2 norm partials
     static constexpr size_t SMEM =
-        sizeof(float2) * (size_t)NC * RS + sizeof(float) * 2 * (size_t)NC + sizeof(double) * 8 * K * K;
+        sizeof(float2) * 2 * (size_t)NC * RS + sizeof(float) * 2 * (size_t)NC + sizeof(double) * 8 * K * K;
 };
 
-// out = M v for one line of 2K values, M^T in shared memory as hi / lo rows (M^T[k][j] = M[j][k]);
-// the outputs are made in two halves of K and handed to store(j, hi, lo) renormalised
-// (|lo| <= ulp(hi) / 2), so that only K accumulator pairs are live beside the line
+// out = M v for one line of 2K values held in shared memory (element i at line[i * stride]), M^T
+// in shared memory as hi / lo rows (M^T[k][j] = M[j][k]); the outputs are made in two halves of K
+// and handed to store(j, hi, lo) renormalised (|lo| <= ulp(hi) / 2).  The k loop is rolled: a few
+// hundred instructions, where a fully unrolled transform (thousands) overflowed the instruction
+// cache and stalled the small launches of the post-processing
 template <int K, class Store>
-__device__ __forceinline__ void pdf_line(const float (&vh)[2 * K], const float (&vl)[2 * K], const float *mth,
-                                         const float *mtl, Store store) {
+__device__ __forceinline__ void pdf_line_smem(const float2 *line, int stride, const float *mth, const float *mtl,
+                                              Store store) {
     constexpr int N2 = 2 * K;
-#pragma unroll
+#pragma unroll 1
     for (int h = 0; h < 2; h++) {
         float oh[K], ol[K];
 #pragma unroll
         for (int j = 0; j < K; j++) oh[j] = ol[j] = 0.0f;
-#pragma unroll
+#pragma unroll 1
         for (int k = 0; k < N2; k++) {
+            const float2 v = line[k * stride];
 #pragma unroll
             for (int j = 0; j < K; j++)
-                pdf_fma(oh[j], ol[j], mth[k * N2 + h * K + j], mtl[k * N2 + h * K + j], vh[k], vl[k]);
+                pdf_fma(oh[j], ol[j], mth[k * N2 + h * K + j], mtl[k * N2 + h * K + j], v.x, v.y);
         }
 #pragma unroll
         for (int j = 0; j < K; j++) {
@@ -90,8 +94,9 @@ __global__ void __launch_bounds__(PostGeo<K>::THREADS, 1)
     using G = PostGeo<K>;
     constexpr int N2 = G::N2, NC = G::NC, K3 = G::K3, RS = G::RS;
     extern __shared__ __align__(16) float2 smem_post[];
-    float2 *s_cube = smem_post;  // cube[Z][Y][X] at (Z * N2 + Y) * RS + X
-    float *s_mth = reinterpret_cast<float *>(s_cube + (size_t)NC * RS);
+    float2 *s_cube = smem_post;               // cube[Z][Y][X] at (Z * N2 + Y) * RS + X: x pass out, z pass out
+    float2 *s_cub2 = s_cube + (size_t)NC * RS;  // the same layout: y pass out
+    float *s_mth = reinterpret_cast<float *>(s_cub2 + (size_t)NC * RS);
     float *s_mtl = s_mth + NC;
     double *s_red = reinterpret_cast<double *>(s_mtl + NC);  // [component][K^2]
     const int tid = threadIdx.x;
@@ -108,57 +113,51 @@ __global__ void __launch_bounds__(PostGeo<K>::THREADS, 1)
 
     for (int t = blockIdx.x; t < n; t += gridDim.x) {
         const PairTask task = tasks[t];
-        double s0 = 0.0, s1 = 0.0;  // MODE 1, z pass: this line's squared norms (Z < K, Z >= K)
-        // The three passes run through one instance of the line transform (an instance per pass
-        // overflowed the instruction cache): x reads the thread's row from the FP64 block(s), y and
-        // z read a line of the shared cube; every pass writes back into the cube, except the
-        // compression's z pass, which writes the parent's FP64 block.  Thread mapping: x (Y, Z) =
-        // (a, bq), y (X, Z) = (a, bq), z (X, Y) = (a, bq).
-#pragma unroll 1
-        for (int dim = 0; dim < 3; dim++) {
-            __syncthreads();  // x: M^T ready, the previous node's cube and partials no longer read;
-                              // y, z: the previous pass's stores are visible
-            if (!active) continue;
-            const int base = dim == 0 ? (bq * N2 + a) * RS : (dim == 1 ? bq * N2 * RS + a : a + bq * RS);
-            const int stride = dim == 0 ? 1 : (dim == 1 ? RS : N2 * RS);
-            float vh[N2], vl[N2];
-            if (dim == 0) {
-                const int cyz = (a >= K ? 2 : 0) | (bq >= K ? 4 : 0);
-                const int r = (bq % K) * K * K + (a % K) * K;
-#pragma unroll
-                for (int X = 0; X < N2; X++) {
-                    const int c = cyz | (X >= K ? 1 : 0);
-                    const double d = MODE == 0 ? task.parent[(size_t)c * K3 + r + X % K]
-                                               : task.child0[(size_t)c * 8 * K3 + r + X % K];
-                    df_split(d, vh[X], vl[X]);
-                }
+        // the FP64 input, split into FP32 pairs, staged as a cube by all threads (coalesced reads):
+        // top-down the parent's block, compression the children's scaling parts (child c in
+        // octant c); then x: s_cube -> s_cub2, y: s_cub2 -> s_cube, z: s_cube -> s_cub2 (top-down)
+        // or the parent's FP64 block with its norms (compression)
+        __syncthreads();  // M^T ready; the previous node's cubes and partials are no longer read
+        for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
+            const int c = gi / K3, r = gi - c * K3;
+            const int ix = r % K, iy = (r / K) % K, iz = r / (K * K);
+            const int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
+            const double d = MODE == 0 ? task.parent[gi] : task.child0[(size_t)c * 8 * K3 + r];
+            float h, l;
+            df_split(d, h, l);
+            s_cube[(size_t)(Z * N2 + Y) * RS + X] = make_float2(h, l);
+        }
+        __syncthreads();
+        if (active) {  // x pass, thread (Y, Z) = (a, bq)
+            const int off = (bq * N2 + a) * RS;
+            pdf_line_smem<K>(s_cube + off, 1, s_mth, s_mtl,
+                             [&](int X, float h, float l) { s_cub2[off + X] = make_float2(h, l); });
+        }
+        __syncthreads();
+        if (active) {  // y pass, thread (X, Z) = (a, bq)
+            const int off = bq * N2 * RS + a;
+            pdf_line_smem<K>(s_cub2 + off, RS, s_mth, s_mtl,
+                             [&](int Y, float h, float l) { s_cube[off + Y * RS] = make_float2(h, l); });
+        }
+        __syncthreads();
+        if (active) {  // z pass, thread (X, Y) = (a, bq)
+            const int off = bq * RS + a;
+            if (MODE == 0) {
+                pdf_line_smem<K>(s_cube + off, N2 * RS, s_mth, s_mtl,
+                                 [&](int Z, float h, float l) { s_cub2[off + Z * N2 * RS] = make_float2(h, l); });
             } else {
-                // the whole line is in registers before the first store
-#pragma unroll
-                for (int i = 0; i < N2; i++) {
-                    const float2 v = s_cube[base + i * stride];
-                    vh[i] = v.x;
-                    vl[i] = v.y;
-                }
-            }
-            const bool to_parent = MODE == 1 && dim == 2;
-            const int cxy = (a >= K ? 1 : 0) | (bq >= K ? 2 : 0);  // z pass: (X, Y) = (a, bq)
-            const int r2 = (bq % K) * K + a % K;
-            pdf_line<K>(vh, vl, s_mth, s_mtl, [&](int j, float h, float l) {
-                if (to_parent) {
-                    const int c = cxy | (j >= K ? 4 : 0);
-                    // CUDA conversions here: the integer join made this pass spill at K = 9, 10
-                    const double v = (double)h + (double)l;
-                    task.parent[(size_t)c * K3 + (size_t)(j % K) * K * K + r2] = v;
-                    if (j < K)
+                const int cxy = (a >= K ? 1 : 0) | (bq >= K ? 2 : 0);
+                const int r2 = (bq % K) * K + a % K;
+                double s0 = 0.0, s1 = 0.0;  // this line's squared norms (Z < K, Z >= K)
+                pdf_line_smem<K>(s_cube + off, N2 * RS, s_mth, s_mtl, [&](int Z, float h, float l) {
+                    const int c = cxy | (Z >= K ? 4 : 0);
+                    const double v = df_widen(h) + df_widen(l);
+                    task.parent[(size_t)c * K3 + (size_t)(Z % K) * K * K + r2] = v;
+                    if (Z < K)
                         s0 = fma(v, v, s0);
                     else
                         s1 = fma(v, v, s1);
-                } else {
-                    s_cube[base + j * stride] = make_float2(h, l);
-                }
-            });
-            if (to_parent) {
+                });
                 s_red[cxy * K * K + r2] = s0;
                 s_red[(cxy | 4) * K * K + r2] = s1;
             }
@@ -170,7 +169,7 @@ __global__ void __launch_bounds__(PostGeo<K>::THREADS, 1)
                 const int c = gi / K3, r = gi - c * K3;
                 const int ix = r % K, iy = (r / K) % K, iz = r / (K * K);
                 const int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
-                const float2 v = s_cube[(size_t)(Z * N2 + Y) * RS + X];
+                const float2 v = s_cub2[(size_t)(Z * N2 + Y) * RS + X];
                 task.child0[(size_t)c * 8 * K3 + r] += df_widen(v.x) + df_widen(v.y);
             }
         }
