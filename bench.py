@@ -34,7 +34,7 @@ ORDER, PREC = 9, 1e-6
 # tier launch of two mixed steps of the first 8 orbitals of the batch with the caches left warm
 # (--cache-control none), divided by those launches' items; summarised with its command in
 # profiles/dram_traffic_tiers_k10.md and re-captured whenever a tier kernel changes
-DRAM_PER_ITEM = {"fp32": 2.45e3, "tf32": 0.43e3, "df32": 4.58e3}
+DRAM_PER_ITEM = {"fp32": 2.45e3, "tf32": 0.43e3, "df32": 4.55e3}
 NORB = 16
 METRIC = "Helmholtz-apply nodes/s: batched mixed vs plain FP64 GPU at 1e-6 rel. error"
 
