@@ -20,9 +20,10 @@
 // which keeps the conversions off GB300's slow FP64 pipe.
 //
 // Layout: one CTA per node, one thread per line of the cube, the two cubes in shared memory
-// (rows padded to 2K + 1 pairs, conflict-free row stores).  The x pass of each input reads its
-// row straight from the FP64 block; the product is formed in b's z pass by the thread that owns
-// the same line of a's cube; the last (z) pass of the backward transform writes the FP64 block.
+// (rows padded to 2K + 1 pairs, conflict-free row stores).  The two input blocks are staged as
+// cubes by coalesced loads; every pass transforms a line in place (the thread reads all of it
+// first); the product is formed in b's z pass by the thread that owns the same line of a's cube;
+// the last (z) pass of the backward transform writes the FP64 block.
 #include "mw_dfconv.cuh"
 #include "mw_host.h"
 
@@ -68,33 +69,35 @@ struct MulGeo {
         sizeof(float2) * 2 * (size_t)NC * RS + sizeof(float) * 4 * (size_t)NC + sizeof(double) * 8 * K * K;
 };
 
-// out = M v for one line of 2K values (M^T in shared memory as hi / lo rows, M^T[k][j] = M[j][k]);
-// outputs in two halves of K, handed to store(j, hi, lo) renormalised
+// out = M v for one line of 2K values held in shared memory (element i at line[i * stride]), M^T
+// in shared memory as hi / lo rows (M^T[k][j] = M[j][k]); every output is formed before the first
+// is handed to store(j, hi, lo) (renormalised), so a pass may write back into the line it read.
+// The k loop is rolled: a few hundred instructions, where a fully unrolled transform (thousands)
+// stalled the warps on instruction fetch.
 template <int K, class Store>
-__device__ __forceinline__ void mdf_line(const float (&vh)[2 * K], const float (&vl)[2 * K], const float *mth,
-                                         const float *mtl, Store store) {
+__device__ __forceinline__ void mdf_line(const float2 *line, int stride, const float *mth, const float *mtl,
+                                         Store store) {
     constexpr int N2 = 2 * K;
+    float oh[N2], ol[N2];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-        float oh[K], ol[K];
+    for (int j = 0; j < N2; j++) oh[j] = ol[j] = 0.0f;
+#pragma unroll 1
+    for (int k = 0; k < N2; k++) {
+        const float2 v = line[k * stride];
 #pragma unroll
-        for (int j = 0; j < K; j++) oh[j] = ol[j] = 0.0f;
+        for (int j = 0; j < N2; j++) mdf_fma(oh[j], ol[j], mth[k * N2 + j], mtl[k * N2 + j], v.x, v.y);
+    }
 #pragma unroll
-        for (int k = 0; k < N2; k++) {
-#pragma unroll
-            for (int j = 0; j < K; j++)
-                mdf_fma(oh[j], ol[j], mth[k * N2 + h * K + j], mtl[k * N2 + h * K + j], vh[k], vl[k]);
-        }
-#pragma unroll
-        for (int j = 0; j < K; j++) {
-            const float t = __fadd_rn(oh[j], ol[j]);
-            store(h * K + j, t, __fsub_rn(ol[j], __fsub_rn(t, oh[j])));
-        }
+    for (int j = 0; j < N2; j++) {
+        const float t = __fadd_rn(oh[j], ol[j]);
+        store(j, t, __fsub_rn(ol[j], __fsub_rn(t, oh[j])));
     }
 }
 
-// The nine line passes of a node, in order; passes of one group run between the same two barriers:
-//   0, 1  x passes of a and b, reading rows from the FP64 blocks        (group 0)
+// The two FP64 input blocks are first staged as cubes of FP32 pairs (coalesced loads); then the
+// nine line passes of a node, in order, each in place on its cube; passes of one group run between
+// the same two barriers:
+//   0, 1  x passes of a and b                                          (group 0)
 //   2, 3  y passes of a and b                                          (group 1)
 //   4, 5  z passes of a (into its cube) and b (product into a's cube)  (group 2)
 //   6     x pass of the product, 7 its y pass                         (groups 3, 4)
@@ -133,6 +136,18 @@ __global__ void __launch_bounds__(MulGeo<K>::THREADS) multiply_df_kernel(DevBasi
         float sh, sl;
         mdf_split(task.scale, sh, sl);
         double s0 = 0.0, s1 = 0.0;  // pass 8: this line's squared norms (Z < K, Z >= K)
+        __syncthreads();  // the matrices are ready; the previous node's cubes are no longer read
+        for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
+            const int c = gi / K3, r = gi - c * K3;
+            const int ix = r % K, iy = (r / K) % K, iz = r / (K * K);
+            const int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
+            const int at = (Z * N2 + Y) * RS + X;
+            float h, l;
+            df_split(task.a[gi], h, l);
+            s_a[at] = make_float2(h, l);
+            df_split(task.b[gi], h, l);
+            s_b[at] = make_float2(h, l);
+        }
 #pragma unroll 1
         for (int pass = 0; pass < 9; pass++) {
             if (pass == 0 || pass == 2 || pass == 4 || pass >= 6) __syncthreads();
@@ -143,25 +158,10 @@ __global__ void __launch_bounds__(MulGeo<K>::THREADS) multiply_df_kernel(DevBasi
             // line start and element stride in the cube
             const int base = dim == 0 ? (q * N2 + p) * RS : (dim == 1 ? q * N2 * RS + p : p + q * RS);
             const int stride = dim == 0 ? 1 : (dim == 1 ? RS : N2 * RS);
-            float vh[N2], vl[N2];
-            if (pass < 2) {  // row X of the FP64 block, (Y, Z) = (p, q)
-                const double *g = on_b ? task.b : task.a;
-                const int cyz = (p >= K ? 2 : 0) | (q >= K ? 4 : 0);
-                const int r = (q % K) * K * K + (p % K) * K;
-#pragma unroll
-                for (int X = 0; X < N2; X++) df_split(g[(size_t)(cyz | (X >= K ? 1 : 0)) * K3 + r + X % K], vh[X], vl[X]);
-            } else {
-#pragma unroll
-                for (int i = 0; i < N2; i++) {
-                    const float2 v = cube[base + i * stride];
-                    vh[i] = v.x;
-                    vl[i] = v.y;
-                }
-            }
             const float *mth = pass < 6 ? s_inh : s_outh, *mtl = pass < 6 ? s_inl : s_outl;
             const int cxy = (p >= K ? 1 : 0) | (q >= K ? 2 : 0);  // pass 8: (X, Y) = (p, q)
             const int r8 = (q % K) * K + p % K;
-            mdf_line<K>(vh, vl, mth, mtl, [&](int j, float h, float l) {
+            mdf_line<K>(cube + base, stride, mth, mtl, [&](int j, float h, float l) {
                 if (pass == 5) {  // product on a's z line: a * scale * b
                     const float2 av = s_a[base + j * stride];
                     const float2 as = mdf_mul(av.x, av.y, sh, sl);
