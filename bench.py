@@ -679,8 +679,9 @@ def run(args):
                "MEASURED_PEAKS.json holds no TF32 figure")
     roofs = {
         "fp64": roof("fp64", st_ser["kernel_ms_fp64"], fp64_tf, "apply_kernel<double,10>", "fp64-pipe", fma_src),
-        # the FP32-accuracy tier of the mixed step runs on the tensor cores as split TF32: three
-        # MMAs (hi*hi, hi*lo, lo*hi) per tile and k-step, 3 x the TF32 tier's issued work
+        # the FP32-accuracy tier of the mixed step runs on the tensor cores as split TF32: per tile
+        # and k-step A_hi * [B_hi B_lo] (width 64) and A_lo * B_hi (width 32), the issued work of
+        # three N = 32 MMAs (hi*hi, hi*lo, lo*hi), 3 x the TF32 tier's
         "fp32": roof("fp32", st_ser["kernel_ms_fp32"], tf32_tf, "apply_tc05_kernel<10,1> (split TF32)", "tensor",
                      mma_src, issued_item=3 * tc_issued_item),
         "tf32": roof("tf32", st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc05_kernel<10,0>", "tensor", mma_src,

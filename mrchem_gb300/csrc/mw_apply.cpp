@@ -490,6 +490,7 @@ ScreenOp oper_screen_view(const Oper &op) {
     so.b64 = op.d_blocks;
     so.b32 = op.d_blocks32;
     so.btc = op.d_blocks_tc;
+    so.btc2 = op.split_blocks();
     so.T = op.T;
     so.S = op.S;
     return so;
@@ -1291,9 +1292,10 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                         const size_t tx = tc5_x_stride(b.K), tb = tc5_b_stride(b.K);
                         T.in[pi] = cd.gen ? (const void *)(s.gbase_tc + tx * (size_t)cd.src)
                                           : (const void *)(inp.d_coefs_tc + tx * (size_t)cd.src);
-                        T.ax[pi] = op.d_blocks_tc + tb * (size_t)bxi;
-                        T.ay[pi] = op.d_blocks_tc + tb * (size_t)byi;
-                        T.az[pi] = op.d_blocks_tc + tb * (size_t)bzi;
+                        const float *bt = cd.tier == 1 ? op.split_blocks() : op.d_blocks_tc;
+                        T.ax[pi] = bt + tb * (size_t)bxi;
+                        T.ay[pi] = bt + tb * (size_t)byi;
+                        T.az[pi] = bt + tb * (size_t)bzi;
                     } else {
                         // the reduced tiers read the FP32 cube-order shadows and the FP32 operator blocks
                         // (high part first, low part after it)

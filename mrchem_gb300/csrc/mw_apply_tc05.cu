@@ -118,8 +118,33 @@ struct T5Mem {
     static constexpr int BSET = 3 * NP * G::BSZ;  // one set of B operands
     static constexpr int SMEM = OB + 2 * BSET;
     static constexpr uint32_t STAGE_BYTES = (uint32_t)(NP * (G::SX + 3 * G::BSZ));
-    static constexpr int MAX_CTAS = SPLIT ? 1 : G::MAX_CTAS;
-    static constexpr int SMEM_LAUNCH = SPLIT ? SMEM : G::SMEM_LAUNCH;
+    // TMEM columns per M tile: the split tier's MMAs of width 2N put A_hi * B_hi in a tile's first N
+    // columns and A_hi * B_lo in the next N; the epilogues add the two halves
+    static constexpr bool WIDE = SPLIT && tc5_split_wide(K);
+    static constexpr int NT = WIDE ? 2 * G::N : G::N;
+    static constexpr int TMEM_COLS = WIDE ? (2 * G::MT * NT <= 64 ? 64 : (2 * G::MT * NT <= 128 ? 128 : (2 * G::MT * NT <= 256 ? 256 : 512)))
+                                          : G::TMEM_COLS;
+    // B operand k-group stride: the wide form's layout holds a group's N hi rows, then its N lo rows
+    static constexpr int LBO_B = WIDE ? 2 * G::LBO_B : G::LBO_B;
+    static_assert(2 * G::MT * NT <= 512, "TMEM budget");
+    // as for the TF32 tier: request enough shared memory that no more CTAs share an SM than its 512
+    // TMEM columns serve (a CTA whose allocation waits would hold its SM's resources idle)
+    static constexpr int MAX_CTAS = SPLIT ? 512 / TMEM_COLS : G::MAX_CTAS;
+    // CTAs per SM of the split tier with the narrow and the wide tiles (TMEM, shared memory, and
+    // registers: about 90 a thread x 288 threads leave room for two CTAs); the wide form is used
+    // only where it keeps the count
+    static constexpr int fits(int tmem_cols) {
+        return (512 / tmem_cols) < (228 * 1024 / SMEM) ? ((512 / tmem_cols) < 2 ? (512 / tmem_cols) : 2)
+                                                       : ((228 * 1024 / SMEM) < 2 ? (228 * 1024 / SMEM) : 2);
+    }
+    static constexpr int WIDE_COLS = 2 * G::MT * 2 * G::N <= 64    ? 64
+                                     : 2 * G::MT * 2 * G::N <= 128 ? 128
+                                     : 2 * G::MT * 2 * G::N <= 256 ? 256
+                                                                   : 512;
+    static_assert(!SPLIT || tc5_split_wide(K) == (fits(WIDE_COLS) >= fits(G::TMEM_COLS)),
+                  "tc5_split_wide: the wide tiles exactly where they keep the CTAs per SM");
+    static constexpr int SMEM_FLOOR = 228 * 1024 / (MAX_CTAS + 1);
+    static constexpr int SMEM_LAUNCH = !SPLIT ? G::SMEM_LAUNCH : (MAX_CTAS >= 8 || SMEM >= SMEM_FLOOR ? SMEM : SMEM_FLOOR);
     static_assert(SPLIT || (OR == G::OR && OB == G::OB && SMEM == G::SMEM && STAGE_BYTES == G::STAGE_BYTES),
                   "the TF32 tier's layout");
     static_assert(OR % 16 == 0 && OB % 16 == 0 && BSET % 16 == 0 && G::RSZ % 16 == 0, "alignment");
@@ -205,14 +230,23 @@ __device__ __forceinline__ float *r_at(uint8_t *R, int r, int k) {
     return reinterpret_cast<float *>(R + (k >> 2) * T5Geo<K>::LBO_R + 16 * r + 4 * (k & 3));
 }
 
-// the epilogue of one pass for the TMEM tiles of this warp (tiles half, half + 2, ... < tiles)
-template <int K, class Row>
+// the epilogue of one pass for the TMEM tiles of this warp (tiles half, half + 2, ... < tiles);
+// WIDE: a tile is 2N columns wide and a row's value is the sum of its two halves
+template <int K, bool WIDE, class Row>
 __device__ __forceinline__ void t5_epilogue(uint32_t tcol, int tiles, int q, int half, int lane, Row row) {
-    constexpr int N = T5Geo<K>::N;
+    constexpr int N = T5Geo<K>::N, NT = WIDE ? 2 * N : N;
     for (int i = half; i < tiles; i += 2) {
         uint32_t a[32];
-        t5_ld<K>(tcol + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * N), a);
+        const uint32_t t = tcol + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * NT);
+        t5_ld<K>(t, a);
         t5_wait(a);
+        if (WIDE) {
+            uint32_t b[32];
+            t5_ld<K>(t + (uint32_t)N, b);
+            t5_wait(b);
+#pragma unroll
+            for (int j = 0; j < N; j++) a[j] = __float_as_uint(__fadd_rn(__uint_as_float(a[j]), __uint_as_float(b[j])));
+        }
         row(i * 128 + 32 * q + lane, a);
     }
 }
@@ -246,7 +280,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
     for (int i = tid; i < M::SMEM / 16; i += blockDim.x) reinterpret_cast<float4 *>(smem5)[i] = make_float4(0, 0, 0, 0);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&s_tmem)),
-                     "r"(G::TMEM_COLS));
+                     "r"(M::TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
@@ -258,11 +292,14 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
     __syncthreads();
     t5_after_sync();
     const uint32_t tmem = s_tmem;
-    const uint32_t tD = tmem, tACC = tmem + (uint32_t)(G::MT * N);  // column offsets
+    const uint32_t tD = tmem, tACC = tmem + (uint32_t)(G::MT * M::NT);  // column offsets
+    // instruction descriptors: F32 accumulator, TF32 A and B, M = 128, N = N (and 2N for the split
+    // tier's MMAs that take B_hi and B_lo side by side)
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    const uint32_t idesc2 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(M::NT >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
     // descriptors of the operands' first core matrices; a tile / k-step adds its byte offset >> 4
     const uint64_t dS = t5_desc(smem_addr(sS), G::LBO_S, 128), dR = t5_desc(smem_addr(sR), G::LBO_R, 128);
-    const uint64_t dB = t5_desc(smem_addr(sB), G::LBO_B, 128);
+    const uint64_t dB = t5_desc(smem_addr(sB), M::LBO_B, 128);
     uint32_t ph = 0;     // bit b: the parity of barrier b's next phase (a thread tracks the ones it waits on)
     uint32_t nitem = 0;  // items this CTA has started: B set nitem & 1
 
@@ -291,23 +328,23 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
         t5_after_sync();
     };
     // the issuing thread: tiles x k-steps of one pass, then a commit to barrier b (none if b < 0)
-    // split tier: hi * hi, then hi * lo and lo * hi into the same accumulator (lo * lo dropped);
-    // a_lo / b_lo: the descriptor offsets of the operands' lo copies
+    // split tier, wide form: per tile and k-step, A_hi * [B_hi B_lo] (width 2N: hi * hi and hi * lo
+    // side by side) and A_lo * B_hi (width N, into the first half); narrow form: hi * hi, hi * lo
+    // and lo * hi into one accumulator of width N (B_lo BSZ bytes after B_hi).  lo * lo is dropped.
+    // a_lo: the descriptor offset of A's lo copy
     auto issue_pass = [&](uint64_t da, int lbo_a, uint32_t a_lo, uint64_t db, int tiles, uint32_t dcol,
                           bool accumulate, int b) {
         if (s_fail) return;
-        const uint32_t b_lo = (uint32_t)(G::BSZ >> 4);
+        constexpr uint32_t b_lo = (uint32_t)(G::BSZ >> 4);
         for (int i = 0; i < tiles; i++)
 #pragma unroll
             for (int s = 0; s < G::KS; s++) {
                 const uint64_t a = da + (uint64_t)((2 * s * lbo_a + i * 2048) >> 4);
-                const uint64_t bb = db + (uint64_t)((2 * s * G::LBO_B) >> 4);
-                const uint32_t d = dcol + (uint32_t)(i * N);
-                t5_mma(d, a, bb, idesc, (accumulate || s > 0) ? 1u : 0u);
-                if (SPLIT) {
-                    t5_mma(d, a, bb + b_lo, idesc, 1u);
-                    t5_mma(d, a + a_lo, bb, idesc, 1u);
-                }
+                const uint64_t bb = db + (uint64_t)((2 * s * M::LBO_B) >> 4);
+                const uint32_t d = dcol + (uint32_t)(i * M::NT);
+                t5_mma(d, a, bb, M::WIDE ? idesc2 : idesc, (accumulate || s > 0) ? 1u : 0u);
+                if (SPLIT && !M::WIDE) t5_mma(d, a, bb + b_lo, idesc, 1u);
+                if (SPLIT) t5_mma(d, a + a_lo, bb, idesc, 1u);
             }
         if (b >= 0) t5_commit(&bar[b]);
     };
@@ -346,7 +383,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                 // ---- x epilogue: D row (Z, Y) -> A_y rows (X', Z) and extra rows (X' < K, Z < K), k = Y
                 wait(1);
                 t5_after_sync();
-                t5_epilogue<K>(tD, G::MTX, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
+                t5_epilogue<K, M::WIDE>(tD, G::MTX, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
                     if (r >= NN) return;
                     const int Z = r / N2, Y = r - Z * N2;
                     float *base = r_at<K>(sR, 0, Y);
@@ -366,7 +403,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                 const float cf = float(L.coef[j]);
                 wait(2);
                 t5_after_sync();
-                t5_epilogue<K>(tD, G::MT, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
+                t5_epilogue<K, M::WIDE>(tD, G::MT, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
                     if (r < NN) {
                         const int xp = r / N2, Z = r - xp * N2;
                         float *base = r_at<K>(sR, 0, Z);
@@ -421,7 +458,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                 }
             };
             if (b0 < b1) {
-                t5_epilogue<K>(tACC, G::MT, q, half, lane, row);
+                t5_epilogue<K, M::WIDE>(tACC, G::MT, q, half, lane, row);
             } else {
                 uint32_t zero[32] = {};
                 for (int i = half; i < G::MT; i += 2) row(i * 128 + 32 * q + lane, zero);
@@ -444,7 +481,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
     __syncthreads();
     t5_after_sync();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(G::TMEM_COLS));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(M::TMEM_COLS));
 }
 
 template <int K, int SPLIT>

@@ -398,9 +398,12 @@ void build_operators(const std::vector<Oper *> &ops, const Basis &b) {
     for (Oper *op : ops) {
         const long nb = std::max<long>(op->nblocks, 1);
         MWG_CUDA(cudaMalloc(&op->d_blocks32, sizeof(float) * 2 * (size_t)nb * bsz));
-        if (tc) MWG_CUDA(cudaMalloc(&op->d_blocks_tc, sizeof(float) * tc5_b_stride(K) * (size_t)nb));
-        k_op_convert(op->d_blocks, op->d_blocks32, tc ? op->d_blocks_tc : nullptr, nb, K, tc5_n(K), 2 * tc5_ks(K),
-                     st);
+        if (tc) {
+            MWG_CUDA(cudaMalloc(&op->d_blocks_tc, sizeof(float) * tc5_b_stride(K) * (size_t)nb));
+            if (tc5_split_wide(K)) MWG_CUDA(cudaMalloc(&op->d_blocks_tc2, sizeof(float) * tc5_b_stride(K) * (size_t)nb));
+        }
+        k_op_convert(op->d_blocks, op->d_blocks32, tc ? op->d_blocks_tc : nullptr, op->d_blocks_tc2, nb,
+                     K, tc5_n(K), 2 * tc5_ks(K), st);
     }
     MWG_CUDA(cudaStreamSynchronize(st));
     for (void *pp : {(void *)d_cc, (void *)d_q, (void *)d_tasks, (void *)d_nrm, (void *)d_band, (void *)d_peak,
@@ -412,10 +415,12 @@ void Oper::free_device() {
     if (d_blocks) cudaFree(d_blocks);
     if (d_blocks32) cudaFree(d_blocks32);
     if (d_blocks_tc) cudaFree(d_blocks_tc);
+    if (d_blocks_tc2) cudaFree(d_blocks_tc2);
     if (d_screen) cudaFree(d_screen);
     d_blocks = nullptr;
     d_blocks32 = nullptr;
     d_blocks_tc = nullptr;
+    d_blocks_tc2 = nullptr;
     d_screen = nullptr;
 }
 

@@ -132,6 +132,9 @@ struct Oper {
     double *d_blocks = nullptr;  // (2K)^2 per block, FP64
     float *d_blocks32 = nullptr; // FP32 copy: per block the high part, then the low part (2 x (2K)^2)
     float *d_blocks_tc = nullptr; // TF32 B operand of the tensor-core tier per block (mw_tc05_layout.h)
+    float *d_blocks_tc2 = nullptr; // ... in the split-TF32 tier's wide layout (tc5_split_wide(K) only)
+    // the operator blocks the split-TF32 tier reads: the wide layout where the kernel uses it
+    const float *split_blocks() const { return d_blocks_tc2 ? d_blocks_tc2 : d_blocks_tc; }
     // the screening tables on the device (bands, block offsets, sub-block norms, amax, xmax, term
     // coefficients), uploaded by the first apply that screens on the GPU (mw_screen.cu)
     void *d_screen = nullptr;
@@ -359,7 +362,7 @@ void k_op_band(int K, const double *W, const double *cc, const double *gx, const
                int ntask, double *nrm, double *head, int *band, double *peak, cudaStream_t s);
 void k_op_blocks(int K, const double *W, const double *cc, const double *gx, const double *gw, const OpBuildTask *tasks,
                  const OpBlockJob *jobs, int njob, cudaStream_t s);
-void k_op_convert(const double *blocks, float *b32, float *btc, long nblocks, int K, int NB, int groups,
+void k_op_convert(const double *blocks, float *b32, float *btc, float *btc2, long nblocks, int K, int NB, int groups,
                   cudaStream_t s);
 // FP32 shadow of whole blocks in cube order cube[Z][Y][X] (X = cx*K + ix): per block a high cube
 // and a low cube (2 * 8K^3 floats, the low one holds the rounded remainder)
@@ -393,7 +396,7 @@ struct ScreenOp {  // one operator's tables (device)
     const double *amax, *xmax, *c;     // [T*S], [T*S], [T]
     const float *amax32, *xmax32;
     const double *b64;                 // blocks in the tier kernels' layouts
-    const float *b32, *btc;
+    const float *b32, *btc, *btc2;
     int T, S;
 };
 struct ScreenJob {  // one job of the apply (device)

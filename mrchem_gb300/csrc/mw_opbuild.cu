@@ -220,8 +220,8 @@ __device__ __forceinline__ float tf32_round(float v) {
     return __uint_as_float(u);
 }
 
-__global__ void op_convert_kernel(const double *blocks, float *b32, float *btc, long nblocks, int K, int NB,
-                                  int groups) {
+__global__ void op_convert_kernel(const double *blocks, float *b32, float *btc, float *btc2, long nblocks, int K,
+                                  int NB, int groups) {
     const int N2 = 2 * K, bsz = N2 * N2;
     const size_t total = (size_t)nblocks * bsz;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
@@ -247,8 +247,14 @@ __global__ void op_convert_kernel(const double *blocks, float *b32, float *btc, 
                 d = blocks[base + (size_t)(n - N2) * N2 + k];
         }
         const float h = tf32_round(__double2float_rn(d));
+        const float l = tf32_round(__double2float_rn(d - (double)h));
         btc[2 * blk * per + rem] = h;
-        btc[2 * blk * per + per + rem] = tf32_round(__double2float_rn(d - (double)h));
+        btc[2 * blk * per + per + rem] = l;
+        if (btc2) {  // the split tier's layout: per k-group its NB hi rows, then its NB lo rows
+            const size_t gb = 2 * blk * per + (size_t)g * 2 * NB * 4 + (size_t)(rem % (NB * 4));
+            btc2[gb] = h;
+            btc2[gb + NB * 4] = l;
+        }
     }
 }
 
@@ -274,10 +280,10 @@ void k_op_blocks(int K, const double *W, const double *cc, const double *gx, con
     MWG_CUDA(cudaGetLastError());
 }
 
-void k_op_convert(const double *blocks, float *b32, float *btc, long nblocks, int K, int NB, int groups,
+void k_op_convert(const double *blocks, float *b32, float *btc, float *btc2, long nblocks, int K, int NB, int groups,
                   cudaStream_t s) {
     if (nblocks <= 0) return;
-    op_convert_kernel<<<1024, 256, 0, s>>>(blocks, b32, btc, nblocks, K, NB, groups);
+    op_convert_kernel<<<1024, 256, 0, s>>>(blocks, b32, btc, btc2, nblocks, K, NB, groups);
     MWG_CUDA(cudaGetLastError());
 }
 

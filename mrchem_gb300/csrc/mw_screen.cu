@@ -630,9 +630,10 @@ __global__ void __launch_bounds__(ST) fill_kernel(ScreenLevel P) {
             } else if (tier == 2 || (tier == 1 && P.tensor)) {
                 // the tensor-core tiers (TF32, and split-TF32 for tier 1 in the tensor modes)
                 P.in[dst] = cd.gen ? (const void *)(P.gtc + P.tx * src) : (const void *)(J.intc + P.tx * src);
-                P.ax[dst] = op.btc + P.tb * bx;
-                P.ay[dst] = op.btc + P.tb * by;
-                P.az[dst] = op.btc + P.tb * bz;
+                const float *bt = tier == 1 ? op.btc2 : op.btc;  // the split tier's operator layout
+                P.ax[dst] = bt + P.tb * bx;
+                P.ay[dst] = bt + P.tb * by;
+                P.az[dst] = bt + P.tb * bz;
             } else {
                 P.in[dst] = cd.gen ? (const void *)(P.g32 + 2 * src * P.bs) : (const void *)(J.in32 + 2 * src * P.bs);
                 P.ax[dst] = op.b32 + 2 * bx * P.bsz;

@@ -17,6 +17,14 @@
 // remainder, value - hi, rounded to TF32 (lo).  The TF32 tier reads hi only; the split-TF32 tier
 // (hi * hi + hi * lo + lo * hi on the tensor cores, the FP32-accuracy tier) reads both, lo at a
 // fixed offset from hi.  Blocks are tc5_x_stride / tc5_b_stride floats apart.
+//
+// Where tc5_split_wide(K) holds, the split tier's operator blocks have a layout of their own with
+// the same size: per k-group the group's N hi rows, then its N lo rows (k-group stride 2 N 16
+// bytes), so that one MMA of width 2N takes B_hi and B_lo side by side (A_hi * B_hi in its first
+// N columns, A_hi * B_lo in the others) and one of width N with the same descriptor reads B_hi
+// alone.  Its TMEM tiles are then 2N columns wide; that is taken only at the orders where it
+// leaves as many CTAs per SM as the three MMAs of width N do (at K = 8 the wide tiles need all
+// 512 columns of an SM, where the narrow kernel fits two CTAs in shared memory and TMEM).
 #pragma once
 
 #include <cstddef>
@@ -34,6 +42,8 @@ MWG_HD constexpr int tc5_kg(int K) { return (2 * K + 3) / 4; }          // k-gro
 MWG_HD constexpr int tc5_ks(int K) { return (tc5_kg(K) + 1) / 2; }      // MMA k-steps of 8
 MWG_HD constexpr size_t tc5_x_floats(int K) { return (size_t)tc5_kg(K) * 4 * (size_t)(2 * K) * (size_t)(2 * K); }
 MWG_HD constexpr size_t tc5_b_floats(int K) { return (size_t)2 * tc5_ks(K) * tc5_n(K) * 4; }
+// the split tier's MMAs of width 2N on the interleaved operator layout (above)
+MWG_HD constexpr bool tc5_split_wide(int K) { return K != 8; }
 // per-block strides of the stored layouts: hi, then lo
 MWG_HD constexpr size_t tc5_x_stride(int K) { return 2 * tc5_x_floats(K); }
 MWG_HD constexpr size_t tc5_b_stride(int K) { return 2 * tc5_b_floats(K); }
