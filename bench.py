@@ -607,13 +607,20 @@ def run(args):
         mw.pin_host(mra, c)
     for r in host_outputs:
         mw.pin_host(mra, r[1])
+    # warm-up steps on the pinned buffers: the first call that overlaps the transfers with the job
+    # groups sizes its staging and stream-ordered allocations
+    for _ in range(max(3, args.warmup)):
+        e2e_step()
     barrier()
     for k in e2e_parts:
         e2e_parts[k] = 0.0
+    e2e_each = []
     t0 = time.perf_counter()
     d2h = 0
     for _ in range(args.e2e_steps):
+        ts = time.perf_counter()
         d2h = e2e_step()
+        e2e_each.append((time.perf_counter() - ts) * 1e3)
     barrier()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps * 1e3, "cuda")
     e2e_v = whole_job_rate(nodes, world, e2e_ms)
@@ -640,31 +647,41 @@ def run(args):
     # kernel uses: three passes, each contracting the (2K)^3 cube of the input block over one
     # dimension with a 2K x 2K operator block: 3 (2K)^4 multiply-adds = 6 (2K)^4 = 96 K^4 flops.
     work_item = 6.0 * (2 * K) ** 4
+    # Every tier kernel sums the x passes of a row (consecutive items of a node with the same term,
+    # ly and lz) and runs the y and z passes once per row: executed cube-pass work is 2 (2K)^4 flops
+    # per item plus 4 (2K)^4 per row.
+    pass_fl = 2.0 * (2 * K) ** 4
     # The tcgen05 tier issues its passes as M128 x N32 x K8 MMAs (mw_apply_tc05.cu's schedule):
-    # ceil(4K^2/128) tiles in the x pass, ceil(5K^2/128) in the y and z passes, ceil(ceil(2K/4)/2)
-    # k-steps each.
+    # ceil(4K^2/128) tiles in the x pass (per item), ceil(5K^2/128) in the y and z passes (per row),
+    # ceil(ceil(2K/4)/2) k-steps each.
     ks = ((2 * K + 3) // 4 + 1) // 2
-    tc_mmas = (-(-4 * K * K // 128) + 2 * -(-5 * K * K // 128)) * ks
-    tc_issued_item = tc_mmas * 2.0 * 128 * (32 if 3 * K > 16 else 16) * 8
+    tc_x_mmas = -(-4 * K * K // 128) * ks
+    tc_yz_mmas = 2 * -(-5 * K * K // 128) * ks
+    mma_fl = 2.0 * 128 * (32 if 3 * K > 16 else 16) * 8
 
     dram_per_item = DRAM_PER_ITEM
     tier_items = {"fp64": st_ser["items_fp64"], "fp32": st_ser["items_fp32"], "tf32": st_ser["items_tf32"],
                   "df32": st_ser["items_df"]}
+    tier_rows = {"fp64": st_ser["rows_fp64"], "fp32": st_ser["rows_fp32"], "tf32": st_ser["rows_tf32"],
+                 "df32": st_ser["rows_df"]}
 
-    def roof(tier, ms, peak, kernel, bound, source, issued_item=None):
-        items = tier_items[tier]
+    def roof(tier, ms, peak, kernel, bound, source, tc_mult=0):
+        items, rows = tier_items[tier], tier_rows[tier]
         sec = ms / 1e3
-        ach = items * work_item / sec / 1e12 if ms > 0 else 0.0
+        executed = items * pass_fl + rows * 2.0 * pass_fl
+        ach = executed / sec / 1e12 if ms > 0 else 0.0
         out = {"bound": bound, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                "frac": ach / peak if peak else None,
-               "work_per_item_flops": work_item,
-               "work_unit": "6 (2K)^4 flops per item: the three cube passes of one (output node, input node, "
-                            "term) contraction",
-               "items": items, "kernel": kernel, "kernel_ms_per_step": ms, "peak_source": source}
-        if issued_item:
-            iss = items * issued_item / sec / 1e12 if ms > 0 else 0.0
-            out.update({"issued_per_item_flops": issued_item, "issued_achieved": iss,
-                        "issued_frac": iss / peak if peak else None})
+               "work_unit": "cube-pass flops executed: 2 (2K)^4 per item (its x pass) + 4 (2K)^4 per row (the y "
+                            "and z passes, once per run of a node's items with the same term, ly and lz)",
+               "items": items, "rows": rows, "executed_flops": executed,
+               "item_equivalent_rate": items * work_item / sec / 1e12 if ms > 0 else 0.0,
+               "item_equivalent_unit": "6 (2K)^4 flops per item (three cube passes per item, as without rows)",
+               "kernel": kernel, "kernel_ms_per_step": ms, "peak_source": source}
+        if tc_mult:
+            mmas = tc_mult * (items * tc_x_mmas + rows * tc_yz_mmas)
+            iss = mmas * mma_fl / sec / 1e12 if ms > 0 else 0.0
+            out.update({"issued_mmas_n32": mmas, "issued_achieved": iss, "issued_frac": iss / peak if peak else None})
         tr = dram_per_item.get(tier)
         out["traffic"] = tr * items if tr is not None else None
         out["traffic_unit"] = "DRAM bytes per step, all launches of the kernel" if tr is not None else None
@@ -683,9 +700,9 @@ def run(args):
         # and k-step A_hi * [B_hi B_lo] (width 64) and A_lo * B_hi (width 32), the issued work of
         # three N = 32 MMAs (hi*hi, hi*lo, lo*hi), 3 x the TF32 tier's
         "fp32": roof("fp32", st_ser["kernel_ms_fp32"], tf32_tf, "apply_tc05_kernel<10,1> (split TF32)", "tensor",
-                     mma_src, issued_item=3 * tc_issued_item),
+                     mma_src, tc_mult=3),
         "tf32": roof("tf32", st_ser["kernel_ms_tf32"], tf32_tf, "apply_tc05_kernel<10,0>", "tensor", mma_src,
-                     issued_item=tc_issued_item),
+                     tc_mult=1),
         # a double-FP32 multiply-add costs about 12 FP32 instructions in this kernel: its ceiling is the
         # FP32 FMA rate / 12 (multiply-adds), i.e. peak flops = FP32 FMA flops / 12
         "df32": roof("df32", st_ser["kernel_ms_df"], fp32_tf / 12.0, "apply_df_kernel<10>",
@@ -737,7 +754,8 @@ def run(args):
                            "policy": "enumeration, screening and item lists on the host cores (mw_ctx_set_screening 0)"},
         "gpu_launches": int(st["launches"]),
         "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "ms_per_step": e2e_ms, **{k: v / args.e2e_steps for k, v in e2e_parts.items()}},
+                "ms_per_step": e2e_ms, "ms_each_step": [round(x, 2) for x in e2e_each],
+                "warmup": max(3, args.warmup), **{k: v / args.e2e_steps for k, v in e2e_parts.items()}},
         "roofline": dict(roofs[dominant], tier=dominant),
         "roofline_tiers": roofs,
         # the whole step against HBM: algorithmic bytes (FP64 blocks of every input and output
@@ -783,7 +801,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="pick the batch's launch settings with mw_apply_batch_autotune before timing")
     ap.add_argument("--cpu-s", type=float, default=12.0,

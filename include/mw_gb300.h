@@ -98,6 +98,12 @@ typedef struct {
     double gpu_post_ms;      /* GPU time of the post-processing (sum over scales, compression, norms),
                                 summed over the job groups, which overlap other groups' levels */
     long long screen_regrows; /* GPU screening: levels walked again after a generation table filled up */
+    long long rows_fp64;      /* rows of the FP64 tier: runs of consecutive items of one node with the
+                                 same term, ly and lz, whose x passes are summed before one y and one
+                                 z pass */
+    long long rows_fp32;      /* ... of the FP32-accuracy tier */
+    long long rows_tf32;      /* ... of the TF32 tier */
+    long long rows_df;        /* ... of the double-FP32 tier */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */

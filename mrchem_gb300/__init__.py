@@ -60,7 +60,8 @@ class Stats(C.Structure):
                 ("kernel_ms_tf32", C.c_double), ("items_df", C.c_longlong), ("flops_df", C.c_double),
                 ("kernel_ms_df", C.c_double), ("host_gen_ms", C.c_double), ("host_launch_ms", C.c_double),
                 ("host_refine_ms", C.c_double), ("gpu_levels_ms", C.c_double), ("gpu_post_ms", C.c_double),
-                ("screen_regrows", C.c_longlong)]
+                ("screen_regrows", C.c_longlong), ("rows_fp64", C.c_longlong), ("rows_fp32", C.c_longlong),
+                ("rows_tf32", C.c_longlong), ("rows_df", C.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -271,7 +271,8 @@ struct LevelItems {
 };
 
 // tier: 0 FP64, 1 FP32 CUDA cores, 2 TF32 tensor cores, 3 double-FP32.  Returns the pinned host copy of the
-// launch's status word (read it after the stream has been synchronised), or nullptr.
+// launch's status word and row count (two ints; read them after the stream has been synchronised),
+// or nullptr when the level has no node in the tier.
 // item arrays written on the GPU by the screening kernels (mw_screen.cu): the tiers one after the
 // other, tier k from base[k]
 struct DevItems {
@@ -353,13 +354,13 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     pk.add(li.coef.data(), nh * sizeof(double));
     pk.add(red.data(), red.size() * sizeof(ReduceTask));
     pk.add(redof.data(), redof.size() * sizeof(int));
-    // the task counter, the status word and the chunk counters start at zero: they travel with the
-    // pack instead of being cleared by separate launches
-    std::vector<int> zeros(2 + red.size(), 0);
+    // the task counter, the status word, the row count and the chunk counters start at zero: they
+    // travel with the pack instead of being cleared by separate launches
+    std::vector<int> zeros(3 + red.size(), 0);
     pk.add(zeros.data(), zeros.size() * sizeof(int));
     pk.ship(ctx, arena);
     int *counter = (int *)pk.ptr(10);
-    int *red_cnt = red.empty() ? nullptr : counter + 2;
+    int *red_cnt = red.empty() ? nullptr : counter + 3;
     ApplyLaunch L;
     L.nnodes = nv;
     L.root = root ? 1 : 0;
@@ -382,6 +383,7 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
     }
     L.counter = counter;
     L.status = counter + 1;
+    L.rows = counter + 2;
     if (!red.empty()) {
         L.red = (const ReduceTask *)pk.ptr(8);
         L.red_of = (const int *)pk.ptr(9);
@@ -399,12 +401,11 @@ int *launch_tier(Ctx &ctx, Arena &arena, LevelItems &li, bool root, bool set, in
             k_apply_tc05(ctx.dbasis, L, tier == 1, ctx.stream);
         else
             k_apply(ctx.dbasis, L, tier, ctx.nsm, ctx.stream);
-        if (tc) {  // the tensor-core kernels wait for bulk copies with a bound
-            hs = (int *)arena.halloc(sizeof(int));
-            *hs = 0;
-            MWG_CUDA(cudaMemcpyAsync(hs, L.status, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
-        }
     }
+    // the status word (the tensor-core kernels wait for bulk copies with a bound) and the row count
+    hs = (int *)arena.halloc(2 * sizeof(int));
+    hs[0] = hs[1] = 0;
+    MWG_CUDA(cudaMemcpyAsync(hs, L.status, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
     return hs;
 }
 
@@ -990,7 +991,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         bool pending = false, done = false;
         LevelItems lt[NTIER];
         cudaEvent_t ev[NTIER + 1];
-        std::vector<int *> status;  // pinned copies of the launches' status words
+        std::vector<std::pair<int, int *>> status;  // per launch: tier, pinned copy of (status, rows)
         std::vector<double *> h_cn;  // pinned staging of each job's component norms
         cudaEvent_t ev_in = nullptr;  // host inputs: the group's input blocks and norms have landed
         double *in_cn = nullptr;      // ... their norms, staged for the host
@@ -1329,7 +1330,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         for (int k = 0; k < NTIER; k++) {
             int *hs = launch_tier(ctx, ar, lt[k], root, false, k, tune.chunk[k], st, dscreen ? &dv : nullptr,
                                   tensor && k == 1);
-            if (hs) G.status.push_back(hs);
+            if (hs) G.status.push_back({k, hs});
             MWG_CUDA(cudaEventRecord(G.ev[k + 1], ctx.stream));
         }
         // norms of the level's output nodes, downloaded into pinned staging
@@ -1367,7 +1368,11 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         ctx.sync();
         auto tR = std::chrono::steady_clock::now();
         st.host_wait_ms += std::chrono::duration<double, std::milli>(tR - tW).count();
-        for (const int *hs : G.status) check_status(hs);
+        for (const auto &ts : G.status) {
+            check_status(ts.second);
+            long long &rows = ts.first == 0 ? st.rows_fp64 : ts.first == 1 ? st.rows_fp32 : ts.first == 2 ? st.rows_tf32 : st.rows_df;
+            rows += ts.second[1];
+        }
         float ms_t[NTIER];
         for (int k = 0; k < NTIER; k++) MWG_CUDA(cudaEventElapsedTime(&ms_t[k], G.ev[k], G.ev[k + 1]));
         kernel_ms += ms_t[0] + ms_t[1] + ms_t[2] + ms_t[3];

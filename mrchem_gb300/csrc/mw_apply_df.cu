@@ -85,9 +85,10 @@ struct DfGeo {
 
 // One CTA per task (output node or chunk), thread (Y', X') owns the output column (Y', X', Z' =
 // 0 .. 2K-1): its node accumulator stays in registers for all of the task's items.  Per item:
-//   x pass, in two halves of Z (the input cube is staged half by half): T1[Z][Y][X'] and u;
-//   y and z passes fused: for each Z the thread forms T2[Z][Y'][X'] (and t2x for Z < K) and adds
-//   c A_z[Z'][Z] T2 to its 2K accumulators at once, so T2 is never stored.
+//   x pass, in two halves of Z (the input cube is staged half by half): T1[Z][Y][X'] and u,
+//   added to the row's earlier items' (same term, ly and lz);
+//   at the row's last item, y and z passes fused: for each Z the thread forms T2[Z][Y'][X'] (and
+//   t2x for Z < K) and adds c A_z[Z'][Z] T2 to its 2K accumulators at once, so T2 is never stored.
 template <int K>
 __global__ void __maxnreg__(DF_MAXREG) apply_df_kernel(ApplyLaunch L) {
     using G = DfGeo<K>;
@@ -113,7 +114,13 @@ __global__ void __maxnreg__(DF_MAXREG) apply_df_kernel(ApplyLaunch L) {
 #pragma unroll
         for (int z = 0; z < N2; z++) acc_h[z] = acc_l[z] = 0.0f;
         const long long b0 = L.begin[w], b1 = L.end[w];
+        int nrows = 0;  // rows of this task
         for (long long j = b0; j < b1; j++) {
+            // rows: items of one term and (ly, lz) (the same A_y and A_z) follow one another in walk
+            // order; their x passes add into T1 and u, and the row's last item runs the y and z passes
+            // once on the sums (every thread reads the same pointers: `last` is uniform)
+            const bool first = j == b0 || L.ay[j - 1] != L.ay[j] || L.az[j - 1] != L.az[j];
+            const bool last = j + 1 == b1 || L.ay[j + 1] != L.ay[j] || L.az[j + 1] != L.az[j];
 #pragma unroll 1
             for (int h = 0; h < 2; h++) {
                 __syncthreads();  // the previous half's x pass, or the previous item, is done with smem
@@ -172,11 +179,19 @@ __global__ void __maxnreg__(DF_MAXREG) apply_df_kernel(ApplyLaunch L) {
                         float th = s0h, tl = s0l;
                         df_add(th, tl, s1h, s1l);
                         const int Z = h * K + z;
-                        s_t1[(Z * N2 + Yp) * N2 + Xp] = df_norm(th, tl);
-                        if (excl && h == 0) s_u[(z * K + Yp) * K + Xp] = df_norm(s1h, s1l);
+                        float2 *t1 = s_t1 + (Z * N2 + Yp) * N2 + Xp;
+                        if (!first) df_add(th, tl, t1->x, t1->y);  // this thread's own earlier value
+                        *t1 = df_norm(th, tl);
+                        if (excl && h == 0) {
+                            float2 *u = s_u + (z * K + Yp) * K + Xp;
+                            if (!first) df_add(s1h, s1l, u->x, u->y);
+                            *u = df_norm(s1h, s1l);
+                        }
                     }
                 }
             }
+            if (!last) continue;
+            nrows++;
             __syncthreads();
             if (active) {  // y and z passes, thread (Y' = Yp, X' = Xp)
                 const float *ayh = s_Ah + NC + Yp * N2, *ayl = s_Al + NC + Yp * N2;
@@ -239,6 +254,7 @@ __global__ void __maxnreg__(DF_MAXREG) apply_df_kernel(ApplyLaunch L) {
             }
         }
         __syncthreads();
+        if (tid == 0 && nrows > 0 && L.rows) atomicAdd(L.rows, nrows);
         finish_chunk(L, w, 8 * K3, &s_redf);
     }
 }

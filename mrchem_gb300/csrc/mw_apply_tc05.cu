@@ -50,7 +50,9 @@
 // MMAs run while the other's warps move data.
 //
 // Rounding: every operand is rounded to TF32 (unit roundoff 2^-11) as in the warp-level MMA
-// version, so an item is off by at most about 6 * 2^-11 * b (b = its screening bound).
+// version, so an item is off by at most about 6 * 2^-11 * b (b = its screening bound).  A row's
+// items share the intermediates' roundings, which are relative to the row's sum: the row is off
+// by at most the sum of its items' bounds, as the items would be one by one.
 //
 // Every wait on an mbarrier is bounded; one that runs out marks the launch failed (status word,
 // reported by the host as MW_ERR_TIMEOUT) and the kernel ends normally, freeing its TMEM.
@@ -356,11 +358,19 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
         const int w = s_node;
         if (w >= L.nnodes) break;
         const long long b0 = L.begin[w], b1 = L.end[w];
+        int nrows = 0;  // rows of this task
         if (issuer && b0 < b1) stage(L.in[b0], L.ax[b0], L.ay[b0], L.az[b0], nitem & 1u);
+        bool acc_on = false;  // the node accumulator holds a row's z pass
         for (long long j = b0; j < b1; j++, nitem++) {
             const uint32_t set = nitem & 1u;
             const uint64_t dBs = dB + (uint64_t)((set * M::BSET) >> 4);
             constexpr uint32_t BPASS = (uint32_t)((M::NP * G::BSZ) >> 4);  // B_x -> B_y -> B_z
+            // rows: a node's items come in walk order (term, then lz, ly, lx), so the items of one
+            // term and (ly, lz), i.e. with the same B_y and B_z, follow one another.  Their x passes
+            // accumulate into D (x is linear), and the row's last item runs the x epilogue and the y
+            // and z passes once, on the sum.  Every thread reads the same pointers: `last` is uniform.
+            const bool first = j == b0 || L.ay[j - 1] != L.ay[j] || L.az[j - 1] != L.az[j];
+            const bool last = j + 1 == b1 || L.ay[j + 1] != L.ay[j] || L.az[j + 1] != L.az[j];
             if (producer) {
                 if (lane == 0) {
                     const bool more = j + 1 < b1;
@@ -372,8 +382,8 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                         naz = L.az[j + 1];
                     }
                     wait(0);  // item j's input block and B operands are in S and B set `set`
-                    issue_pass(dS, G::LBO_S, S_LO, dBs, G::MTX, tD, false, 1);
-                    // the x MMAs, and every earlier MMA (the previous item's z pass), are done:
+                    issue_pass(dS, G::LBO_S, S_LO, dBs, G::MTX, tD, !first, 1);
+                    // the x MMAs, and every earlier MMA (the previous row's z pass), are done:
                     // S and the other B set are free for item j+1
                     wait(1);
                     if (more) stage(nin, nax, nay, naz, set ^ 1u);
@@ -381,9 +391,9 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                 __syncwarp();
             } else {
                 // ---- x epilogue: D row (Z, Y) -> A_y rows (X', Z) and extra rows (X' < K, Z < K), k = Y
-                wait(1);
-                t5_after_sync();
-                t5_epilogue<K, M::WIDE>(tD, G::MTX, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
+                wait(1);  // every item's x MMAs, so that the barrier's phases are waited in order
+                if (last) t5_after_sync();
+                if (last) t5_epilogue<K, M::WIDE>(tD, G::MTX, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
                     if (r >= NN) return;
                     const int Z = r / N2, Y = r - Z * N2;
                     float *base = r_at<K>(sR, 0, Y);
@@ -396,6 +406,8 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                     }
                 });
             }
+            if (!last) continue;
+            nrows++;
             publish();
             if (issuer) issue_pass(dR, G::LBO_R, R_LO, dBs + BPASS, G::MT, tD, false, 2);
             if (!producer) {
@@ -422,7 +434,8 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                 });
             }
             publish();
-            if (issuer) issue_pass(dR, G::LBO_R, R_LO, dBs + 2 * BPASS, G::MT, tACC, j != b0, -1);
+            if (issuer) issue_pass(dR, G::LBO_R, R_LO, dBs + 2 * BPASS, G::MT, tACC, acc_on, -1);
+            acc_on = true;
         }
         // ---- node epilogue: accumulator rows (Y', X'), columns Z' -> component-major FP64 block
         if (b0 < b1 && issuer && !s_fail) t5_commit(&bar[3]);
@@ -467,6 +480,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
         t5_before_sync();
         __syncthreads();
         t5_after_sync();
+        if (tid == 0 && nrows > 0 && L.rows) atomicAdd(L.rows, nrows);
         finish_chunk(L, w, 8 * K3, &s_redf);
     }
     if (s_fail && issuer) {

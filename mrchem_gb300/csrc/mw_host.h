@@ -279,6 +279,7 @@ struct ApplyLaunch {
     const double *coef;           // per item
     int *counter;                 // dynamic node counter (persistent grid); zero at launch
     int *status;                  // 0, or non-zero when a bounded wait of the launch ran out (TF32 tier)
+    int *rows = nullptr;          // rows processed (y and z passes run), summed over the launch's tasks
     // chunked nodes: per task the index of its node's ReduceTask (-1: the task is a whole node),
     // and per ReduceTask a counter of finished chunks (zero at launch).  The CTA that finishes a
     // node's last chunk sums the partials into the node's block (mw_chunks.cuh).

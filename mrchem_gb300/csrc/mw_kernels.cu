@@ -297,6 +297,8 @@ __global__ void __launch_bounds__(128) generate_kernel(DevBasis b, const GenTask
 //   x pass  t1[Z][Y][X'] = sum_X Ax[X'][X] in[Z][Y][X]            (shared)
 //   y pass  t2[Z]        = sum_Y Ay[Y'][Y] t1[Z][Y][X']           (registers)
 //   z pass  acc[Z']     += c sum_Z Az[Z'][Z] t2[Z]
+// Rows: consecutive items with the same Ay, Az (and so the same term and coefficient) add their
+// x passes into t1 and u, and the row's last item runs the y and z passes once on the sums.
 // Below the root scale the all-scaling path (f = 000 -> g = 000) is left out
 // exactly: u holds the wavelet-in-x part of t1 on the scaling octant, and
 // t2x the y pass that avoids the scaling-scaling path, used by g = 000.
@@ -323,7 +325,10 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32) apply_kernel(App
 #pragma unroll
         for (int z = 0; z < N2; z++) acc[z] = T(0);
         const long long b0 = L.begin[w], b1 = L.end[w];
+        int nrows = 0;  // rows of this task
         for (long long j = b0; j < b1; j++) {
+            const bool first = j == b0 || L.ay[j - 1] != L.ay[j] || L.az[j - 1] != L.az[j];
+            const bool last = j + 1 == b1 || L.ay[j + 1] != L.ay[j] || L.az[j + 1] != L.az[j];
             __syncthreads();
             const T *gin = reinterpret_cast<const T *>(L.in[j]);
             for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
@@ -355,10 +360,16 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32) apply_kernel(App
                     for (int X = 0; X < K; X++) s0 += a[X] * src[X];
 #pragma unroll
                     for (int X = K; X < N2; X++) s1 += a[X] * src[X];
-                    s_t1[(Z * N2 + Yp) * N2 + Xp] = s0 + s1;
-                    if (excl && Z < K) s_u[(Z * K + Yp) * K + Xp] = s1;
+                    T *t1 = s_t1 + (Z * N2 + Yp) * N2 + Xp;  // this thread's own entries
+                    *t1 = first ? s0 + s1 : *t1 + (s0 + s1);
+                    if (excl && Z < K) {
+                        T *u = s_u + (Z * K + Yp) * K + Xp;
+                        *u = first ? s1 : *u + s1;
+                    }
                 }
             }
+            if (!last) continue;
+            nrows++;
             __syncthreads();
             if (active) {
                 const T *arow = s_A + NC + Yp * N2;
@@ -407,6 +418,7 @@ __global__ void __launch_bounds__(((4 * K * K + 31) / 32) * 32) apply_kernel(App
             }
         }
         __syncthreads();
+        if (tid == 0 && nrows > 0 && L.rows) atomicAdd(L.rows, nrows);
         finish_chunk(L, w, 8 * K3, &s_redf);
     }
 }
@@ -442,7 +454,8 @@ __device__ __forceinline__ void lds_row(float (&r)[N], const float *p) {
 // few rows of t1T, and hold their two A_y rows in registers; the node
 // accumulator acc[Z'][X'][Y'] lives in shared memory (two CTAs per SM).  Each
 // output's sums run in the same order as in the one-output form.  The FP32
-// partial sum of the node is added once to its FP64 block.
+// partial sum of the node is added once to its FP64 block.  Rows as in
+// apply_kernel: a row's x passes add into t1T and u, its y and z passes run once.
 template <int K>
 __global__ void __launch_bounds__(((2 * K * K + 31) / 32) * 32, 2) apply32_kernel(ApplyLaunch L) {
     constexpr int N2 = 2 * K, NC = N2 * N2, C = NC * N2, K3 = K * K * K, U = ((K3 + 3) / 4) * 4;
@@ -470,7 +483,10 @@ __global__ void __launch_bounds__(((2 * K * K + 31) / 32) * 32, 2) apply32_kerne
         if (w >= L.nnodes) break;
         for (int i = tid; i < C; i += blockDim.x) s_acc[i] = 0.0f;
         const long long b0 = L.begin[w], b1 = L.end[w];
+        int nrows = 0;  // rows of this task
         for (long long j = b0; j < b1; j++) {
+            const bool first = j == b0 || L.ay[j - 1] != L.ay[j] || L.az[j - 1] != L.az[j];
+            const bool last = j + 1 == b1 || L.ay[j + 1] != L.ay[j] || L.az[j + 1] != L.az[j];
             __syncthreads();
             // FP32 input blocks are stored in cube order: a straight 16-byte vector copy
             const float4 *gin4 = reinterpret_cast<const float4 *>(L.in[j]);
@@ -505,11 +521,17 @@ __global__ void __launch_bounds__(((2 * K * K + 31) / 32) * 32, 2) apply32_kerne
                         p1 = fmaf(a0[X], row[X], p1);
                         q1 = fmaf(a1[X], row[X], q1);
                     }
-                    s_t1[(Z * N2 + Xh) * N2 + Yp] = p0 + p1;
-                    s_t1[(Z * N2 + Xh + K) * N2 + Yp] = q0 + q1;
-                    if (excl && Z < K) s_u[(Z * K + Xh) * K + Yp] = p1;
+                    float *t0 = s_t1 + (Z * N2 + Xh) * N2 + Yp, *t1 = s_t1 + (Z * N2 + Xh + K) * N2 + Yp;
+                    *t0 = first ? p0 + p1 : *t0 + (p0 + p1);  // this thread's own entries
+                    *t1 = first ? q0 + q1 : *t1 + (q0 + q1);
+                    if (excl && Z < K) {
+                        float *u = s_u + (Z * K + Xh) * K + Yp;
+                        *u = first ? p1 : *u + p1;
+                    }
                 }
             }
+            if (!last) continue;
+            nrows++;
             __syncthreads();
             if (active) {  // y and z passes
                 float ay0[N2], ay1[N2], t20[N2], t21[N2], t2x[K];
@@ -580,6 +602,7 @@ __global__ void __launch_bounds__(((2 * K * K + 31) / 32) * 32, 2) apply32_kerne
             }
         }
         __syncthreads();
+        if (tid == 0 && nrows > 0 && L.rows) atomicAdd(L.rows, nrows);
         finish_chunk(L, w, 8 * K3, &s_redf);
     }
 }
