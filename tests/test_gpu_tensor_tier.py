@@ -160,3 +160,20 @@ def test_autotune_batch(engine):
     with pytest.raises(engine.MWError):
         engine.autotune_batch([prec] * 5, outs, ops, phis, abs_prec=True, precision="mixed", repeats=1)
     mra.set_overlap(True)
+
+
+def test_row_counts(engine):
+    # every tier kernel sums the x passes of a row (consecutive items of a node with the same term,
+    # ly and lz) before one y and one z pass, and counts its rows: at most one per item, and fewer
+    # rows than items where neighbouring translations survive together
+    prec = 1e-5
+    mra = engine.MultiResolutionAnalysis(9)
+    f = engine.project(prec, engine.FunctionTree(mra), GAUSS, abs_prec=True)
+    H = engine.HelmholtzOperator(mra, 1.1, prec)
+    for precision, main in (("mixed", "tf32"), ("fp64", "fp64"), ("mixed-fp32", "fp32"), ("df", "df")):
+        _, st = run(engine, mra, H, f, prec, precision, True)
+        assert st["items_" + main] > 0, (precision, st)
+        for t in ("fp64", "fp32", "tf32", "df"):
+            items, rows = st["items_" + t], st["rows_" + t]
+            assert (0 < rows <= items) if items else rows == 0, (precision, t, rows, items)
+        assert sum(st["rows_" + t] for t in ("fp64", "fp32", "tf32", "df")) < st["items"], (precision, st)
