@@ -814,8 +814,10 @@ void screen_level_gpu(Ctx &ctx, Arena &ar, DevScreen &ds, const std::vector<JobS
             GenTask *tasks = (GenTask *)ar.alloc(sizeof(GenTask) * (size_t)ngen);
             k_screen_gen_tasks(P, tasks, ngen, ctx.stream);
             const int ggrid = std::min(ngen, 4 * std::max(ctx.nsm, 1));
-            double *gscratch = (double *)ar.alloc(sizeof(double) * generate_scratch_doubles(K) * ggrid);
-            k_generate(ctx.dbasis, tasks, ngen, gscratch, ggrid, ctx.stream);
+            double *gscratch = (K >= 4 && K <= KMAX)
+                                   ? nullptr
+                                   : (double *)ar.alloc(sizeof(double) * generate_scratch_doubles(K) * ggrid);
+            k_generate(ctx.dbasis, tasks, ngen, gscratch, ggrid, ctx.nsm, ctx.stream);
             k_screen_gen_norms32(P, ngen, ctx.stream);
             st.launches += 3;
             st.generated += ngen;

@@ -307,8 +307,9 @@ struct AddTask {
 };
 
 void k_project(const DevBasis &b, const ProjFunc &f, const ProjTask *tasks, int n, cudaStream_t s);
-// scratch: grid x generate_scratch_doubles(K) doubles (one slice per CTA)
-void k_generate(const DevBasis &b, const GenTask *tasks, int n, double *scratch, int grid, cudaStream_t s);
+// K = 4 .. 10: generate_kernel_t<K> (shared memory, scratch unused); other K: scratch holds
+// grid x generate_scratch_doubles(K) doubles (one slice per CTA)
+void k_generate(const DevBasis &b, const GenTask *tasks, int n, double *scratch, int grid, int nsm, cudaStream_t s);
 inline size_t generate_scratch_doubles(int K) {
     return (size_t)4 * K * K * K + (size_t)2 * K * K * K + (size_t)K * K * K;
 }

@@ -291,6 +291,108 @@ __global__ void __launch_bounds__(128) generate_kernel(DevBasis b, const GenTask
     }
 }
 
+// The same generation with K known at compile time: the filter matrix and the three
+// intermediates in shared memory (56 KB at K = 10, four CTAs per SM), the loops unrolled.  The
+// sums run in the same order as in generate_kernel, so the blocks and norms are identical.
+template <int K>
+__global__ void __launch_bounds__(256) generate_kernel_t(DevBasis b, const GenTask *tasks, int n) {
+    constexpr int N2 = 2 * K, K3 = K * K * K, KK = K * K;
+    extern __shared__ double gsm[];
+    double *wt = gsm;                // W^T rows (c K + x) of length 2K, as b.WT
+    double *t1 = wt + N2 * N2;       // t1[Z][Y][x] (first step) or t1[z][y][x']
+    double *t2 = t1 + N2 * N2 * K;   // t2[Z][y][x] (first step) or t2[z][y'][x]
+    double *sc = t2 + N2 * KK;       // s[z][y][x]
+    __shared__ double s_red[8];
+    for (int i = threadIdx.x; i < N2 * N2; i += blockDim.x) wt[i] = b.WT[i];
+    __syncthreads();
+    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+        const GenTask task = tasks[t];
+        for (int s = 0; s < task.steps; s++) {
+            const int c = (int)((task.path >> (3 * s)) & 7);
+            const double *wx = wt + (c & 1) * K * N2, *wy = wt + ((c >> 1) & 1) * K * N2,
+                         *wz = wt + ((c >> 2) & 1) * K * N2;
+            if (s == 0) {
+                for (int i = threadIdx.x; i < N2 * N2 * K; i += blockDim.x) {
+                    const int x = i % K, YZ = i / K, Y = YZ % N2, Z = YZ / N2;
+                    const int cyz = ((Y >= K) ? 2 : 0) | ((Z >= K) ? 4 : 0);
+                    const double *row = task.anc + (Z % K) * KK + (Y % K) * K;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int X = 0; X < N2; X++) acc += wx[x * N2 + X] * row[(cyz | (X >= K ? 1 : 0)) * K3 + (X % K)];
+                    t1[i] = acc;
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < N2 * KK; i += blockDim.x) {
+                    const int x = i % K, y = (i / K) % K, Z = i / KK;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int Y = 0; Y < N2; Y++) acc += wy[y * N2 + Y] * t1[(Z * N2 + Y) * K + x];
+                    t2[i] = acc;
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                    const int xy = i % KK, z = i / KK;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int Z = 0; Z < N2; Z++) acc += wz[z * N2 + Z] * t2[Z * KK + xy];
+                    sc[i] = acc;
+                }
+            } else {
+                for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                    const int x = i % K, zy = i / K;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int X = 0; X < K; X++) acc += wx[x * N2 + X] * sc[zy * K + X];
+                    t1[i] = acc;
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                    const int x = i % K, y = (i / K) % K, z = i / KK;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int Y = 0; Y < K; Y++) acc += wy[y * N2 + Y] * t1[(z * K + Y) * K + x];
+                    t2[i] = acc;
+                }
+                __syncthreads();
+                for (int i = threadIdx.x; i < K3; i += blockDim.x) {
+                    const int xy = i % KK, z = i / KK;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int Z = 0; Z < K; Z++) acc += wz[z * N2 + Z] * t2[Z * KK + xy];
+                    sc[i] = acc;
+                }
+            }
+            __syncthreads();
+        }
+        double ss = 0.0;
+        for (int i = threadIdx.x; i < 8 * K3; i += blockDim.x) {
+            const double v = i < K3 ? sc[i] : 0.0;
+            task.out[i] = v;
+            ss += v * v;
+        }
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = ss;
+        __syncthreads();
+        if (threadIdx.x < 8) {
+            double tot = 0.0;
+            if (threadIdx.x == 0)
+                for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += s_red[w];
+            task.cn[threadIdx.x] = threadIdx.x == 0 ? sqrt(tot) : 0.0;
+        }
+        __syncthreads();
+    }
+}
+
+template <int K>
+void launch_generate_t(const DevBasis &b, const GenTask *tasks, int n, int nsm, cudaStream_t s) {
+    constexpr int N2 = 2 * K;
+    constexpr size_t smem = sizeof(double) * ((size_t)N2 * N2 + (size_t)N2 * N2 * K + (size_t)N2 * K * K + (size_t)K * K * K);
+    MWG_CUDA(cudaFuncSetAttribute(generate_kernel_t<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = std::min(n, 4 * std::max(nsm, 1));
+    generate_kernel_t<K><<<grid, 256, smem, s>>>(b, tasks, n);
+    MWG_CUDA(cudaGetLastError());
+}
+
 // ----------------------------------------------------------------- NS-form apply
 // One CTA per output node (persistent grid, dynamic node counter).  Thread
 // (Yp, Xp) owns the output column cube[:, Yp, Xp] in registers.  Per item:
@@ -795,8 +897,18 @@ void k_project(const DevBasis &b, const ProjFunc &f, const ProjTask *tasks, int 
     MWG_CUDA(cudaGetLastError());
 }
 
-void k_generate(const DevBasis &b, const GenTask *tasks, int n, double *scratch, int grid, cudaStream_t s) {
+void k_generate(const DevBasis &b, const GenTask *tasks, int n, double *scratch, int grid, int nsm, cudaStream_t s) {
     if (n <= 0) return;
+    switch (b.K) {
+        case 4: launch_generate_t<4>(b, tasks, n, nsm, s); return;
+        case 5: launch_generate_t<5>(b, tasks, n, nsm, s); return;
+        case 6: launch_generate_t<6>(b, tasks, n, nsm, s); return;
+        case 7: launch_generate_t<7>(b, tasks, n, nsm, s); return;
+        case 8: launch_generate_t<8>(b, tasks, n, nsm, s); return;
+        case 9: launch_generate_t<9>(b, tasks, n, nsm, s); return;
+        case 10: launch_generate_t<10>(b, tasks, n, nsm, s); return;
+        default: break;
+    }
     generate_kernel<<<grid, 128, 0, s>>>(b, tasks, n, scratch);
     MWG_CUDA(cudaGetLastError());
 }

@@ -481,37 +481,64 @@ __global__ void __launch_bounds__(ST) screen_kernel(ScreenLevel P, int maxT, int
                 }
             }
         } else {
-            // two walks of the row: count its items, then write them at their place in walk order
+            // two walks of the row: screen and count its items, then write them at their place in
+            // walk order.  Rows of at most 32 translations keep the first walk's survivors and tiers
+            // in bit masks, so that the second walk only looks the inputs up again
             int c = 0;
+            const int xlo = max(-L, wlo[0]), xhi = min(L, whi[0]);
+            const bool keep = xhi - xlo < 32;
+            unsigned surv = 0u;
+            unsigned long long tiers = 0ull;
             if (live)
-                for (int lx = max(-L, wlo[0]); lx <= min(L, whi[0]); lx++) {
+                for (int lx = xlo; lx <= xhi; lx++) {
                     const int p[3] = {nd.l[0] - lx, nd.l[1] - ly, nd.l[2] - lz};
+                    const double *nx = op.norms + 4 * (size_t)(ob + lx);
                     Item it;
-                    if (final_item(P, J, nd, p, lx, ly, lz, op.norms + 4 * (size_t)(ob + lx),
-                                   op.norms32 + 4 * (size_t)(ob + lx), rw, it))
-                        c++;
+                    if (!final_item(P, J, nd, p, lx, ly, lz, nx, op.norms32 + 4 * (size_t)(ob + lx), rw, it)) continue;
+                    c++;
+                    if (keep) {
+                        surv |= 1u << (lx - xlo);
+                        tiers |= (unsigned long long)it.tier << (2 * (lx - xlo));
+                    }
+                    atomicAdd(&s_cnt[it.tier], 1);
+                    atomicAdd(&s_cnt[4 + it.tier], item_pairs_d(nx, rw.ny, rw.nz, it.cn, P.root != 0));
                 }
             unsigned total;
             const int pos = (int)block_scan<unsigned>((unsigned)c, wsum, &total);
             if (live && c > 0) {
                 int k = 0;
-                for (int lx = max(-L, wlo[0]); lx <= min(L, whi[0]); lx++) {
-                    const int p[3] = {nd.l[0] - lx, nd.l[1] - ly, nd.l[2] - lz};
-                    const double *nx = op.norms + 4 * (size_t)(ob + lx);
-                    Item it;
-                    if (!final_item(P, J, nd, p, lx, ly, lz, nx, op.norms32 + 4 * (size_t)(ob + lx), rw, it)) continue;
-                    const int tier = it.tier;
+                auto put = [&](int lx, int src, int gen, int tier) {
                     ScreenCand &cd = P.cand[base + written + pos + k];
-                    cd.src = it.src;
+                    cd.src = src;
                     cd.lx = (short)lx;
                     cd.ly = (short)ly;
                     cd.lz = (short)lz;
                     cd.tier = (unsigned char)tier;
-                    cd.gen = (unsigned char)it.gen;
+                    cd.gen = (unsigned char)gen;
                     cd.t = t;
-                    atomicAdd(&s_cnt[tier], 1);
-                    atomicAdd(&s_cnt[4 + tier], item_pairs_d(nx, rw.ny, rw.nz, it.cn, P.root != 0));
                     k++;
+                };
+                if (keep) {
+                    for (unsigned m = surv; m; m &= m - 1) {
+                        const int bit = __ffs(m) - 1, lx = xlo + bit;
+                        const int p[3] = {nd.l[0] - lx, nd.l[1] - ly, nd.l[2] - lz};
+                        // the input as final_item found it: a node of the input tree, or a generated slot
+                        int src = hash_find(J, P.n, p[0], p[1], p[2]), gen = 0;
+                        if (src < 0) {
+                            src = gen_find(P, nd, p);
+                            gen = 1;
+                        }
+                        put(lx, src, gen, (int)((tiers >> (2 * bit)) & 3ull));
+                    }
+                } else {
+                    for (int lx = xlo; lx <= xhi; lx++) {
+                        const int p[3] = {nd.l[0] - lx, nd.l[1] - ly, nd.l[2] - lz};
+                        Item it;
+                        if (!final_item(P, J, nd, p, lx, ly, lz, op.norms + 4 * (size_t)(ob + lx),
+                                        op.norms32 + 4 * (size_t)(ob + lx), rw, it))
+                            continue;
+                        put(lx, it.src, it.gen, it.tier);
+                    }
                 }
             }
             written += total;

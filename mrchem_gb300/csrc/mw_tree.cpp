@@ -416,8 +416,10 @@ void generate_all(const std::vector<std::pair<GenSet *, const Tree *>> &sets, Ar
     pk.add(tasks.data(), tasks.size() * sizeof(GenTask));
     pk.ship(ctx, arena);
     const int ggrid = (int)std::min<long>(total, 4L * std::max(ctx.nsm, 1));
-    double *gscratch = (double *)arena.alloc(sizeof(double) * generate_scratch_doubles(ctx.basis.K) * ggrid);
-    k_generate(ctx.dbasis, (const GenTask *)pk.ptr(0), (int)total, gscratch, ggrid, ctx.stream);
+    const int K = ctx.basis.K;
+    double *gscratch =
+        (K >= 4 && K <= KMAX) ? nullptr : (double *)arena.alloc(sizeof(double) * generate_scratch_doubles(K) * ggrid);
+    k_generate(ctx.dbasis, (const GenTask *)pk.ptr(0), (int)total, gscratch, ggrid, ctx.nsm, ctx.stream);
     if (st) {
         st->launches++;
         st->generated += total;
