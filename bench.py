@@ -15,6 +15,7 @@ p_i a random cubic (20 N(0,1) coefficients), a_i log-uniform in [0.3, 20], R_i u
 available to build) on the same metric.
 """
 import argparse
+import gc
 import json
 import math
 import os
@@ -559,6 +560,9 @@ def run(args):
         for _ in range(args.warmup):
             step("mixed", outs)
         barrier()
+        # the interpreter's cyclic collector runs before the timed steps, not inside them
+        gc.collect()
+        gc.disable()
         clk.mark(True)
         start.record()
         for _ in range(args.steps):
@@ -566,6 +570,7 @@ def run(args):
         end.record()
         barrier()
         clk.mark(False)
+        gc.enable()
     ms = start.elapsed_time(end) / args.steps
     nodes = stats[-1]["out_nodes"]
     errs = [rel_err(o, r) for o, r in zip(outs, ref)]
@@ -615,6 +620,8 @@ def run(args):
     for k in e2e_parts:
         e2e_parts[k] = 0.0
     e2e_each = []
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     d2h = 0
     for _ in range(args.e2e_steps):
@@ -622,6 +629,7 @@ def run(args):
         d2h = e2e_step()
         e2e_each.append((time.perf_counter() - ts) * 1e3)
     barrier()
+    gc.enable()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps * 1e3, "cuda")
     e2e_v = whole_job_rate(nodes, world, e2e_ms)
 

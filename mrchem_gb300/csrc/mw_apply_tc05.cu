@@ -10,7 +10,8 @@
 // as three GEMMs D[M x N] = A[M x 8k] B[N x 8k]^T of tcgen05.mma.kind::tf32 with M = 128,
 // N = 32 (16 for K <= 5) and FP32 accumulation in tensor memory (TMEM).  The rows of a pass are
 // its (2K)^2 index pairs, padded to whole tiles of 128; the columns are the 2K output indices.
-// One thread issues the MMAs of a pass and commits them to an mbarrier; eight warps then read
+// One thread issues the MMAs of a pass and commits them to an mbarrier; eight warps (sixteen in
+// the split kernel where it has an SM to itself) then read
 // the result out of TMEM (tcgen05.ld, one row per thread), round it to TF32 (cvt.rna) and store
 // it as the A operand of the next pass.  The z pass accumulates into a second TMEM region that
 // holds the output node for all of its items and is written to the FP64 block once.
@@ -90,8 +91,6 @@ struct T5Geo {
     static constexpr int SMEM = OB + 6 * BSZ;
     static constexpr int TMEM_COLS = 2 * MT * N <= 32 ? 32 : (2 * MT * N <= 64 ? 64 : (2 * MT * N <= 128 ? 128 : 256));
     static constexpr uint32_t STAGE_BYTES = (uint32_t)(SX + 3 * BSZ);
-    static constexpr int EPI_WARPS = 8;                 // warps that read TMEM and store operands
-    static constexpr int THREADS = 32 * EPI_WARPS + 32; // + one warp that issues copies and MMAs
     // dynamic shared memory requested at launch: at least enough that no more CTAs share an SM
     // than its 512 TMEM columns serve (an allocation beyond them would wait for another CTA)
     static constexpr int MAX_CTAS = 512 / TMEM_COLS;
@@ -145,6 +144,14 @@ struct T5Mem {
                                                                    : 512;
     static_assert(!SPLIT || tc5_split_wide(K) == (fits(WIDE_COLS) >= fits(G::TMEM_COLS)),
                   "tc5_split_wide: the wide tiles exactly where they keep the CTAs per SM");
+    // epilogue warps: where the split kernel has an SM to itself (its shared memory admits one CTA)
+    // sixteen, one TMEM tile quarter each per pass, so that its epilogues take half as long; else
+    // eight (two CTAs per SM overlap one CTA's epilogues with the other's MMAs).  Warp w reads
+    // lane quarter w % 4 of tiles w / 4, w / 4 + TS, ...
+    static constexpr int EPI_WARPS = (SPLIT && SMEM > 114 * 1024) ? 16 : 8;
+    static constexpr int TS = EPI_WARPS / 4;
+    static constexpr int THREADS = 32 * EPI_WARPS + 32;  // + one warp that issues copies and MMAs
+    static_assert(!(SPLIT && SMEM > 114 * 1024) || THREADS * 120 <= 65536, "registers for one CTA");
     static constexpr int SMEM_FLOOR = 228 * 1024 / (MAX_CTAS + 1);
     static constexpr int SMEM_LAUNCH = !SPLIT ? G::SMEM_LAUNCH : (MAX_CTAS >= 8 || SMEM >= SMEM_FLOOR ? SMEM : SMEM_FLOOR);
     static_assert(SPLIT || (OR == G::OR && OB == G::OB && SMEM == G::SMEM && STAGE_BYTES == G::STAGE_BYTES),
@@ -232,12 +239,12 @@ __device__ __forceinline__ float *r_at(uint8_t *R, int r, int k) {
     return reinterpret_cast<float *>(R + (k >> 2) * T5Geo<K>::LBO_R + 16 * r + 4 * (k & 3));
 }
 
-// the epilogue of one pass for the TMEM tiles of this warp (tiles half, half + 2, ... < tiles);
+// the epilogue of one pass for the TMEM tiles of this warp (tiles half, half + TS, ... < tiles);
 // WIDE: a tile is 2N columns wide and a row's value is the sum of its two halves
-template <int K, bool WIDE, class Row>
+template <int K, bool WIDE, int TS, class Row>
 __device__ __forceinline__ void t5_epilogue(uint32_t tcol, int tiles, int q, int half, int lane, Row row) {
     constexpr int N = T5Geo<K>::N, NT = WIDE ? 2 * N : N;
-    for (int i = half; i < tiles; i += 2) {
+    for (int i = half; i < tiles; i += TS) {
         uint32_t a[32];
         const uint32_t t = tcol + ((uint32_t)(32 * q) << 16) + (uint32_t)(i * NT);
         t5_ld<K>(t, a);
@@ -254,7 +261,7 @@ __device__ __forceinline__ void t5_epilogue(uint32_t tcol, int tiles, int q, int
 }
 
 template <int K, int SPLIT>
-__global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_kernel(ApplyLaunch L) {
+__global__ void __launch_bounds__(T5Mem<K, SPLIT>::THREADS, SPLIT ? 1 : 2) apply_tc05_kernel(ApplyLaunch L) {
     using G = T5Geo<K>;
     using M = T5Mem<K, SPLIT>;
     constexpr int N2 = G::N2, NN = G::NN, KK = G::KK, K3 = G::K3, N = G::N;
@@ -273,9 +280,9 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
     __shared__ int s_node, s_redf;
     __shared__ volatile int s_fail;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const bool producer = warp == G::EPI_WARPS;  // copies and MMAs (lane 0)
+    const bool producer = warp == M::EPI_WARPS;  // copies and MMAs (lane 0)
     const bool issuer = producer && lane == 0;
-    const int q = warp & 3, half = warp >> 2;  // epilogue warps: TMEM lane quarter, tile parity
+    const int q = warp & 3, half = warp >> 2;  // epilogue warps: TMEM lane quarter, first tile
     const bool excl = !L.root;
 
     // zero everything once: padding rows, columns and k-groups are read by the MMAs
@@ -393,7 +400,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                 // ---- x epilogue: D row (Z, Y) -> A_y rows (X', Z) and extra rows (X' < K, Z < K), k = Y
                 wait(1);  // every item's x MMAs, so that the barrier's phases are waited in order
                 if (last) t5_after_sync();
-                if (last) t5_epilogue<K, M::WIDE>(tD, G::MTX, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
+                if (last) t5_epilogue<K, M::WIDE, M::TS>(tD, G::MTX, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
                     if (r >= NN) return;
                     const int Z = r / N2, Y = r - Z * N2;
                     float *base = r_at<K>(sR, 0, Y);
@@ -415,7 +422,7 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                 const float cf = float(L.coef[j]);
                 wait(2);
                 t5_after_sync();
-                t5_epilogue<K, M::WIDE>(tD, G::MT, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
+                t5_epilogue<K, M::WIDE, M::TS>(tD, G::MT, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
                     if (r < NN) {
                         const int xp = r / N2, Z = r - xp * N2;
                         float *base = r_at<K>(sR, 0, Z);
@@ -471,10 +478,10 @@ __global__ void __launch_bounds__(T5Geo<K>::THREADS, SPLIT ? 1 : 2) apply_tc05_k
                 }
             };
             if (b0 < b1) {
-                t5_epilogue<K, M::WIDE>(tACC, G::MT, q, half, lane, row);
+                t5_epilogue<K, M::WIDE, M::TS>(tACC, G::MT, q, half, lane, row);
             } else {
                 uint32_t zero[32] = {};
-                for (int i = half; i < G::MT; i += 2) row(i * 128 + 32 * q + lane, zero);
+                for (int i = half; i < G::MT; i += M::TS) row(i * 128 + 32 * q + lane, zero);
             }
         }
         t5_before_sync();
@@ -506,7 +513,7 @@ void launch_tc05(const ApplyLaunch &L, cudaStream_t s) {
                                   M::SMEM_LAUNCH));
     const int grid = L.nnodes;
     if (grid < 1) return;
-    apply_tc05_kernel<K, SPLIT><<<grid, G::THREADS, M::SMEM_LAUNCH, s>>>(L);
+    apply_tc05_kernel<K, SPLIT><<<grid, M::THREADS, M::SMEM_LAUNCH, s>>>(L);
     MWG_CUDA(cudaGetLastError());
 }
 

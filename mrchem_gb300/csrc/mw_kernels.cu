@@ -94,21 +94,23 @@ __device__ void store_block(double *g, const double *cube, int K) {
 }
 
 // 8 component norms of a block in global memory; deterministic fixed-order reduction
+// the 8 component norms of a block: per thread strided sums of squares, a butterfly sum per warp,
+// then the warps' sums in warp order (blockDim a multiple of 32; red holds 8 x warps doubles)
 __device__ void block_norms(const double *g, double *cn, int K, double *red) {
-    int K3 = K * K * K;
-    int nt = blockDim.x;
+    const int K3 = K * K * K, nt = blockDim.x, nw = nt >> 5, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int c = 0; c < 8; c++) {
         double s = 0.0;
         for (int i = threadIdx.x; i < K3; i += nt) {
-            double v = g[c * K3 + i];
+            const double v = g[c * K3 + i];
             s += v * v;
         }
-        red[c * nt + threadIdx.x] = s;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[c * nw + w] = s;
     }
     __syncthreads();
     if (threadIdx.x < 8) {
         double s = 0.0;
-        for (int i = 0; i < nt; i++) s += red[threadIdx.x * nt + i];
+        for (int i = 0; i < nw; i++) s += red[threadIdx.x * nw + i];
         cn[threadIdx.x] = sqrt(s);
     }
     __syncthreads();
