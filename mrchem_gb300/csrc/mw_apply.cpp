@@ -1662,6 +1662,7 @@ struct MulState {
     GenSet ga, gb;
     std::vector<MulTask> tasks;  // this level's node tasks
     std::vector<double> crit;    // ... and their max-norm criteria
+    std::vector<const float2 *> va, vb;  // ... their inputs' cached value cubes (nullptr: none)
 };
 
 }  // namespace
@@ -1707,11 +1708,62 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
         for (int i = 0; i < out.nn(); i++)
             if (out.nodes[i].child0 < 0) s.work.push_back(i);
     }
+    // The node kernel works from the inputs' value cubes (mw_multiply_df.cu).  An input tree that
+    // feeds several products gets the value cube of every node once, up front (stream-ordered
+    // allocation, freed at the end); the other inputs' blocks at a level's nodes (generated ones,
+    // nodes of trees used once) get theirs per level.
+    const size_t VS = mul_value_floats(bsis.K);
+    std::vector<std::pair<const Tree *, float2 *>> vcache;
+    std::vector<const double *> cblk;  // the cached trees' blocks and their value cubes, computed
+    std::vector<float2 *> cval;        // with the first level's launches (its pack, its arena)
+    {
+        std::vector<const Tree *> order;
+        std::unordered_map<const Tree *, int> uses;
+        for (auto &j : jobs)
+            for (const Tree *t : {j.a, j.b})
+                if (uses[t]++ == 0) order.push_back(t);
+        size_t bytes = 0;
+        for (const Tree *t : order)
+            if (uses[t] >= 2) bytes += sizeof(float) * VS * (size_t)t->nn();
+        size_t free_b = 0, total_b = 0;
+        MWG_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        if (bytes > 0 && bytes <= free_b / 4) {
+            for (const Tree *t : order) {
+                if (uses[t] < 2) continue;
+                float2 *p = nullptr;
+                MWG_CUDA(cudaMallocAsync(&p, sizeof(float) * VS * (size_t)t->nn(), ctx.stream));
+                vcache.push_back({t, p});
+                for (int i = 0; i < t->nn(); i++) {
+                    cblk.push_back(t->block(i));
+                    cval.push_back(p + (VS / 2) * (size_t)i);
+                }
+            }
+        }
+    }
+    auto cached = [&](const Tree *t) -> float2 * {
+        for (auto &c : vcache)
+            if (c.first == t) return c.second;
+        return nullptr;
+    };
+    for (auto &s : ms) {
+        s.va.clear();
+        s.vb.clear();
+    }
     while (true) {
         bool any = false;
         for (auto &s : ms) any |= !s.work.empty();
         if (!any) break;
         arena.reset();
+        if (!cblk.empty()) {  // the cached value cubes, ahead of the first level's launches
+            Packer pc;
+            pc.add(cblk.data(), cblk.size() * sizeof(const double *));
+            pc.add(cval.data(), cval.size() * sizeof(float2 *));
+            pc.ship(ctx, arena);
+            k_values_df(ctx.dbasis, (const double *const *)pc.ptr(0), (float2 *const *)pc.ptr(1), (int)cblk.size(),
+                        ctx.nsm, ctx.stream);
+            st.launches++;
+            cblk.clear();
+        }
         auto tA = clk::now();
         // input blocks to generate at this level's output nodes (jobs in parallel: each has its own
         // sets and reads its shared input trees only)
@@ -1744,9 +1796,14 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
             Tree &out = *s.job->out, &a = *s.job->a, &b = *s.job->b;
             s.tasks.resize(s.work.size());
             s.crit.assign(s.work.size(), 0.0);
+            s.va.assign(s.work.size(), nullptr);
+            s.vb.assign(s.work.size(), nullptr);
+            float2 *ca = cached(&a), *cb = cached(&b);
             for (size_t w = 0; w < s.work.size(); w++) {
                 const NodeInfo &o = out.nodes[s.work[w]];
                 int ia = a.find(o.n, o.l), ib = b.find(o.n, o.l);
+                if (ca && ia >= 0) s.va[w] = ca + (VS / 2) * (size_t)ia;
+                if (cb && ib >= 0) s.vb[w] = cb + (VS / 2) * (size_t)ib;
                 MulTask &tk = s.tasks[w];
                 tk.a = block_at(a, s.ga, s.ga.base, o.n, o.l);
                 tk.b = block_at(b, s.gb, s.gb.base, o.n, o.l);
@@ -1763,14 +1820,53 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
                 }
             }
         }
-        std::vector<MulTask> tasks;
-        for (auto &s : ms) tasks.insert(tasks.end(), s.tasks.begin(), s.tasks.end());
+        // the level's inputs without a cached value cube get theirs into level scratch: per job
+        // its count, then the blocks and the value pointers in job order
+        std::vector<size_t> voff(ms.size() + 1, 0), toff(ms.size() + 1, 0);
+        for (size_t j = 0; j < ms.size(); j++) {
+            size_t c = 0;
+            for (size_t w = 0; w < ms[j].tasks.size(); w++) c += (ms[j].va[w] ? 0 : 1) + (ms[j].vb[w] ? 0 : 1);
+            voff[j + 1] = voff[j] + c;
+            toff[j + 1] = toff[j] + ms[j].tasks.size();
+        }
+        const size_t nv = voff.back(), nt = toff.back();
+        float2 *lvals = nv ? (float2 *)arena.alloc(sizeof(float) * VS * nv) : nullptr;
+        std::vector<const double *> vblk(nv);
+        std::vector<float2 *> vdst(nv);
+        std::vector<MulVTask> tasks(nt);
+#pragma omp parallel for schedule(dynamic, 4)
+        for (long j = 0; j < (long)ms.size(); j++) {
+            MulState &s = ms[j];
+            size_t k = voff[j];
+            for (size_t w = 0; w < s.tasks.size(); w++) {
+                const MulTask &tk = s.tasks[w];
+                MulVTask &vt = tasks[toff[j] + w];
+                auto value_of = [&](const float2 *v, const double *blk) -> const float2 * {
+                    if (v) return v;
+                    vblk[k] = blk;
+                    vdst[k] = lvals + (VS / 2) * k;
+                    return vdst[k++];
+                };
+                vt.a = value_of(s.va[w], tk.a);
+                vt.b = value_of(s.vb[w], tk.b);
+                vt.out = tk.out;
+                vt.cn = tk.cn;
+                vt.scale = tk.scale;
+            }
+        }
         st.host_items_ms += since(tC);
         auto tD = clk::now();
         Packer pk;
-        pk.add(tasks.data(), tasks.size() * sizeof(MulTask));
+        pk.add(tasks.data(), tasks.size() * sizeof(MulVTask));
+        pk.add(vblk.data(), vblk.size() * sizeof(const double *));
+        pk.add(vdst.data(), vdst.size() * sizeof(float2 *));
         pk.ship(ctx, arena);
-        k_multiply_df(ctx.dbasis, (const MulTask *)pk.ptr(0), (int)tasks.size(), ctx.nsm, ctx.stream);
+        if (nv) {
+            k_values_df(ctx.dbasis, (const double *const *)pk.ptr(1), (float2 *const *)pk.ptr(2), (int)nv, ctx.nsm,
+                        ctx.stream);
+            st.launches++;
+        }
+        k_multiply_values_df(ctx.dbasis, (const MulVTask *)pk.ptr(0), (int)tasks.size(), ctx.nsm, ctx.stream);
         st.launches++;
         st.out_nodes += (long long)tasks.size();
         // the norms of the nodes computed at this level (each job's index range: the children
@@ -1842,6 +1938,7 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
         st.host_refine_ms += since(tE);
         st.levels++;
     }
+    for (auto &c : vcache) MWG_CUDA(cudaFreeAsync(c.second, ctx.stream));
     std::vector<Tree *> outs;
     for (auto &j : jobs) outs.push_back(j.out);
     arena.reset();

@@ -340,7 +340,17 @@ void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int
 void k_topdown_df(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s);
 void k_compress_df(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s);
 // the multiply's node kernel (mw_multiply_df.cu): double-FP32 transforms, FP64 blocks in and out
-void k_multiply_df(const DevBasis &b, const MulTask *tasks, int n, int nsm, cudaStream_t s);
+// the tree multiply split at its values (mw_multiply_df.cu): value cubes of blocks (2 (2K)^3 floats
+// each, (hi, lo) pairs in cube order), and nodes from two value cubes
+struct MulVTask {
+    const float2 *a, *b;  // value cubes of the inputs at the node
+    double *out;
+    double *cn;
+    double scale;         // coef * 2^{3(n+1)/2}
+};
+size_t mul_value_floats(int K);
+void k_values_df(const DevBasis &b, const double *const *blocks, float2 *const *vals, int n, int nsm, cudaStream_t s);
+void k_multiply_values_df(const DevBasis &b, const MulVTask *tasks, int n, int nsm, cudaStream_t s);
 // dst[off[r] ..] = the len[r] doubles at src[r], for n ranges (one download of many small arrays)
 void k_gather_ranges(const double *const *src, const long long *off, const int *len, int n, double *dst,
                      cudaStream_t s);
