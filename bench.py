@@ -809,7 +809,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
                     help="pick the batch's launch settings with mw_apply_batch_autotune before timing")
     ap.add_argument("--cpu-s", type=float, default=12.0,

@@ -1659,7 +1659,9 @@ struct MulState {
     const std::vector<double> *ta = nullptr, *tb = nullptr;  // the inputs' detail tails (useMaxNorms)
     std::vector<int> work;
     int iter = 0;
-    GenSet ga, gb;
+    int tia = 0, tib = 0;                  // the inputs' indices among the batch's distinct trees
+    std::vector<Key> ra, rb;               // this level's missing input nodes of a and b ...
+    std::vector<int> aa, ab;               // ... and their leaf ancestors
     std::vector<MulTask> tasks;  // this level's node tasks
     std::vector<double> crit;    // ... and their max-norm criteria
     std::vector<const float2 *> va, vb;  // ... their inputs' cached value cubes (nullptr: none)
@@ -1749,6 +1751,25 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
         s.va.clear();
         s.vb.clear();
     }
+    // the batch's distinct input trees and, per tree, the (job, side) pairs that read it: a block
+    // missing from a tree is generated once per level however many products need it
+    std::vector<const Tree *> dtrees;
+    std::vector<std::vector<std::pair<int, int>>> readers;
+    {
+        std::unordered_map<const Tree *, int> tix;
+        for (size_t j = 0; j < ms.size(); j++)
+            for (int side = 0; side < 2; side++) {
+                const Tree *t = side ? jobs[j].b : jobs[j].a;
+                auto it = tix.emplace(t, (int)dtrees.size());
+                if (it.second) {
+                    dtrees.push_back(t);
+                    readers.emplace_back();
+                }
+                readers[it.first->second].push_back({(int)j, side});
+                (side ? ms[j].tib : ms[j].tia) = it.first->second;
+            }
+    }
+    std::vector<GenSet> tgs(dtrees.size());
     while (true) {
         bool any = false;
         for (auto &s : ms) any |= !s.work.empty();
@@ -1765,29 +1786,50 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
             cblk.clear();
         }
         auto tA = clk::now();
-        // input blocks to generate at this level's output nodes (jobs in parallel: each has its own
-        // sets and reads its shared input trees only)
+        // input blocks to generate at this level's output nodes: each job's missing nodes (jobs in
+        // parallel), then per input tree its readers' requests in job order (trees in parallel)
 #pragma omp parallel for schedule(dynamic, 4)
         for (long j = 0; j < (long)ms.size(); j++) {
             MulState &s = ms[j];
-            s.ga.clear();
-            s.gb.clear();
+            s.ra.clear();
+            s.rb.clear();
+            s.aa.clear();
+            s.ab.clear();
             Tree &out = *s.job->out, &a = *s.job->a, &b = *s.job->b;
             for (int oi : s.work) {
                 const NodeInfo &o = out.nodes[oi];
-                if (a.find(o.n, o.l) < 0) s.ga.request(a, o.n, o.l, find_ancestor(a, o.n, o.l, nullptr));
-                if (b.find(o.n, o.l) < 0) s.gb.request(b, o.n, o.l, find_ancestor(b, o.n, o.l, nullptr));
+                const Key k{o.n, {o.l[0], o.l[1], o.l[2]}};
+                if (a.find(o.n, o.l) < 0) {
+                    s.ra.push_back(k);
+                    s.aa.push_back(find_ancestor(a, o.n, o.l, nullptr));
+                }
+                if (b.find(o.n, o.l) < 0) {
+                    s.rb.push_back(k);
+                    s.ab.push_back(find_ancestor(b, o.n, o.l, nullptr));
+                }
+            }
+        }
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long t = 0; t < (long)dtrees.size(); t++) {
+            GenSet &gs = tgs[t];
+            gs.clear();
+            for (const auto &rd : readers[t]) {
+                const MulState &s = ms[rd.first];
+                const std::vector<Key> &keys = rd.second ? s.rb : s.ra;
+                const std::vector<int> &anc = rd.second ? s.ab : s.aa;
+                for (size_t r = 0; r < keys.size(); r++) gs.request(*dtrees[t], keys[r].n, keys[r].l, anc[r]);
             }
         }
         std::vector<std::pair<GenSet *, const Tree *>> sets;
-        for (auto &s : ms) {
-            sets.push_back({&s.ga, s.job->a});
-            sets.push_back({&s.gb, s.job->b});
-        }
+        for (size_t t = 0; t < dtrees.size(); t++) sets.push_back({&tgs[t], dtrees[t]});
         st.host_enum_ms += since(tA);
         auto tB = clk::now();
         generate_all(sets, arena, &st);
         st.host_gen_ms += since(tB);
+        // the generated blocks' value cubes, once per block: tree t's block g at gvoff[t] + g
+        std::vector<size_t> gvoff(dtrees.size() + 1, 0);
+        for (size_t t = 0; t < dtrees.size(); t++) gvoff[t + 1] = gvoff[t] + tgs[t].keys.size();
+        float2 *gvals = gvoff.back() ? (float2 *)arena.alloc(sizeof(float) * VS * gvoff.back()) : nullptr;
         auto tC = clk::now();
         // node tasks and max-norm criteria, jobs in parallel, then concatenated in job order
 #pragma omp parallel for schedule(dynamic, 4)
@@ -1799,21 +1841,24 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
             s.va.assign(s.work.size(), nullptr);
             s.vb.assign(s.work.size(), nullptr);
             float2 *ca = cached(&a), *cb = cached(&b);
+            const GenSet &ga = tgs[s.tia], &gb = tgs[s.tib];
             for (size_t w = 0; w < s.work.size(); w++) {
                 const NodeInfo &o = out.nodes[s.work[w]];
+                const Key k{o.n, {o.l[0], o.l[1], o.l[2]}};
                 int ia = a.find(o.n, o.l), ib = b.find(o.n, o.l);
-                if (ca && ia >= 0) s.va[w] = ca + (VS / 2) * (size_t)ia;
-                if (cb && ib >= 0) s.vb[w] = cb + (VS / 2) * (size_t)ib;
+                if (ia < 0) s.va[w] = gvals + (VS / 2) * (gvoff[s.tia] + (size_t)ga.slot.at(k));
+                else if (ca) s.va[w] = ca + (VS / 2) * (size_t)ia;
+                if (ib < 0) s.vb[w] = gvals + (VS / 2) * (gvoff[s.tib] + (size_t)gb.slot.at(k));
+                else if (cb) s.vb[w] = cb + (VS / 2) * (size_t)ib;
                 MulTask &tk = s.tasks[w];
-                tk.a = block_at(a, s.ga, s.ga.base, o.n, o.l);
-                tk.b = block_at(b, s.gb, s.gb.base, o.n, o.l);
+                tk.a = block_at(a, ga, ga.base, o.n, o.l);
+                tk.b = block_at(b, gb, gb.base, o.n, o.l);
                 tk.out = out.block(s.work[w]);
                 tk.cn = out.d_cn + (size_t)8 * s.work[w];
                 tk.scale = s.job->coef * std::pow(2.0, 1.5 * (o.n + 1));
                 if (s.job->use_max_norms) {
-                    Key k{o.n, {o.l[0], o.l[1], o.l[2]}};
-                    const double *cna = ia >= 0 ? &a.cn[8 * (size_t)ia] : &s.ga.cn[8 * (size_t)s.ga.slot.at(k)];
-                    const double *cnb = ib >= 0 ? &b.cn[8 * (size_t)ib] : &s.gb.cn[8 * (size_t)s.gb.slot.at(k)];
+                    const double *cna = ia >= 0 ? &a.cn[8 * (size_t)ia] : &ga.cn[8 * (size_t)ga.slot.at(k)];
+                    const double *cnb = ib >= 0 ? &b.cn[8 * (size_t)ib] : &gb.cn[8 * (size_t)gb.slot.at(k)];
                     double sc = std::pow(2.0, 1.5 * o.n);
                     s.crit[w] = (ia >= 0 ? (*s.ta)[ia] : 0.0) * block_norm8(cnb) * sc +
                                 (ib >= 0 ? (*s.tb)[ib] : 0.0) * block_norm8(cna) * sc;
@@ -1829,10 +1874,17 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
             voff[j + 1] = voff[j] + c;
             toff[j + 1] = toff[j] + ms[j].tasks.size();
         }
-        const size_t nv = voff.back(), nt = toff.back();
-        float2 *lvals = nv ? (float2 *)arena.alloc(sizeof(float) * VS * nv) : nullptr;
+        const size_t ng = gvoff.back();
+        const size_t nv = voff.back() + ng, nt = toff.back();
+        float2 *lvals = voff.back() ? (float2 *)arena.alloc(sizeof(float) * VS * voff.back()) : nullptr;
         std::vector<const double *> vblk(nv);
         std::vector<float2 *> vdst(nv);
+        // the generated blocks first, then the per-task blocks
+        for (size_t t = 0; t < dtrees.size(); t++)
+            for (size_t g = 0; g < tgs[t].keys.size(); g++) {
+                vblk[gvoff[t] + g] = tgs[t].base + (size_t)g * bsis.bs;
+                vdst[gvoff[t] + g] = gvals + (VS / 2) * (gvoff[t] + g);
+            }
         std::vector<MulVTask> tasks(nt);
 #pragma omp parallel for schedule(dynamic, 4)
         for (long j = 0; j < (long)ms.size(); j++) {
@@ -1843,9 +1895,9 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
                 MulVTask &vt = tasks[toff[j] + w];
                 auto value_of = [&](const float2 *v, const double *blk) -> const float2 * {
                     if (v) return v;
-                    vblk[k] = blk;
-                    vdst[k] = lvals + (VS / 2) * k;
-                    return vdst[k++];
+                    vblk[ng + k] = blk;
+                    vdst[ng + k] = lvals + (VS / 2) * k;
+                    return vdst[ng + k++];
                 };
                 vt.a = value_of(s.va[w], tk.a);
                 vt.b = value_of(s.vb[w], tk.b);
