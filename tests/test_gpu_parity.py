@@ -230,6 +230,25 @@ def test_multiply_matches_oracle(engine, oracle, k7):
         same_tree(out, oout, 1e-11)
 
 
+def test_batched_multiply_equals_single_products(engine, k7):
+    # a batch whose trees feed several products maps their nodes to values once and shares the
+    # generation of missing nodes; every product must come out bit-identical to a single multiply
+    mra, _ = k7
+    prec = 1e-6
+    fs = [engine.project(prec, engine.FunctionTree(mra), [g], abs_prec=True) for g in GAUSS4[:3]]
+    pairs = [(0, 0), (0, 1), (1, 2), (2, 0), (2, 2)]
+    for use_max in (False, True):
+        outs = [engine.FunctionTree(mra) for _ in pairs]
+        engine.multiply_batch(prec, outs, 1.3, [fs[i] for i, _ in pairs], [fs[j] for _, j in pairs], abs_prec=True,
+                              use_max_norms=use_max)
+        for (i, j), o in zip(pairs, outs):
+            ref = engine.FunctionTree(mra)
+            engine.multiply(prec, ref, 1.3, fs[i], fs[j], abs_prec=True, use_max_norms=use_max)
+            k1, c1, l1 = o.download()
+            k2, c2, l2 = ref.download()
+            assert np.array_equal(k1, k2) and np.array_equal(l1, l2) and np.array_equal(c1, c2), (i, j, use_max)
+
+
 def test_square_fixed_grid_and_integral_identity(engine, k7):
     """int f*f = |f|^2 (tests/qmfunctions/qmfunction.cpp:258-259), on the copied grid."""
     mra, _ = k7
