@@ -101,8 +101,10 @@ class ClockSampler:
         sm = [float(s[0]) for s in inside if s[0].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for s in inside for i in range(4) if s[3 + i].lower() == "active"})
+        pw = [float(s[2]) for s in inside if s[2].replace(".", "").isdigit()]
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": float(inside[0][1]) if inside[0][1].replace(".", "").isdigit() else None,
+                "sm_mhz_min": min(sm) if sm else None, "power_w_max": max(pw) if pw else None,
                 "reasons": reasons, "samples": len(inside)}
 
 
@@ -622,15 +624,20 @@ def run(args):
     e2e_each = []
     gc.collect()
     gc.disable()
-    t0 = time.perf_counter()
-    d2h = 0
-    for _ in range(args.e2e_steps):
-        ts = time.perf_counter()
-        d2h = e2e_step()
-        e2e_each.append((time.perf_counter() - ts) * 1e3)
-    barrier()
+    with ClockSampler() as e2e_clk:
+        time.sleep(0.3)  # nvidia-smi's first samples
+        e2e_clk.mark(True)
+        t0 = time.perf_counter()
+        d2h = 0
+        for _ in range(args.e2e_steps):
+            ts = time.perf_counter()
+            d2h = e2e_step()
+            e2e_each.append((time.perf_counter() - ts) * 1e3)
+        barrier()
+        e2e_t1 = time.perf_counter()
+        e2e_clk.mark(False)
     gc.enable()
-    e2e_ms = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps * 1e3, "cuda")
+    e2e_ms = max_over_ranks((e2e_t1 - t0) / args.e2e_steps * 1e3, "cuda")
     e2e_v = whole_job_rate(nodes, world, e2e_ms)
 
     st = stats[-1]
@@ -763,6 +770,7 @@ def run(args):
         "gpu_launches": int(st["launches"]),
         "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_ms, "ms_each_step": [round(x, 2) for x in e2e_each],
+                "clocks": e2e_clk.summary(),
                 "warmup": max(3, args.warmup), **{k: v / args.e2e_steps for k, v in e2e_parts.items()}},
         "roofline": dict(roofs[dominant], tier=dominant),
         "roofline_tiers": roofs,

@@ -262,10 +262,7 @@ __global__ void __maxnreg__(DF_MAXREG) apply_df_kernel(ApplyLaunch L) {
 template <int K>
 void launch_df(const ApplyLaunch &L, int nsm, cudaStream_t s) {
     using G = DfGeo<K>;
-    MWG_CUDA(cudaFuncSetAttribute(apply_df_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
-    int per_sm = 0;
-    MWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, apply_df_kernel<K>, G::THREADS, G::SMEM));
-    if (per_sm < 1) per_sm = 1;
+    kernel_smem((const void *)apply_df_kernel<K>, (int)G::SMEM);
     // one CTA per task (tasks are ordered longest first and taken in that order): CTAs end
     // throughout the launch, so kernels of other streams get SM slots without waiting for it
     (void)nsm;

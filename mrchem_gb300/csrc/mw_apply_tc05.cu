@@ -509,8 +509,7 @@ template <int K, int SPLIT>
 void launch_tc05(const ApplyLaunch &L, cudaStream_t s) {
     using G = T5Geo<K>;
     using M = T5Mem<K, SPLIT>;
-    MWG_CUDA(cudaFuncSetAttribute(apply_tc05_kernel<K, SPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  M::SMEM_LAUNCH));
+    kernel_smem((const void *)apply_tc05_kernel<K, SPLIT>, M::SMEM_LAUNCH);
     const int grid = L.nnodes;
     if (grid < 1) return;
     apply_tc05_kernel<K, SPLIT><<<grid, M::THREADS, M::SMEM_LAUNCH, s>>>(L);

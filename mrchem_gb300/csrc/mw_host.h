@@ -306,6 +306,12 @@ struct AddTask {
     int first, count;  // into the (src, coef) arrays
 };
 
+// Launch settings a kernel needs once per device, kept so that a launch makes no extra driver calls
+// (the apply launches a few hundred to a few thousand kernels per call): the dynamic shared memory
+// it may request (cudaFuncSetAttribute), and its resident CTAs per SM at a block size and request.
+void kernel_smem(const void *fn, int bytes);
+int kernel_ctas_per_sm(const void *fn, int threads, int bytes);
+
 void k_project(const DevBasis &b, const ProjFunc &f, const ProjTask *tasks, int n, cudaStream_t s);
 // K = 4 .. 10: generate_kernel_t<K> (shared memory, scratch unused); other K: scratch holds
 // grid x generate_scratch_doubles(K) doubles (one slice per CTA)

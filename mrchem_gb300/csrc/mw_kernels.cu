@@ -8,6 +8,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "mw_chunks.cuh"
 #include "mw_host.h"
@@ -389,7 +392,7 @@ template <int K>
 void launch_generate_t(const DevBasis &b, const GenTask *tasks, int n, int nsm, cudaStream_t s) {
     constexpr int N2 = 2 * K;
     constexpr size_t smem = sizeof(double) * ((size_t)N2 * N2 + (size_t)N2 * N2 * K + (size_t)N2 * K * K + (size_t)K * K * K);
-    MWG_CUDA(cudaFuncSetAttribute(generate_kernel_t<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel_smem((const void *)generate_kernel_t<K>, (int)smem);
     const int grid = std::min(n, 4 * std::max(nsm, 1));
     generate_kernel_t<K><<<grid, 256, smem, s>>>(b, tasks, n);
     MWG_CUDA(cudaGetLastError());
@@ -718,9 +721,8 @@ void launch_apply_t(const ApplyLaunch &L, int nsm, cudaStream_t s) {
     const int threads = f32 ? ((NC / 2 + 31) / 32) * 32 : ((NC + 31) / 32) * 32;
     const size_t smem = f32 ? sizeof(float) * (3 * C + ((K3 + 3) / 4) * 4 + 3 * NC) : sizeof(T) * (2 * C + K3 + 3 * NC);
     auto fn = f32 ? apply32_kernel<K> : apply_kernel<T, K>;
-    MWG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    MWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    kernel_smem((const void *)fn, (int)smem);
+    int per_sm = kernel_ctas_per_sm((const void *)fn, threads, (int)smem);
     if (per_sm < 1) per_sm = 1;
     // one CTA per task (tasks are ordered longest first and taken in that order): CTAs end
     // throughout the launch, so kernels of other streams get SM slots without waiting for it
@@ -932,7 +934,7 @@ void k_norms(const DevBasis &b, double *const *blocks, double *const *cn, int n,
 void k_topdown(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s) {
     if (n <= 0) return;
     size_t smem = 2 * cube_bytes(b.K);
-    MWG_CUDA(cudaFuncSetAttribute(topdown_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel_smem((const void *)topdown_kernel, (int)smem);
     topdown_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, n);
     MWG_CUDA(cudaGetLastError());
 }
@@ -940,7 +942,7 @@ void k_topdown(const DevBasis &b, const PairTask *tasks, int n, cudaStream_t s) 
 void k_compress(const DevBasis &b, const PairTask *tasks, double *const *cn, int n, cudaStream_t s) {
     if (n <= 0) return;
     size_t smem = 2 * cube_bytes(b.K) + 8 * 256 * sizeof(double);
-    MWG_CUDA(cudaFuncSetAttribute(compress_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel_smem((const void *)compress_kernel, (int)smem);
     compress_kernel<<<grid_for(n), 256, smem, s>>>(b, tasks, cn, n);
     MWG_CUDA(cudaGetLastError());
 }
@@ -1128,4 +1130,33 @@ double probe_fma_tflops(int fp64, int nsm, cudaStream_t s) {
     double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
     return flops / (best * 1e-3) / 1e12;
 }
+namespace {
+std::mutex g_launch_mu;
+std::map<std::pair<const void *, int>, int> g_smem_set;                    // (kernel, device) -> bytes
+std::map<std::tuple<const void *, int, int, int>, int> g_ctas;               // (kernel, device, threads, bytes)
+}  // namespace
+
+void kernel_smem(const void *fn, int bytes) {
+    int dev = 0;
+    MWG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_launch_mu);
+    int &have = g_smem_set[{fn, dev}];
+    if (have >= bytes) return;
+    MWG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    have = bytes;
+}
+
+int kernel_ctas_per_sm(const void *fn, int threads, int bytes) {
+    int dev = 0;
+    MWG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_launch_mu);
+    auto key = std::make_tuple(fn, dev, threads, bytes);
+    auto it = g_ctas.find(key);
+    if (it != g_ctas.end()) return it->second;
+    int per_sm = 0;
+    MWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, (size_t)bytes));
+    g_ctas[key] = per_sm;
+    return per_sm;
+}
+
 }  // namespace mwg

@@ -223,9 +223,8 @@ __global__ void __launch_bounds__(ValGeo<K>::THREADS) multiply_values_df_kernel(
 template <int K, class Fn>
 int persistent_grid(Fn fn, int n, int nsm) {
     using G = ValGeo<K>;
-    MWG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
-    int per_sm = 0;
-    MWG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, G::THREADS, G::SMEM));
+    kernel_smem((const void *)fn, (int)G::SMEM);
+    int per_sm = kernel_ctas_per_sm((const void *)fn, G::THREADS, (int)G::SMEM);
     if (per_sm < 1) per_sm = 1;
     const int slots = per_sm * (nsm > 0 ? nsm : 1);
     return n < slots ? n : slots;

@@ -191,7 +191,7 @@ template <int K, int MODE>
 void launch_post_df(const double *M, const PairTask *tasks, double *const *cn, int n, cudaStream_t s) {
     using G = PostGeo<K>;
     auto fn = post_df_kernel<K, MODE>;
-    MWG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM));
+    kernel_smem((const void *)fn, (int)G::SMEM);
     const int grid = n < 4096 ? n : 4096;
     fn<<<grid, G::THREADS, G::SMEM, s>>>(M, tasks, cn, n);
     MWG_CUDA(cudaGetLastError());

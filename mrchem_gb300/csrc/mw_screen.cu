@@ -682,7 +682,7 @@ size_t screen_smem(int maxT, int zmax) { return sizeof(int) * ((size_t)maxT + 2 
 void k_screen_count(const ScreenLevel &P, int maxT, int zmax, cudaStream_t s) {
     if (P.nn <= 0) return;
     const size_t sm = screen_smem(maxT, zmax);
-    if (sm > 48 * 1024) cudaFuncSetAttribute(screen_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (sm > 48 * 1024) kernel_smem((const void *)screen_kernel<0>, (int)sm);
     screen_kernel<0><<<P.nn, ST, sm, s>>>(P, maxT, zmax);
 }
 
@@ -699,7 +699,7 @@ void k_screen_gen_norms32(const ScreenLevel &P, int ngen, cudaStream_t s) {
 void k_screen_write(const ScreenLevel &P, int maxT, int zmax, cudaStream_t s) {
     if (P.nn <= 0) return;
     const size_t sm = screen_smem(maxT, zmax);
-    if (sm > 48 * 1024) cudaFuncSetAttribute(screen_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (sm > 48 * 1024) kernel_smem((const void *)screen_kernel<1>, (int)sm);
     screen_kernel<1><<<P.nn, ST, sm, s>>>(P, maxT, zmax);
     tier_offsets_kernel<<<1, 1024, 0, s>>>(P);
 }
