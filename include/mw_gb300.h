@@ -104,6 +104,9 @@ typedef struct {
     long long rows_fp32;      /* ... of the FP32-accuracy tier */
     long long rows_tf32;      /* ... of the TF32 tier */
     long long rows_df;        /* ... of the double-FP32 tier */
+    double host_io_ms;        /* mw_apply_batch_host: host time building the input trees' structures,
+                                 waiting for each job group's uploaded inputs and preparing them, and
+                                 queueing the outputs' downloads */
 } mw_stats;
 
 /* ---- context (replaces MultiResolutionAnalysis<3>, src/mrenv.cpp:105-122) ---- */

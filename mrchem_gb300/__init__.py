@@ -61,7 +61,7 @@ class Stats(C.Structure):
                 ("kernel_ms_df", C.c_double), ("host_gen_ms", C.c_double), ("host_launch_ms", C.c_double),
                 ("host_refine_ms", C.c_double), ("gpu_levels_ms", C.c_double), ("gpu_post_ms", C.c_double),
                 ("screen_regrows", C.c_longlong), ("rows_fp64", C.c_longlong), ("rows_fp32", C.c_longlong),
-                ("rows_tf32", C.c_longlong), ("rows_df", C.c_longlong)]
+                ("rows_tf32", C.c_longlong), ("rows_df", C.c_longlong), ("host_io_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -931,9 +931,11 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     // host inputs: the input trees' structures now (host work), their blocks per job group below
     std::vector<std::vector<int>> in_maps;
     if (hin) {
+        const auto tS = std::chrono::steady_clock::now();
         std::vector<Tree *> itrees;
         for (ApplyJob &job : jobs) itrees.push_back(job.inp);
         in_maps = upload_structures(itrees, hin->nnodes.data(), hin->keys.data());
+        st.host_io_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tS).count();
     }
     std::vector<JobState> js(jobs.size());
     int max_levels = 0;
@@ -1081,6 +1083,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         if (hin && level == 0) {
             // the group's inputs have landed: their norms to the host, then what the apply derives
             // from them (pruning norms per level, reduced-precision copies, screening tables)
+            const auto tI = std::chrono::steady_clock::now();
             MWG_CUDA(cudaEventSynchronize(G.ev_in));
             size_t off = 0;
             for (int j : G.jobs) {
@@ -1094,6 +1097,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             // the screening and generation kernels run on the high-priority stream and read what
             // was just written on the group's stream (input blocks, norms, reduced copies, tables)
             MWG_CUDA(cudaStreamSynchronize(ctx.stream));
+            st.host_io_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tI).count();
         }
         bool any = false;
         for (JobState *sp : jp) any |= !sp->work.empty();
@@ -1511,6 +1515,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                     post_process(jset, *G.arena);
                     MWG_CUDA(cudaEventRecord(ev_post[2 * g + 1], ctx.stream));
                     if (hin && hin->out_nnodes) {
+                        const auto tO = std::chrono::steady_clock::now();
                         // the group's outputs that fit go down now, beside the other groups' levels
                         std::vector<Tree *> trees;
                         std::vector<int *> k;
@@ -1527,6 +1532,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
                             l.push_back(hin->out_leaf[j]);
                         }
                         download_enqueue(trees, k.data(), c.data(), l.data(), *G.arena);
+                        st.host_io_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tO).count();
                     }
                 }
             }
