@@ -567,14 +567,15 @@ void screen_setup_inputs(Ctx &ctx, std::vector<ApplyJob> &jobs, const std::vecto
         J.in32 = t.d_coefs32;
         J.intc = t.d_coefs_tc;
     }
-    MWG_CUDA(cudaMemcpyAsync(d, h, off.back(), cudaMemcpyHostToDevice, ctx.stream));
+    // read by kernels from the pinned staging: with host inputs these tables go up while the later
+    // job groups' input blocks still occupy the copy engines
+    k_fetch(d, h, off.back(), ctx.stream);
     // the entries go to their jobs' places in the apply's ScreenJob array (contiguous runs copied
     // together)
     for (size_t q = 0; q < idx.size();) {
         size_t r = q + 1;
         while (r < idx.size() && idx[r] == idx[r - 1] + 1) r++;
-        MWG_CUDA(cudaMemcpyAsync(ds.djobs + idx[q], hj + q, sizeof(ScreenJob) * (r - q), cudaMemcpyHostToDevice,
-                                 ctx.stream));
+        k_fetch(ds.djobs + idx[q], hj + q, sizeof(ScreenJob) * (r - q), ctx.stream);
         q = r;
     }
 }
@@ -911,6 +912,8 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     const bool df_only = precision_mode == MW_PREC_DF;
     auto t_start = std::chrono::steady_clock::now();
     Arena &arena = ctx.arena;
+    // copies into the arenas that an apply which failed part-way left in flight end first
+    if (ctx.ustream) MWG_CUDA(cudaStreamSynchronize(ctx.ustream));
     arena.reset();
     float kernel_ms = 0.0f;
     // GPU spans: set-up + levels, and the post-processing after them
@@ -928,10 +931,76 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             st.launches++;
         }
     };
-    // host inputs: the input trees' structures now (host work), their blocks per job group below
+    // The jobs are split into up to four groups that take turns: while the GPU runs the other
+    // groups' levels, the host enumerates, screens and builds the items of one group's level.
+    // Group 0 works on the context's stream and arena, the others on extra streams and arenas of
+    // the context.  A single job runs as one group.
+    struct Group {
+        std::vector<int> jobs;
+        cudaStream_t stream = nullptr;
+        Arena *arena = nullptr;
+        int level = 0;
+        bool pending = false, done = false;
+        LevelItems lt[NTIER];
+        cudaEvent_t ev[NTIER + 1];
+        std::vector<std::pair<int, int *>> status;  // per launch: tier, pinned copy of (status, rows)
+        std::vector<double *> h_cn;  // pinned staging of each job's component norms
+        cudaEvent_t ev_up = nullptr;  // host inputs: the group's input blocks are on the device ...
+        double *in_blocks = nullptr;  // ... here, in the caller's order
+        cudaEvent_t ev_in = nullptr;  // ... are in the trees, with their norms on the host
+        double *in_cn = nullptr;      // ... here
+        cudaStream_t pstream = nullptr;  // ... the high-priority stream that prepares them
+        cudaEvent_t ev_prep = nullptr;   // ... reduced copies and screening tables written
+    };
+    // launch settings: the autotuner's for this (order, jobs, mode) if it ran, else the context's
+    Ctx::Tuning tune;
+    tune.groups = ctx.groups;
+    {
+        auto it = ctx.tuned.find(std::make_tuple(b.K, (int)jobs.size(), precision_mode));
+        if (it != ctx.tuned.end() && ctx.groups > 1) tune = it->second;
+    }
+    const int ngroups = std::max(1, std::min<int>(tune.groups, (int)jobs.size()));
+    std::vector<Group> groups(ngroups);
+    {
+        // balance the groups by input size, largest jobs first into the lightest group
+        auto in_nn = [&](int j) -> long { return hin ? hin->nnodes[j] : jobs[j].inp->nn(); };
+        std::vector<int> ord(jobs.size());
+        for (size_t j = 0; j < jobs.size(); j++) ord[j] = (int)j;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return in_nn(a) > in_nn(c); });
+        std::vector<long> load(ngroups, 0);
+        for (int j : ord) {
+            int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            groups[g].jobs.push_back(j);
+            load[g] += in_nn(j);
+        }
+        for (auto &g : groups) std::sort(g.jobs.begin(), g.jobs.end());
+    }
+    groups[0].stream = ctx.stream;
+    groups[0].arena = &arena;
+    for (int g = 1; g < ngroups; g++) {
+        ctx.xarena[g - 1].reset();
+        groups[g].arena = &ctx.xarena[g - 1];
+    }
+    // host inputs: every group's blocks start up on the copy stream, in group order, and the host
+    // builds the input trees' structures while they move; each group's blocks are permuted into
+    // its trees on the group's stream below
     std::vector<std::vector<int>> in_maps;
     if (hin) {
         const auto tS = std::chrono::steady_clock::now();
+        if (!ctx.ustream) MWG_CUDA(cudaStreamCreateWithFlags(&ctx.ustream, cudaStreamNonBlocking));
+        for (Group &G : groups) {
+            size_t tot = 0;
+            for (int j : G.jobs) tot += (size_t)hin->nnodes[j];
+            G.in_blocks = (double *)G.arena->alloc(sizeof(double) * (size_t)bs * tot);
+            size_t off = 0;
+            for (int j : G.jobs) {
+                MWG_CUDA(cudaMemcpyAsync(G.in_blocks + off * bs, hin->coefs[j], sizeof(double) * (size_t)bs * hin->nnodes[j],
+                                         cudaMemcpyHostToDevice, ctx.ustream));
+                off += (size_t)hin->nnodes[j];
+            }
+            MWG_CUDA(cudaEventCreateWithFlags(&G.ev_up, cudaEventDisableTiming));
+            MWG_CUDA(cudaEventRecord(G.ev_up, ctx.ustream));
+        }
         std::vector<Tree *> itrees;
         for (ApplyJob &job : jobs) itrees.push_back(job.inp);
         in_maps = upload_structures(itrees, hin->nnodes.data(), hin->keys.data());
@@ -983,47 +1052,6 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
             if (s.job->out->nodes[i].n == n) s.work.push_back(i);
     };
 
-    // The jobs are split into up to four groups that take turns: while the GPU runs the other
-    // groups' levels, the host enumerates, screens and builds the items of one group's level.
-    // Group 0 works on the context's stream and arena, the others on extra streams and arenas of
-    // the context.  A single job runs as one group.
-    struct Group {
-        std::vector<int> jobs;
-        cudaStream_t stream = nullptr;
-        Arena *arena = nullptr;
-        int level = 0;
-        bool pending = false, done = false;
-        LevelItems lt[NTIER];
-        cudaEvent_t ev[NTIER + 1];
-        std::vector<std::pair<int, int *>> status;  // per launch: tier, pinned copy of (status, rows)
-        std::vector<double *> h_cn;  // pinned staging of each job's component norms
-        cudaEvent_t ev_in = nullptr;  // host inputs: the group's input blocks and norms have landed
-        double *in_cn = nullptr;      // ... their norms, staged for the host
-    };
-    // launch settings: the autotuner's for this (order, jobs, mode) if it ran, else the context's
-    Ctx::Tuning tune;
-    tune.groups = ctx.groups;
-    {
-        auto it = ctx.tuned.find(std::make_tuple(b.K, (int)jobs.size(), precision_mode));
-        if (it != ctx.tuned.end() && ctx.groups > 1) tune = it->second;
-    }
-    const int ngroups = std::max(1, std::min<int>(tune.groups, (int)jobs.size()));
-    std::vector<Group> groups(ngroups);
-    {
-        // balance the groups by input size, largest jobs first into the lightest group
-        std::vector<int> ord(jobs.size());
-        for (size_t j = 0; j < jobs.size(); j++) ord[j] = (int)j;
-        std::stable_sort(ord.begin(), ord.end(), [&](int a, int c) { return jobs[a].inp->nn() > jobs[c].inp->nn(); });
-        std::vector<long> load(ngroups, 0);
-        for (int j : ord) {
-            int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-            groups[g].jobs.push_back(j);
-            load[g] += jobs[j].inp->nn();
-        }
-        for (auto &g : groups) std::sort(g.jobs.begin(), g.jobs.end());
-    }
-    groups[0].stream = ctx.stream;
-    groups[0].arena = &arena;
     if (!ctx.fast) {
         int least = 0, greatest = 0;
         MWG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
@@ -1041,29 +1069,36 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         for (int g = 1; g < ngroups; g++) {
             cudaStream_t &xs = ctx.xstream[g - 1];
             if (!xs) MWG_CUDA(cudaStreamCreateWithFlags(&xs, cudaStreamNonBlocking));
-            ctx.xarena[g - 1].reset();
             groups[g].stream = xs;
-            groups[g].arena = &ctx.xarena[g - 1];
             MWG_CUDA(cudaStreamWaitEvent(xs, ev_start, 0));
             MWG_CUDA(cudaEventCreateWithFlags(&ev_end[g], cudaEventDisableTiming));
         }
     }
     for (auto &g : groups)
         for (auto &e : g.ev) MWG_CUDA(cudaEventCreate(&e));
-    // host inputs: each group's input blocks go up on the group's stream, in group order, so that
-    // the first groups compute while the copy engine still moves the later groups' blocks
+    // host inputs: each group's blocks go into its trees on the group's high-priority stream once
+    // they are on the device, so that the first groups compute while the copy engine still moves
+    // the later groups' blocks
     if (hin)
-        for (auto &G : groups) {
-            StreamSwap swap(ctx, G.stream);
+        for (int g = 0; g < ngroups; g++) {
+            Group &G = groups[g];
+            cudaStream_t &ps = ctx.pstream[g];
+            if (!ps) {
+                int least = 0, greatest = 0;
+                MWG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+                MWG_CUDA(cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, greatest));
+            }
+            G.pstream = ps;
+            MWG_CUDA(cudaStreamWaitEvent(ps, ev_start, 0));
+            StreamSwap swap(ctx, ps);
+            MWG_CUDA(cudaStreamWaitEvent(ctx.stream, G.ev_up, 0));
             std::vector<Tree *> trees;
             std::vector<const int *> maps;
-            std::vector<const double *> coefs;
             for (int j : G.jobs) {
                 trees.push_back(jobs[j].inp);
                 maps.push_back(in_maps[j].data());
-                coefs.push_back(hin->coefs[j]);
             }
-            G.in_cn = upload_enqueue(trees, maps, coefs, *G.arena);
+            G.in_cn = upload_enqueue(trees, maps, G.in_blocks, *G.arena);
             MWG_CUDA(cudaEventCreateWithFlags(&G.ev_in, cudaEventDisableTiming));
             MWG_CUDA(cudaEventRecord(G.ev_in, ctx.stream));
         }
@@ -1082,21 +1117,27 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         }
         if (hin && level == 0) {
             // the group's inputs have landed: their norms to the host, then what the apply derives
-            // from them (pruning norms per level, reduced-precision copies, screening tables)
+            // from them (pruning norms per level; reduced-precision copies and screening tables on
+            // the group's high-priority stream, which the group's stream and the screening stream
+            // wait for on the GPU)
             const auto tI = std::chrono::steady_clock::now();
             MWG_CUDA(cudaEventSynchronize(G.ev_in));
-            size_t off = 0;
-            for (int j : G.jobs) {
-                Tree &in = *jobs[j].inp;
-                std::copy(G.in_cn + off, G.in_cn + off + 8 * (size_t)in.nn(), in.cn.begin());
-                off += 8 * (size_t)in.nn();
-                js[j].set_fmax(in, b.n0);
-                if (mixed) convert_input(in);
+            {
+                StreamSwap pswap(ctx, G.pstream);
+                size_t off = 0;
+                for (int j : G.jobs) {
+                    Tree &in = *jobs[j].inp;
+                    std::copy(G.in_cn + off, G.in_cn + off + 8 * (size_t)in.nn(), in.cn.begin());
+                    off += 8 * (size_t)in.nn();
+                    js[j].set_fmax(in, b.n0);
+                    if (mixed) convert_input(in);
+                }
+                if (ds.on) screen_setup_inputs(ctx, jobs, G.jobs, ds);
+                MWG_CUDA(cudaEventCreateWithFlags(&G.ev_prep, cudaEventDisableTiming));
+                MWG_CUDA(cudaEventRecord(G.ev_prep, ctx.stream));
             }
-            if (ds.on) screen_setup_inputs(ctx, jobs, G.jobs, ds);
-            // the screening and generation kernels run on the high-priority stream and read what
-            // was just written on the group's stream (input blocks, norms, reduced copies, tables)
-            MWG_CUDA(cudaStreamSynchronize(ctx.stream));
+            MWG_CUDA(cudaStreamWaitEvent(ctx.stream, G.ev_prep, 0));
+            MWG_CUDA(cudaStreamWaitEvent(ctx.fast, G.ev_prep, 0));
             st.host_io_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tI).count();
         }
         bool any = false;
@@ -1573,8 +1614,11 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
         }
     }
     for (auto &e : ev_post) cudaEventDestroy(e);
-    for (auto &G : groups)
+    for (auto &G : groups) {
         if (G.ev_in) cudaEventDestroy(G.ev_in);
+        if (G.ev_up) cudaEventDestroy(G.ev_up);
+        if (G.ev_prep) cudaEventDestroy(G.ev_prep);
+    }
     for (auto &e : ev_span) cudaEventDestroy(e);
     if (ds.ev_counts) cudaEventDestroy(ds.ev_counts);
     st.kernel_ms += kernel_ms;

@@ -131,6 +131,9 @@ static void ctx_free(mw_ctx c) {
     for (auto &xs : c->ctx.xstream)
         if (xs) cudaStreamSynchronize(xs);
     if (c->ctx.fast) cudaStreamSynchronize(c->ctx.fast);
+    if (c->ctx.ustream) cudaStreamSynchronize(c->ctx.ustream);
+    for (auto &ps : c->ctx.pstream)
+        if (ps) cudaStreamSynchronize(ps);
     c->ctx.arena.release();
     c->ctx.sarena.release();
     for (auto &xa : c->ctx.xarena) xa.release();
@@ -140,6 +143,9 @@ static void ctx_free(mw_ctx c) {
     for (auto &xs : c->ctx.xstream)
         if (xs) cudaStreamDestroy(xs);
     if (c->ctx.fast) cudaStreamDestroy(c->ctx.fast);
+    if (c->ctx.ustream) cudaStreamDestroy(c->ctx.ustream);
+    for (auto &ps : c->ctx.pstream)
+        if (ps) cudaStreamDestroy(ps);
     if (c->ctx.fast_done) cudaEventDestroy(c->ctx.fast_done);
     delete c;
 }

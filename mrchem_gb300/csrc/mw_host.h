@@ -208,6 +208,13 @@ struct Ctx {
     // generation gets the next free slot instead of waiting for whole kernels of other groups
     cudaStream_t fast = nullptr;
     cudaEvent_t fast_done = nullptr;
+    // copy stream of a batched apply from host buffers: every job group's input blocks go up on
+    // it in group order, while the host builds the input trees' structures
+    cudaStream_t ustream = nullptr;
+    // high-priority streams, one per job group, that put the group's uploaded blocks into its
+    // trees and derive the reduced copies and screening tables from them: their kernels take the
+    // next free SM slots beside the other groups' contractions
+    cudaStream_t pstream[XGROUPS + 1] = {};
     void *h_pinned = nullptr;
     size_t pinned_bytes = 0;
     void *pinned(size_t bytes);
@@ -390,6 +397,9 @@ void k_dot(const double *const *a, const double *const *b, const int *start, int
 void k_scale(double *x, size_t n, double c, cudaStream_t s);
 // dst block j = src block map[j]; bs even
 void k_permute_blocks(double *dst, const double *src, const int *map, int n, int bs, cudaStream_t s);
+// device memory from pinned host memory (allocated by cudaMallocHost) with a kernel instead of
+// a copy engine
+void k_fetch(void *dst, const void *src_pinned, size_t bytes, cudaStream_t s);
 // ---------------------------------------------------------------- screening on the GPU (mw_screen.cu)
 // Hash of a node key, shared by the host (which fills an input tree's table) and the device (which
 // looks positions up in it).

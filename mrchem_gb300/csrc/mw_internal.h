@@ -90,11 +90,12 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
 // sized first); per tree, the caller's block index of each tree node
 std::vector<std::vector<int>> upload_structures(const std::vector<Tree *> &trees, const int *nnodes,
                                                 const int *const *keys);
-// on the context's current stream: the caller's pinned blocks into the trees (permuted into tree
-// order), the trees' norms, and the norms' download into pinned staging, returned (8 per node,
-// tree after tree); read it after the stream has passed this point
+// on the context's current stream: the caller's blocks, already copied to the device in the
+// caller's order (`staged`, tree after tree), permuted into the trees' order, the trees' norms,
+// and the norms' download into pinned staging, returned (8 per node, tree after tree); read it
+// after the stream has passed this point
 double *upload_enqueue(const std::vector<Tree *> &trees, const std::vector<const int *> &maps,
-                       const std::vector<const double *> &coefs, Arena &arena);
+                       const double *staged, Arena &arena);
 // on the context's current stream: the trees' blocks in canonical order into the caller's pinned
 // buffers; keys and leaf flags (host data, either may be null) are written before it returns
 void download_enqueue(const std::vector<Tree *> &trees, int *const *keys, double *const *coefs,

@@ -992,6 +992,29 @@ __global__ void permute_blocks_kernel(double *dst, const double *src, const int 
     }
 }
 
+// A pinned host buffer into device memory, read by the SMs over the host link: an upload of this
+// kind never queues behind bulk copies on the copy engines (the input blocks of a host-buffer
+// apply moving beside the first levels).  16-byte words where both ends are 16-byte aligned.
+__global__ void fetch_kernel(char *dst, const char *src, size_t bytes, int vec) {
+    const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    size_t head = 0;
+    if (vec) {
+        const size_t n16 = bytes / 16;
+        for (size_t i = tid; i < n16; i += stride) reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(src)[i];
+        head = n16 * 16;
+    }
+    for (size_t i = head + tid; i < bytes; i += stride) dst[i] = src[i];
+}
+
+void k_fetch(void *dst, const void *src_pinned, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) return;
+    const int vec = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src_pinned)) & 15) == 0;
+    const size_t units = vec ? (bytes + 15) / 16 : bytes;
+    const int blocks = (int)std::min<size_t>((units + 255) / 256, 1024);
+    fetch_kernel<<<blocks, 256, 0, s>>>((char *)dst, (const char *)src_pinned, bytes, vec);
+    MWG_CUDA(cudaGetLastError());
+}
+
 void k_permute_blocks(double *dst, const double *src, const int *map, int n, int bs, cudaStream_t s) {
     if (n <= 0) return;
     permute_blocks_kernel<<<std::min(n, 4096), 256, 0, s>>>(dst, src, map, n, bs);

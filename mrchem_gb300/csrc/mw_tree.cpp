@@ -147,7 +147,12 @@ void Packer::ship(Ctx &ctx, Arena &arena) {
         }
     }
     dev = (char *)arena.alloc(total);
-    MWG_CUDA(cudaMemcpyAsync(dev, h, total, cudaMemcpyHostToDevice, ctx.stream));
+    // packs up to a few MB are read by a kernel, so that they never wait behind bulk copies on the
+    // copy engines; larger ones take a copy engine
+    if (total <= ((size_t)4 << 20))
+        k_fetch(dev, h, total, ctx.stream);
+    else
+        MWG_CUDA(cudaMemcpyAsync(dev, h, total, cudaMemcpyHostToDevice, ctx.stream));
 }
 
 // ------------------------------------------------------------------ tree
@@ -662,15 +667,11 @@ std::vector<std::vector<int>> upload_structures(const std::vector<Tree *> &trees
 }
 
 double *upload_enqueue(const std::vector<Tree *> &trees, const std::vector<const int *> &maps,
-                       const std::vector<const double *> &coefs, Arena &arena) {
+                       const double *staged, Arena &arena) {
     Ctx &ctx = *trees[0]->ctx;
     const int bs = ctx.basis.bs, n = (int)trees.size();
     std::vector<size_t> first(n + 1, 0);
     for (int i = 0; i < n; i++) first[i + 1] = first[i] + (size_t)trees[i]->nn();
-    double *scratch = (double *)arena.alloc(sizeof(double) * (size_t)bs * first[n]);
-    for (int i = 0; i < n; i++)
-        MWG_CUDA(cudaMemcpyAsync(scratch + first[i] * bs, coefs[i], sizeof(double) * (size_t)bs * trees[i]->nn(),
-                                 cudaMemcpyHostToDevice, ctx.stream));
     std::vector<int> m;
     std::vector<double *> bl, cnp;
     m.reserve(first[n]);
@@ -688,7 +689,7 @@ double *upload_enqueue(const std::vector<Tree *> &trees, const std::vector<const
     pk.ship(ctx, arena);
     const int *dmap = (const int *)pk.ptr(0);
     for (int i = 0; i < n; i++)
-        k_permute_blocks(trees[i]->d_coefs, scratch + first[i] * bs, dmap + first[i], trees[i]->nn(), bs, ctx.stream);
+        k_permute_blocks(trees[i]->d_coefs, staged + first[i] * bs, dmap + first[i], trees[i]->nn(), bs, ctx.stream);
     k_norms(ctx.dbasis, (double *const *)pk.ptr(1), (double *const *)pk.ptr(2), (int)bl.size(), ctx.stream);
     double *h = (double *)arena.halloc(sizeof(double) * 8 * first[n]);
     for (int i = 0; i < n; i++)
