@@ -274,8 +274,12 @@ __global__ void __launch_bounds__(T5Mem<K, SPLIT>::THREADS, SPLIT ? 1 : 2) apply
         dst[0] = h;
         if (SPLIT) dst[G::RSZ / 4] = tf32r(__fsub_rn(v, h));
     };
-    // barriers: 0 staging copies, 1 x MMAs, 2 y MMAs, 3 end of a node, 4 draining after a failed wait
-    __shared__ __align__(8) uint64_t bar[5];
+    // barriers: 0 staging copies, 1 x MMAs (every item; the issuing thread waits), 2 y MMAs, 3 end
+    // of a node, 4 draining after a failed wait, 5 x MMAs of a row's last item (the epilogue warps
+    // wait).  A barrier's waiters tell its phases apart by parity only, so none may complete twice
+    // before every waiter has seen the first: the items of a row sync nowhere, so the epilogue warps
+    // wait on bar 5, which completes once per row, before a sync, and never on bar 1.
+    __shared__ __align__(8) uint64_t bar[6];
     __shared__ uint32_t s_tmem;
     __shared__ int s_node, s_redf;
     __shared__ volatile int s_fail;
@@ -293,7 +297,7 @@ __global__ void __launch_bounds__(T5Mem<K, SPLIT>::THREADS, SPLIT ? 1 : 2) apply
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        for (int b = 0; b < 5; b++) mbar_init(&bar[b]);
+        for (int b = 0; b < 6; b++) mbar_init(&bar[b]);
         s_fail = 0;
     }
     async_fence();
@@ -390,6 +394,7 @@ __global__ void __launch_bounds__(T5Mem<K, SPLIT>::THREADS, SPLIT ? 1 : 2) apply
                     }
                     wait(0);  // item j's input block and B operands are in S and B set `set`
                     issue_pass(dS, G::LBO_S, S_LO, dBs, G::MTX, tD, !first, 1);
+                    if (last && !s_fail) t5_commit(&bar[5]);
                     // the x MMAs, and every earlier MMA (the previous row's z pass), are done:
                     // S and the other B set are free for item j+1
                     wait(1);
@@ -398,7 +403,7 @@ __global__ void __launch_bounds__(T5Mem<K, SPLIT>::THREADS, SPLIT ? 1 : 2) apply
                 __syncwarp();
             } else {
                 // ---- x epilogue: D row (Z, Y) -> A_y rows (X', Z) and extra rows (X' < K, Z < K), k = Y
-                wait(1);  // every item's x MMAs, so that the barrier's phases are waited in order
+                if (last) wait(5);  // the row's x MMAs
                 if (last) t5_after_sync();
                 if (last) t5_epilogue<K, M::WIDE, M::TS>(tD, G::MTX, q, half, lane, [&](int r, const uint32_t (&v)[32]) {
                     if (r >= NN) return;

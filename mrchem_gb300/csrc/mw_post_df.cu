@@ -49,59 +49,65 @@ __device__ __forceinline__ void pdf_split(double d, float &h, float &l) {
 
 template <int K>
 struct PostGeo {
-    static constexpr int N2 = 2 * K, NC = N2 * N2, K3 = K * K * K, RS = N2 + 1;
+    static constexpr int N2 = 2 * K, NC = N2 * N2, K3 = K * K * K, RS = N2 + 1, RH = K + 1;
+    // one thread per line of the staged cube in the x pass, per half line in the y and z passes
     static constexpr int THREADS = ((NC + 31) / 32) * 32;
-    // two cubes (N2 x N2 rows of RS pairs: the y pass reads one and writes the other), M^T hi and lo
-    // (NC floats each), 8 K^2 norm partials
-    static constexpr size_t SMEM =
-        sizeof(float2) * 2 * (size_t)NC * RS + sizeof(float) * 2 * (size_t)NC + sizeof(double) * 8 * K * K;
+    // the full input cube (N2 x N2 rows of RS pairs; later the y pass's half cube), the half cube of
+    // the x and z passes (N2 x N2 rows of RH pairs), M^T hi and lo (NC floats each), and the
+    // compression's norm partials (4 components x K^2)
+    static constexpr size_t SMEM = sizeof(float2) * (size_t)NC * RS + sizeof(float2) * (size_t)NC * RH +
+                                   sizeof(float) * 2 * (size_t)NC + sizeof(double) * 4 * K * K;
 };
 
-// out = M v for one line of 2K values held in shared memory (element i at line[i * stride]), M^T
-// in shared memory as hi / lo rows (M^T[k][j] = M[j][k]); the outputs are made in two halves of K
-// and handed to store(j, hi, lo) renormalised (|lo| <= ulp(hi) / 2).  The k loop is rolled: a few
-// hundred instructions, where a fully unrolled transform (thousands) overflowed the instruction
-// cache and stalled the small launches of the post-processing
-template <int K, class Store>
-__device__ __forceinline__ void pdf_line_smem(const float2 *line, int stride, const float *mth, const float *mtl,
-                                              Store store) {
+// K outputs (half h of the 2K) of M v for one line of 2K values held in shared memory (element i at
+// line[i * stride]), M^T in shared memory as hi / lo rows (M^T[k][j] = M[j][k]), handed to
+// store(j, hi, lo) renormalised (|lo| <= ulp(hi) / 2).  The k loop is rolled: a few hundred
+// instructions, where a fully unrolled transform (thousands) overflowed the instruction cache and
+// stalled the small launches of the post-processing
+template <int K>
+__device__ __forceinline__ void pdf_half_line(const float2 *line, int stride, const float *mth, const float *mtl, int h,
+                                              float (&oh)[K], float (&ol)[K]) {
     constexpr int N2 = 2 * K;
+#pragma unroll
+    for (int j = 0; j < K; j++) oh[j] = ol[j] = 0.0f;
 #pragma unroll 1
-    for (int h = 0; h < 2; h++) {
-        float oh[K], ol[K];
+    for (int k = 0; k < N2; k++) {
+        const float2 v = line[k * stride];
 #pragma unroll
-        for (int j = 0; j < K; j++) oh[j] = ol[j] = 0.0f;
-#pragma unroll 1
-        for (int k = 0; k < N2; k++) {
-            const float2 v = line[k * stride];
+        for (int j = 0; j < K; j++) pdf_fma(oh[j], ol[j], mth[k * N2 + h * K + j], mtl[k * N2 + h * K + j], v.x, v.y);
+    }
 #pragma unroll
-            for (int j = 0; j < K; j++)
-                pdf_fma(oh[j], ol[j], mth[k * N2 + h * K + j], mtl[k * N2 + h * K + j], v.x, v.y);
-        }
-#pragma unroll
-        for (int j = 0; j < K; j++) {
-            const float t = __fadd_rn(oh[j], ol[j]);
-            store(h * K + j, t, __fsub_rn(ol[j], __fsub_rn(t, oh[j])));
-        }
+    for (int j = 0; j < K; j++) {
+        const float t = __fadd_rn(oh[j], ol[j]);
+        ol[j] = __fsub_rn(ol[j], __fsub_rn(t, oh[j]));
+        oh[j] = t;
     }
 }
 
 // MODE 0: top-down (M = W^T, input = the parent's block, children's scaling parts +=)
 // MODE 1: bottom-up (M = W, input = the children's scaling parts, parent's block = and its norms)
+//
+// Two CTAs per node, one per half hx of the output's x range: a CTA transforms the whole staged
+// cube along x into its half, then that half along y and z, so the two halves split the node's
+// work with nothing computed twice, and a node of a small level finishes in half the time.  The
+// CTA of half hx writes the four children (top-down) or parent components (compression) whose
+// octant has x half hx.
 template <int K, int MODE>
-__global__ void __launch_bounds__(PostGeo<K>::THREADS, 1)
+__global__ void __launch_bounds__(PostGeo<K>::THREADS, 2)
     post_df_kernel(const double *M, const PairTask *tasks, double *const *cn, int n) {
     using G = PostGeo<K>;
-    constexpr int N2 = G::N2, NC = G::NC, K3 = G::K3, RS = G::RS;
+    constexpr int N2 = G::N2, NC = G::NC, K3 = G::K3, RS = G::RS, RH = G::RH;
     extern __shared__ __align__(16) float2 smem_post[];
-    float2 *s_cube = smem_post;               // cube[Z][Y][X] at (Z * N2 + Y) * RS + X: x pass out, z pass out
-    float2 *s_cub2 = s_cube + (size_t)NC * RS;  // the same layout: y pass out
-    float *s_mth = reinterpret_cast<float *>(s_cub2 + (size_t)NC * RS);
+    float2 *s_full = smem_post;                   // input cube[Z][Y][X] at (Z * N2 + Y) * RS + X; y pass out (half)
+    float2 *s_half = s_full + (size_t)NC * RS;    // half cube[Z][Y][x'] at (Z * N2 + Y) * RH + x': x and z pass out
+    float *s_mth = reinterpret_cast<float *>(s_half + (size_t)NC * RH);
     float *s_mtl = s_mth + NC;
-    double *s_red = reinterpret_cast<double *>(s_mtl + NC);  // [component][K^2]
+    double *s_red = reinterpret_cast<double *>(s_mtl + NC);  // [component >> 1][K^2] (compression)
     const int tid = threadIdx.x;
     const bool active = tid < NC;
-    const int a = tid % N2, bq = tid / N2;  // the line's two fixed coordinates
+    // x pass: line (Y, Z); y and z passes: (x', the line's other coordinate, output half)
+    const int xa = tid % N2, xb = tid / N2;
+    const int px = tid % K, pl = (tid / K) % N2, ph = tid / (K * N2);
 
     for (int i = tid; i < NC; i += blockDim.x) {
         const int k = i / N2, j = i - k * N2;  // M^T[k][j] = M[j][k]
@@ -111,12 +117,12 @@ __global__ void __launch_bounds__(PostGeo<K>::THREADS, 1)
         s_mtl[i] = l;
     }
 
-    for (int t = blockIdx.x; t < n; t += gridDim.x) {
+    for (int u = blockIdx.x; u < 2 * n; u += gridDim.x) {
+        const int t = u >> 1, hx = u & 1;
         const PairTask task = tasks[t];
         // the FP64 input, split into FP32 pairs, staged as a cube by all threads (coalesced reads):
         // top-down the parent's block, compression the children's scaling parts (child c in
-        // octant c); then x: s_cube -> s_cub2, y: s_cub2 -> s_cube, z: s_cube -> s_cub2 (top-down)
-        // or the parent's FP64 block with its norms (compression)
+        // octant c)
         __syncthreads();  // M^T ready; the previous node's cubes and partials are no longer read
         for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
             const int c = gi / K3, r = gi - c * K3;
@@ -125,63 +131,63 @@ __global__ void __launch_bounds__(PostGeo<K>::THREADS, 1)
             const double d = MODE == 0 ? task.parent[gi] : task.child0[(size_t)c * 8 * K3 + r];
             float h, l;
             df_split(d, h, l);
-            s_cube[(size_t)(Z * N2 + Y) * RS + X] = make_float2(h, l);
+            s_full[(size_t)(Z * N2 + Y) * RS + X] = make_float2(h, l);
         }
         __syncthreads();
-        if (active) {  // x pass, thread (Y, Z) = (a, bq)
-            const int off = (bq * N2 + a) * RS;
-            pdf_line_smem<K>(s_cube + off, 1, s_mth, s_mtl,
-                             [&](int X, float h, float l) { s_cub2[off + X] = make_float2(h, l); });
+        float oh[K], ol[K];
+        if (active) {  // x pass: line (Y, Z) = (xa, xb), outputs X = hx K + j
+            const int row = xb * N2 + xa;
+            pdf_half_line<K>(s_full + row * RS, 1, s_mth, s_mtl, hx, oh, ol);
+#pragma unroll
+            for (int j = 0; j < K; j++) s_half[row * RH + j] = make_float2(oh[j], ol[j]);
         }
         __syncthreads();
-        if (active) {  // y pass, thread (X, Z) = (a, bq)
-            const int off = bq * N2 * RS + a;
-            pdf_line_smem<K>(s_cub2 + off, RS, s_mth, s_mtl,
-                             [&](int Y, float h, float l) { s_cube[off + Y * RS] = make_float2(h, l); });
+        if (active) {  // y pass: line (x', Z) = (px, pl), outputs Y = ph K + j, into s_full as a half cube
+            pdf_half_line<K>(s_half + pl * N2 * RH + px, RH, s_mth, s_mtl, ph, oh, ol);
+#pragma unroll
+            for (int j = 0; j < K; j++) s_full[(pl * N2 + ph * K + j) * RH + px] = make_float2(oh[j], ol[j]);
         }
         __syncthreads();
-        if (active) {  // z pass, thread (X, Y) = (a, bq)
-            const int off = bq * RS + a;
+        if (active) {  // z pass: line (x', Y) = (px, pl), outputs Z = ph K + j
+            pdf_half_line<K>(s_full + pl * RH + px, N2 * RH, s_mth, s_mtl, ph, oh, ol);
             if (MODE == 0) {
-                pdf_line_smem<K>(s_cube + off, N2 * RS, s_mth, s_mtl,
-                                 [&](int Z, float h, float l) { s_cub2[off + Z * N2 * RS] = make_float2(h, l); });
+#pragma unroll
+                for (int j = 0; j < K; j++) s_half[((ph * K + j) * N2 + pl) * RH + px] = make_float2(oh[j], ol[j]);
             } else {
-                const int cxy = (a >= K ? 1 : 0) | (bq >= K ? 2 : 0);
-                const int r2 = (bq % K) * K + a % K;
-                double s0 = 0.0, s1 = 0.0;  // this line's squared norms (Z < K, Z >= K)
-                pdf_line_smem<K>(s_cube + off, N2 * RS, s_mth, s_mtl, [&](int Z, float h, float l) {
-                    const int c = cxy | (Z >= K ? 4 : 0);
-                    const double v = df_widen(h) + df_widen(l);
-                    task.parent[(size_t)c * K3 + (size_t)(Z % K) * K * K + r2] = v;
-                    if (Z < K)
-                        s0 = fma(v, v, s0);
-                    else
-                        s1 = fma(v, v, s1);
-                });
-                s_red[cxy * K * K + r2] = s0;
-                s_red[(cxy | 4) * K * K + r2] = s1;
+                // parent component c = hx | (Y >= K) << 1 | ph << 2, element (Z % K, Y % K, x')
+                const int c = hx | (pl >= K ? 2 : 0) | (ph << 2);
+                const int r2 = (pl % K) * K + px;
+                double s = 0.0;
+#pragma unroll
+                for (int j = 0; j < K; j++) {
+                    const double v = df_widen(oh[j]) + df_widen(ol[j]);
+                    task.parent[(size_t)c * K3 + (size_t)j * K * K + r2] = v;
+                    s = fma(v, v, s);
+                }
+                s_red[(c >> 1) * K * K + r2] = s;
             }
         }
         __syncthreads();
         if (MODE == 0) {
-            // child c's scaling part += octant c of the cube
-            for (int gi = tid; gi < 8 * K3; gi += blockDim.x) {
-                const int c = gi / K3, r = gi - c * K3;
+            // child c's scaling part += octant c of the output, for the four children of half hx
+            for (int gi = tid; gi < 4 * K3; gi += blockDim.x) {
+                const int q = gi / K3, r = gi - q * K3;
+                const int c = hx | (q << 1);
                 const int ix = r % K, iy = (r / K) % K, iz = r / (K * K);
-                const int X = (c & 1) * K + ix, Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
-                const float2 v = s_cub2[(size_t)(Z * N2 + Y) * RS + X];
+                const int Y = ((c >> 1) & 1) * K + iy, Z = (c >> 2) * K + iz;
+                const float2 v = s_half[(size_t)(Z * N2 + Y) * RH + ix];
                 task.child0[(size_t)c * 8 * K3 + r] += df_widen(v.x) + df_widen(v.y);
             }
         }
         if (MODE == 1) {
             // component c summed by one warp: lane-strided, then a fixed butterfly (deterministic)
             const int warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
-            for (int c = warp; c < 8; c += nw) {
+            for (int q = warp; q < 4; q += nw) {
                 double s = 0.0;
-                for (int j = lane; j < K * K; j += 32) s += s_red[c * K * K + j];
+                for (int j = lane; j < K * K; j += 32) s += s_red[q * K * K + j];
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                if (lane == 0) cn[t][c] = sqrt(s);
+                if (lane == 0) cn[t][hx | (q << 1)] = sqrt(s);
             }
         }
     }
@@ -192,7 +198,7 @@ void launch_post_df(const double *M, const PairTask *tasks, double *const *cn, i
     using G = PostGeo<K>;
     auto fn = post_df_kernel<K, MODE>;
     kernel_smem((const void *)fn, (int)G::SMEM);
-    const int grid = n < 4096 ? n : 4096;
+    const int grid = 2 * n < 8192 ? 2 * n : 8192;
     fn<<<grid, G::THREADS, G::SMEM, s>>>(M, tasks, cn, n);
     MWG_CUDA(cudaGetLastError());
 }
