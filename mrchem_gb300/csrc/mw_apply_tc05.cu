@@ -260,8 +260,13 @@ __device__ __forceinline__ void t5_epilogue(uint32_t tcol, int tiles, int q, int
     }
 }
 
+// The TF32 tier at k >= 7 is held to 64 registers (it needs 71 at K = 10; no spills at 64): two
+// of its CTAs (2 x 9 warps x 64) and one CTA of the double-FP32 tier (13 warps x 112) then fit in
+// an SM's 65,536 registers together, as they do in shared memory, so the two tiers' kernels of
+// different job groups can share SMs (tensor pipe and FP32 pipe side by side).
 template <int K, int SPLIT>
-__global__ void __launch_bounds__(T5Mem<K, SPLIT>::THREADS, SPLIT ? 1 : 2) apply_tc05_kernel(ApplyLaunch L) {
+__global__ void __launch_bounds__(T5Mem<K, SPLIT>::THREADS, SPLIT ? 1 : 2) __maxnreg__(SPLIT || K < 8 ? 128 : 64)
+    apply_tc05_kernel(ApplyLaunch L) {
     using G = T5Geo<K>;
     using M = T5Mem<K, SPLIT>;
     constexpr int N2 = G::N2, NN = G::NN, KK = G::KK, K3 = G::K3, N = G::N;

@@ -206,6 +206,48 @@ def test_apply_batch_host_matches_upload_then_apply(engine, precision):
                 engine.unpin_host(mra, c)
 
 
+def test_apply_batch_host_groups_and_node_order(engine):
+    # the host-buffer apply with one to three job groups (each group's blocks on the copy stream,
+    # its preparation on its own stream) and with the caller's nodes in a shuffled order (the
+    # blocks permuted into tree order on the device): outputs bit-identical to upload + apply
+    prec = 1e-6
+    rng = np.random.default_rng(20261205)
+    mra = engine.MultiResolutionAnalysis(9)
+    srcs, ops = [], []
+    for _ in range(5):
+        R = tuple(rng.uniform(-2.0, 2.0, 3))
+        alpha = float(np.exp(rng.uniform(np.log(0.5), np.log(10.0))))
+        f = engine.project(prec, engine.FunctionTree(mra), [(1.0, alpha, R, (0, 1, 0)), (0.7, 1.5 * alpha, R, (0, 0, 1))],
+                           abs_prec=True)
+        f.rescale(1.0 / f.norm())
+        srcs.append(f)
+        ops.append(engine.HelmholtzOperator(mra, float(rng.uniform(0.5, 2.0)), prec))
+    host = [s.download() for s in srcs]
+    inps_a = engine.upload_batch([engine.FunctionTree(mra) for _ in srcs], host)
+    outs_a = [engine.FunctionTree(mra) for _ in srcs]
+    engine.apply_batch([prec] * 5, outs_a, ops, inps_a, abs_prec=True, precision="mixed")
+    ref = engine.download_batch(outs_a)
+    shuffled = []
+    for k, c, l in host:
+        p = rng.permutation(k.shape[0])
+        b = (np.ascontiguousarray(k[p]), np.ascontiguousarray(c[p]), np.ascontiguousarray(l[p]))
+        engine.pin_host(mra, b[1])
+        shuffled.append(b)
+    try:
+        for groups in (1, 2, 3):
+            mra.set_groups(groups)
+            outs = [engine.FunctionTree(mra) for _ in srcs]
+            st = engine.apply_batch_host([prec] * 5, outs, ops, [engine.FunctionTree(mra) for _ in srcs], shuffled,
+                                         abs_prec=True, precision="mixed")
+            assert st["items"] > 0
+            for (k1, c1, l1), (k2, c2, l2) in zip(engine.download_batch(outs), ref):
+                assert np.array_equal(k1, k2) and np.array_equal(c1, c2) and np.array_equal(l1, l2)
+    finally:
+        mra.set_groups(4)
+        for b in shuffled:
+            engine.unpin_host(mra, b[1])
+
+
 def test_apply_batch_host_outputs(engine):
     # the outputs of mw_apply_batch_host go down per job group into the caller's pinned buffers:
     # equal to a download_batch afterwards; an output whose buffer is too small is left for
