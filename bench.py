@@ -770,6 +770,8 @@ def run(args):
         "gpu_launches": int(st["launches"]),
         "e2e": {"value": e2e_v, "unit": "nodes/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_ms, "ms_each_step": [round(x, 2) for x in e2e_each],
+                # the mean above is the reported rate; the median shows a typical step beside it
+                "ms_median_step": sorted(e2e_each)[len(e2e_each) // 2],
                 "clocks": e2e_clk.summary(),
                 "warmup": max(3, args.warmup), **{k: v / args.e2e_steps for k, v in e2e_parts.items()}},
         "roofline": dict(roofs[dominant], tier=dominant),
