@@ -616,16 +616,17 @@ def run(args):
         mw.pin_host(mra, r[1])
     # warm-up steps on the pinned buffers: the first call that overlaps the transfers with the job
     # groups sizes its staging and stream-ordered allocations
-    for _ in range(max(3, args.warmup)):
-        e2e_step()
-    barrier()
-    for k in e2e_parts:
-        e2e_parts[k] = 0.0
     e2e_each = []
-    gc.collect()
-    gc.disable()
+    # the sampler starts before the warm-up steps, as for the device-resident loop: nvidia-smi's
+    # start-up (its first samples come after a while) then overlaps them, not the timed steps
     with ClockSampler() as e2e_clk:
-        time.sleep(0.3)  # nvidia-smi's first samples
+        for _ in range(max(3, args.warmup)):
+            e2e_step()
+        barrier()
+        for k in e2e_parts:
+            e2e_parts[k] = 0.0
+        gc.collect()
+        gc.disable()
         e2e_clk.mark(True)
         t0 = time.perf_counter()
         d2h = 0
