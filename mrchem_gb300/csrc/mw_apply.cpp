@@ -570,12 +570,14 @@ void screen_setup_inputs(Ctx &ctx, std::vector<ApplyJob> &jobs, const std::vecto
     // read by kernels from the pinned staging: with host inputs these tables go up while the later
     // job groups' input blocks still occupy the copy engines
     k_fetch(d, h, off.back(), ctx.stream);
+    ctx.fetch_launches++;
     // the entries go to their jobs' places in the apply's ScreenJob array (contiguous runs copied
     // together)
     for (size_t q = 0; q < idx.size();) {
         size_t r = q + 1;
         while (r < idx.size() && idx[r] == idx[r - 1] + 1) r++;
         k_fetch(ds.djobs + idx[q], hj + q, sizeof(ScreenJob) * (r - q), ctx.stream);
+        ctx.fetch_launches++;
         q = r;
     }
 }
@@ -911,6 +913,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     const bool dfp = tensor;  // the double-FP32 tier comes with the tensor-core tier
     const bool df_only = precision_mode == MW_PREC_DF;
     auto t_start = std::chrono::steady_clock::now();
+    const long long fetch0 = ctx.fetch_launches;
     Arena &arena = ctx.arena;
     // copies into the arenas that an apply which failed part-way left in flight end first
     if (ctx.ustream) MWG_CUDA(cudaStreamSynchronize(ctx.ustream));
@@ -1622,6 +1625,7 @@ void apply_batch(std::vector<ApplyJob> &jobs, int precision_mode, bool fixed_gri
     for (auto &e : ev_span) cudaEventDestroy(e);
     if (ds.ev_counts) cudaEventDestroy(ds.ev_counts);
     st.kernel_ms += kernel_ms;
+    st.launches += ctx.fetch_launches - fetch0;
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }
 
@@ -1731,6 +1735,7 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
     const Basis &bsis = ctx.basis;
     Arena &arena = ctx.arena;
     auto t_start = std::chrono::steady_clock::now();
+    const long long fetch0 = ctx.fetch_launches;
     using clk = std::chrono::steady_clock;
     auto since = [](clk::time_point t0) { return std::chrono::duration<double, std::milli>(clk::now() - t0).count(); };
     std::vector<MulState> ms(jobs.size());
@@ -2047,6 +2052,7 @@ void multiply_batch(std::vector<MulJob> &jobs, mw_stats &st) {
     auto tF = clk::now();
     compress_batch(outs, arena, &st, true);
     st.gpu_post_ms += since(tF);
+    st.launches += ctx.fetch_launches - fetch0;
     st.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
 }
 

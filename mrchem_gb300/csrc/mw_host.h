@@ -215,6 +215,9 @@ struct Ctx {
     // trees and derive the reduced copies and screening tables from them: their kernels take the
     // next free SM slots beside the other groups' contractions
     cudaStream_t pstream[XGROUPS + 1] = {};
+    // k_fetch launches so far (packs of a few MB, screening tables); the batched apply and multiply
+    // add theirs to their launch counts
+    long long fetch_launches = 0;
     void *h_pinned = nullptr;
     size_t pinned_bytes = 0;
     void *pinned(size_t bytes);

@@ -149,9 +149,10 @@ void Packer::ship(Ctx &ctx, Arena &arena) {
     dev = (char *)arena.alloc(total);
     // packs up to a few MB are read by a kernel, so that they never wait behind bulk copies on the
     // copy engines; larger ones take a copy engine
-    if (total <= ((size_t)4 << 20))
+    if (total <= ((size_t)4 << 20)) {
         k_fetch(dev, h, total, ctx.stream);
-    else
+        ctx.fetch_launches++;
+    } else
         MWG_CUDA(cudaMemcpyAsync(dev, h, total, cudaMemcpyHostToDevice, ctx.stream));
 }
 
