@@ -214,9 +214,11 @@ int mw_apply_batch(int n, const double *precs, mw_tree *outs, mw_op *ops, mw_tre
                    const mw_tree *prec_trees, int max_iter, int abs_prec, int precision_mode);
 /* apply on a fixed output grid (the output's current grid, no refinement) */
 /* mw_tree_upload_batch of the inputs, mw_apply_batch (no precision trees) and, optionally,
- * mw_tree_download_batch of the outputs, with the transfers overlapped: each job group's input
- * blocks go up on the group's stream and the group starts computing once they have landed; each
- * group's outputs go down as soon as its post-processing is queued, beside the other groups' work.
+ * mw_tree_download_batch of the outputs, with the transfers overlapped: the job groups' input
+ * blocks go up on one copy stream in group order while the host builds the input trees, each
+ * group is prepared on its own high-priority stream and starts computing once its blocks have
+ * landed; each group's outputs go down as soon as its post-processing is queued, beside the other
+ * groups' work.
  * in_keys / in_coefs as in mw_tree_upload_batch.  Outputs (out_cap may be NULL for none): per job,
  * buffers for out_cap[i] nodes as mw_tree_download_batch fills them; out_nnodes[i] is the output's
  * node count when they were filled, minus it when the output did not fit or out_coefs[i] is not
