@@ -66,7 +66,6 @@ def run(rows, per_row_barrier, rng, max_steps=20000):
     threads = {"P": producer(), "E": epilogue()}
     parity = {("P", b): 0 for b in bars} | {("E", b): 0 for b in bars}
     current = {t: next(g) for t, g in threads.items()}
-    at_sync = set()
     for _ in range(max_steps):
         if all(a is None for a in current.values()):
             return True
