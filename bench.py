@@ -701,7 +701,7 @@ def run(args):
         tr = dram_per_item.get(tier)
         out["traffic"] = tr * items if tr is not None else None
         out["traffic_unit"] = "DRAM bytes per step, all launches of the kernel" if tr is not None else None
-        # the survey's per-component-pair count (6 K^4 per surviving (ft, gt) pair), kept apart:
+        # the per-component-pair count (6 K^4 per surviving (ft, gt) pair, MRCPP's own unit), kept apart:
         # the cube passes share partial sums across pairs, so this rate can exceed the pipe's peak
         fl = st_ser["flops_" + ("df" if tier == "df32" else tier)]
         out["pair_unit_rate"] = fl / sec / 1e12 if ms > 0 else 0.0
